@@ -1,0 +1,345 @@
+"""Benchmark: FBP of one 2048 x 2048 slice from 1800 views x 2048 rays
+(Ram-Lak filter + slant-stack backprojection), in GUPS = (pixels x views)
+updates per second.
+
+Workload (seeded synthetic, no dataset): 40 random ellipses (centres uniform
+in the unit disk, semi-axes U(0.02, 0.4), angles U(0, pi), densities
+U(0, 1)); transmission sinogram = slant-stack Radon scaled to a maximum
+attenuation of 3, Poisson counts at I0 = 1e4 per ray, -log(counts / I0) with
+counts >= 1.  One step = one rg_fbp call (filter + backprojection) on a
+resident sinogram.  The sinogram (14.7 MB) fits in L2, so L2 is flushed
+(256 MiB write) before every timed step and the step time is the sum of
+per-step CUDA-event intervals.
+
+Also reported: the backprojection kernel alone against the HBM roofline of
+the gather-byte model (8 B per interpolated update + compulsory image and
+sinogram bytes), the end-to-end time of the same call with pinned host
+buffers and both copies inside the timed region, and the reference
+algorithm on the host cores (oracle port, bounded sample).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N, A, R = 2048, 1800, 2048
+METRIC = "FBP GUPS (2048^2 image, 1800 views, 2048 rays; Ram-Lak + slant-stack BP)"
+UNIT = "GUPS"
+UPDATES = N * N * A
+# ncu (dram__bytes_read.sum + dram__bytes_write.sum) of one backprojection
+# launch at this size; profiles/bp_2048x1800_ncu.md.  None until captured.
+BP_TRAFFIC_BYTES = None
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------
+# Clock sampling during the timed region
+
+class Clocks:
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        cmd = ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,"
+               "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+               "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "100"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL,
+                                         text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[3 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+# ----------------------------------------------------------------------------
+# CPU baseline (bounded sample of the same workload on the host cores)
+
+def cpu_fbp_sample(sino_np, kind_ref):
+    """Time the filter on a subset of views and the backprojection on a
+    subset of image rows; scale to the full step.  Returns (est_step_s,
+    sample description, cores, kind)."""
+    import numpy as np
+    from oracle import oracle as O
+    cores = os.cpu_count() or 1
+    rows, views = 64, 96
+    dt = 2.0 / (R - 1)
+    t0 = time.perf_counter()
+    O.ramlak_views(np.ascontiguousarray(sino_np.T), dt, views, threads=cores)
+    t_filter = (time.perf_counter() - t0) * (A / views)
+    t0 = time.perf_counter()
+    O.backprojection_rows(sino_np, N, N // 2 - rows // 2, N // 2 + rows // 2, threads=cores)
+    t_bp = (time.perf_counter() - t0) * (N / rows)
+    sample = (f"FP64 oracle port of raft_backprojection_slantstack on {rows} of {N} image "
+              f"rows and the Ram-Lak convolution on {views} of {A} views, each scaled to the "
+              f"full 2048^2 x 1800 step")
+    return t_filter + t_bp, sample, cores, "port"
+
+
+# ----------------------------------------------------------------------------
+
+def make_sinogram(torch, rg, seed):
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    desc = rg.random_ellipses(40, rng)
+    ph = rg.phantom_fromdesc((N, N), desc, device=True)
+    # slant-stack rows are bottom-up: flip the top-down raster
+    ph = rg.gpu_image(torch.flip(ph.data, dims=[0]).contiguous())
+    p = rg.radon(ph, (R, A), rg.radon_method.SLANTSTACK)
+    mu = 3.0 / float(p.data.max())
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    counts = torch.poisson(1e4 * torch.exp(-p.data * mu), generator=gen).clamp_(min=1.0)
+    s = -torch.log(counts / 1e4)
+    return s.contiguous()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+    warm = max(3, args.warmup)
+
+    if args.impl == "reference":
+        return reference_arm(args, rank, world, warm)
+
+    import numpy as np
+    import torch
+    import pyraft_gb300 as rg
+    from pyraft_gb300 import _native
+    from pyraft_gb300.raftypes import rg_image
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    L = _native.load()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    sino = make_sinogram(torch, rg, 1234 + rank)                  # (R, A) rays x views
+    img = torch.zeros((N, N), dtype=torch.float32, device="cuda")
+    S = rg_image(rg.gpu_image(sino, (0.0, 1.0), (math.pi, -1.0)))
+    I = rg_image(rg.gpu_image(img))
+    ws_bytes = L.rg_fbp_workspace(S, I, _native.RG_FILTER_RAMLAK)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        _native.check(L.rg_fbp(S, I, _native.RG_FILTER_RAMLAK, ws.data_ptr(), ws_bytes, sp))
+
+    for _ in range(warm):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        step()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+    value = world * UPDATES / (ms * 1e-3) / 1e9
+
+    # ---- backprojection kernel alone (roofline of the dominant kernel)
+    filt_am = torch.empty((A, R), dtype=torch.float32, device="cuda")
+    FA = rg_image(rg.gpu_image(filt_am.t(), (0.0, 1.0), (math.pi, -1.0)))   # view-major view
+    FS = rg_image(rg.gpu_image(sino, (0.0, 1.0), (math.pi, -1.0)))
+    fws = L.rg_filter_workspace(FS, _native.RG_FILTER_RAMLAK)
+    fwsb = torch.empty(fws, dtype=torch.uint8, device="cuda")
+    _native.check(L.rg_filter(FS, FA, _native.RG_FILTER_RAMLAK, fwsb.data_ptr(), fws, sp))
+    assert L.rg_backprojection_slantstack_workspace(FA, I) == 0
+    bp_ms = []
+    for k in range(warm + args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        _native.check(L.rg_backprojection_slantstack(FA, I, None, 0, sp))
+        b.record(stream)
+        b.synchronize()
+        if k >= warm:
+            bp_ms.append(a.elapsed_time(b))
+    bp_ms = statistics.mean(bp_ms)
+    compulsory = N * N * 4 + R * A * 4
+    alg_bytes = 8 * UPDATES + compulsory
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (bp_ms * 1e-3) / 1e9
+
+    # ---- end to end: pinned host sinogram in, image out, through rg_fbp
+    h_in = torch.empty((R, A), dtype=torch.float32).pin_memory()
+    h_in.copy_(sino.cpu())
+    h_out = torch.empty((N, N), dtype=torch.float32).pin_memory()
+    d_in = torch.empty_like(sino)
+    d_out = torch.empty_like(img)
+    S2 = rg_image(rg.gpu_image(d_in, (0.0, 1.0), (math.pi, -1.0)))
+    I2 = rg_image(rg.gpu_image(d_out))
+
+    def e2e_step():
+        d_in.copy_(h_in, non_blocking=True)
+        _native.check(L.rg_fbp(S2, I2, _native.RG_FILTER_RAMLAK, ws.data_ptr(), ws_bytes, sp))
+        h_out.copy_(d_out, non_blocking=True)
+
+    for _ in range(warm):
+        e2e_step()
+    torch.cuda.synchronize()
+    e_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e2e_step()
+        b.record(stream)
+        b.synchronize()
+        e_ms.append(a.elapsed_time(b))
+    e_ms = statistics.mean(e_ms)
+    if dist:
+        t = torch.tensor([e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e_ms = float(t)
+    ok = bool(torch.isfinite(h_out).all())
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": warm, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded random-ellipse transmission sinogram, Poisson I0=1e4)",
+        "config": {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
+                               "slant-stack backprojection, one slice per GPU",
+                   "image": N, "views": A, "rays": R, "filter": "ramlak",
+                   "l2": "flushed (256 MiB write) before every timed step; step time = sum "
+                         "of per-step CUDA-event intervals",
+                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "e2e": {"value": round(world * UPDATES / (e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
+                "h2d_bytes_per_step": R * A * 4, "d2h_bytes_per_step": N * N * 4,
+                "ms_per_step": round(e_ms, 4), "api": "rg_fbp (C ABI), pinned host buffers",
+                "finite": ok},
+        "roofline": {"bound": "hbm", "kernel": "k_gather<0> (backprojection)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 3), "traffic": BP_TRAFFIC_BYTES,
+                     "algorithmic_bytes": alg_bytes, "kernel_ms": round(bp_ms, 4),
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                     "model": "8 B per (pixel, view) update + image and sinogram bytes once"},
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+        "wall_s_timed_region": round(wall, 3),
+    }
+    if rank == 0:
+        t_cpu, sample, cores, kind = cpu_fbp_sample(h_in.numpy().astype(np.float64), False)
+        line["cpu_baseline"] = {"value": round(UPDATES / t_cpu / 1e9, 4), "unit": UNIT,
+                                "cores": cores, "kind": kind, "sample": sample,
+                                "est_s_per_step": round(t_cpu, 2)}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def reference_arm(args, rank, world, warm):
+    """The reference's CPU algorithm on the host cores (compiled reference if
+    present, else the oracle port), same metric and config, bounded sample
+    per step.  Under torchrun only rank 0 works."""
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle as O
+    rng = np.random.default_rng(1234)
+    sino = rng.random((R, A))
+    steps = []
+    for k in range(warm + args.steps):
+        t, sample, cores, kind = cpu_fbp_sample(sino, True)
+        if k >= warm:
+            steps.append(t)
+    t = statistics.mean(steps)
+    v = UPDATES / t / 1e9
+    print(json.dumps({
+        "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": warm, "ms_per_step": round(t * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "impl": "reference",
+        "config": {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
+                               "slant-stack backprojection", "image": N, "views": A, "rays": R},
+        "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,203 @@
+/*
+ * raftgb.h -- C ABI of libraftgb.so, the GB300 (sm_103a) implementation of
+ * pyraft's reconstruction hot path: slant-stack Radon, its backprojection and
+ * matched adjoint, the DDA (Bresenham) projector pair, the ramp filter step,
+ * and the EM/OSEM multiplicative update.
+ *
+ * Conventions shared by every entry point
+ *  - Images and sinograms are passed as rg_image, which mirrors the
+ *    reference's raft_image (raft/raft_image.h:11-19, raft/raft_matrix.h:
+ *    11-19, marshalled by pyraft/raftypes.py:85-100,413-449): element (i, j)
+ *    lives at data[i * column_stride + j * line_stride]; tl_/br_ give the
+ *    top-left / bottom-right corners.  Sinograms are (nrays x nviews): line =
+ *    ray, column = view, as in raft/raft_radon_slantstack.c:114.  Unlike the
+ *    reference (host double*), data is a DEVICE float* owned by the caller.
+ *  - The reference passes `int nthreads` and blocks; here every operator
+ *    takes a CUDA stream (cudaStream_t passed as void*, NULL = legacy default
+ *    stream) and returns as soon as the work is queued.
+ *  - Scratch: operators need device scratch memory.  Pass `workspace` /
+ *    `workspace_bytes` (size from the matching *_workspace query), or
+ *    workspace == NULL to let the call take stream-ordered memory from the
+ *    device's default pool (cudaMallocAsync/cudaFreeAsync on `stream`).
+ *  - Every entry point returns RG_OK (0) or a negative RG_E* code; the text
+ *    of the last error on the calling thread is available from
+ *    rg_last_error().  The reference reports no errors at all (its
+ *    allocation failures silently return, raft/raft_filter.cpp:131-133).
+ *  - Nothing here calls cudaDeviceReset (the reference's GPU wrappers do,
+ *    raft/raft_radon_gpu.cu:34) and no call synchronises the device, except
+ *    the *_host convenience wrappers, which return when their result is in
+ *    host memory.
+ *  - Plans: per-view constants are computed on the host in FP64 (with the
+ *    host libm, the same cos/sin/tan the reference evaluates) and uploaded
+ *    once per geometry.  The rg_image entry points keep a small per-device
+ *    cache of plans keyed by geometry; the rg_plan_* entry points expose
+ *    them for CUDA-graph capture and batching.
+ */
+#ifndef RAFTGB_H
+#define RAFTGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_OK            0
+#define RG_EINVAL       -1   /* bad size, stride, corner or pointer         */
+#define RG_ECUDA        -2   /* a CUDA runtime call or kernel launch failed */
+#define RG_ENOMEM       -3   /* device or host allocation failed            */
+#define RG_EUNSUPPORTED -4   /* geometry outside what the kernels handle    */
+#define RG_EWORKSPACE   -5   /* workspace smaller than the query returned   */
+
+typedef struct {
+    float *data;          /* device pointer                                  */
+    int lines;            /* rows                                            */
+    int line_stride;      /* distance between elements of one row (floats)   */
+    int columns;          /* columns                                         */
+    int column_stride;    /* distance between rows (floats)                  */
+    double tl_x, tl_y;    /* top-left corner                                 */
+    double br_x, br_y;    /* bottom-right corner                             */
+} rg_image;
+
+/* Method ids, as raft/raft_enums.h:4-9 and pyraft/sinogram/sino.py:159-167. */
+#define RG_BRESENHAM  1
+#define RG_SLANTSTACK 2
+
+/* Text of the last error on this thread ("" if none). */
+const char *rg_last_error(void);
+/* ABI version (major * 100 + minor). */
+int rg_version(void);
+
+/* ----------------------------------------------------------------------
+ * Slant-stack projector family (square images).
+ * -------------------------------------------------------------------- */
+
+/* Radon transform, ray-driven line integral with linear interpolation.
+ * Replaces raft_radon_slantstack (raft/raft_radon_slantstack.c:44,
+ * declared raft/raft_radon_slantstack.h:10; bound at pyraft/raftypes.py:159).
+ * phantom: size x size; radon: nrays x nviews.                              */
+size_t rg_radon_slantstack_workspace(rg_image phantom, rg_image radon);
+int rg_radon_slantstack(rg_image phantom, rg_image radon,
+                        void *workspace, size_t workspace_bytes, void *stream);
+
+/* Pixel-driven backprojection with linear interpolation in t, scaled by
+ * the view spacing.  Replaces raft_backprojection_slantstack
+ * (raft/raft_backprojection_slantstack.c:43; bound at pyraft/raftypes.py:161).
+ * Not the transpose of rg_radon_slantstack, exactly like the reference.    */
+size_t rg_backprojection_slantstack_workspace(rg_image sinogram, rg_image backprojection);
+int rg_backprojection_slantstack(rg_image sinogram, rg_image backprojection,
+                                 void *workspace, size_t workspace_bytes, void *stream);
+
+/* Matched adjoint: the exact transpose of rg_radon_slantstack (the
+ * reference has none; pyraft's radon_transpose offers only the DDA pair,
+ * pyraft/backprojection/backprojection.py:220-233).  Backward pass of the
+ * autograd Radon and backprojector of the EM/OSEM update.                   */
+size_t rg_radon_transpose_slantstack_workspace(rg_image sinogram, rg_image image);
+int rg_radon_transpose_slantstack(rg_image sinogram, rg_image image,
+                                  void *workspace, size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------------------------------
+ * DDA (Bresenham) projector pair (rectangular images, top-down rows).
+ * -------------------------------------------------------------------- */
+
+/* Replaces raft_radon_bresenham (raft/raft_radon_bresenham.cpp:63;
+ * bound at pyraft/raftypes.py:152).                                         */
+size_t rg_radon_bresenham_workspace(rg_image image, rg_image sino);
+int rg_radon_bresenham(rg_image image, rg_image sino,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* Replaces raft_radon_transpose_bresenham
+ * (raft/raft_radon_transpose_bresenham.cpp:97; bound at pyraft/raftypes.py:156). */
+size_t rg_radon_transpose_bresenham_workspace(rg_image sino, rg_image image);
+int rg_radon_transpose_bresenham(rg_image sino, rg_image image,
+                                 void *workspace, size_t workspace_bytes, void *stream);
+
+/* Pixel index sequences of a list of rays, for checking the traversal:
+ * replaces stepping raft_ddaiterator_set_theta/_set_t/_update/_end
+ * (raft/raft_ddaiterator.h:26-33) by hand.  thetas, ts: nrays_in HOST
+ * doubles (cos/sin are taken on the host, as the reference does);
+ * out_i/out_j/out_sigma: nrays_in * cap DEVICE entries (ray r at offset
+ * r*cap); out_count: nrays_in device ints (full step counts).  Synchronous. */
+int rg_dda_trace(int lines, int columns, const double img_corners[4],
+                 const double *thetas, const double *ts, int nrays_in, int cap,
+                 int *out_i, int *out_j, double *out_sigma, int *out_count,
+                 void *stream);
+
+/* ----------------------------------------------------------------------
+ * Ramp filter step of FBP: row-wise spatial convolution along t.
+ * kind RG_FILTER_RAMLAK: discrete Ram-Lak kernel, linear convolution,
+ *   q[n] = dt * sum_k h[n-k] p[k], h[0] = 1/(4dt^2), h[odd m] =
+ *   -1/(pi^2 m^2 dt^2) (replaces the FFT ramp of raft_filter1d_ramp,
+ *   raft/raft_filter.cpp:184, bound at pyraft/raftypes.py:185).
+ * kind RG_FILTER_LOWPASS: the cosine-windowed ramp of pyraft's
+ *   lowpassino_fbp (pyraft/filters/filters.py:13-68), applied as the
+ *   equivalent circular convolution.
+ * in and out: nrays x nviews; may be the same image.                        */
+#define RG_FILTER_RAMLAK  1
+#define RG_FILTER_LOWPASS 2
+size_t rg_filter_workspace(rg_image sino, int kind);
+int rg_filter(rg_image sino_in, rg_image sino_out, int kind,
+              void *workspace, size_t workspace_bytes, void *stream);
+
+/* FBP: filter + slant-stack backprojection (replaces raft_fbp,
+ * raft/raft_fbp.c:5-24, and pyraft's fbp_gpu, pyraft/inversion/inversion.py:32). */
+size_t rg_fbp_workspace(rg_image sino, rg_image image, int kind);
+int rg_fbp(rg_image sino, rg_image image, int kind,
+           void *workspace, size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------------------------------
+ * EM / OSEM (emission MLEM, x <- x * A^T(y / Ax) / A^T 1).
+ * Replaces raft_em_gpu (raft/raft_em_gpu.cu:20, bound at
+ * pyraft/raftypes.py:211) and pyraft's make_em/em
+ * (pyraft/iterative/em.py:109-169).  image holds x0 on entry and the
+ * iterate on return.  method RG_SLANTSTACK uses the slant-stack Radon with
+ * its matched adjoint; RG_BRESENHAM the DDA pair, as pyraft's em().
+ * nsubsets == 1 is plain EM; > 1 is OSEM over interleaved view subsets
+ * (subset s = views s, s+S, s+2S, ...).  Guards: y/0 -> 0, and pixels with
+ * zero sensitivity are set to 0 (the reference divides by zero).
+ * The sensitivity A^T 1 is accumulated in FP64.                             */
+size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets);
+int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets,
+          void *workspace, size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------------------------------
+ * Batched uneven OSEM: nslices independent reconstructions of different
+ * sizes and view counts in one persistent launch per sub-iteration over a
+ * (slice, tile) work queue.  Each slice s reads sinos[s] and updates
+ * images[s] in place.  Work runs on `stream`; with graph != 0 the
+ * iterations are captured once into a CUDA graph and replayed.           */
+size_t rg_osem_batch_workspace(const rg_image *sinos, const rg_image *images,
+                               int nslices, int nsubsets);
+int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices,
+                  int niter, int nsubsets, int graph,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
+/* ----------------------------------------------------------------------
+ * Ellipse phantoms (test inputs; replace raft_image_phantom_fromdesc,
+ * raft/raft_image_phantom_fromdesc.c:4, and raft_radon_fromdesc,
+ * raft/raft_radon_fromdesc.c:4).  desc: host (n x 6) row-major doubles
+ * [alpha, a, b, x0, y0, theta]; results are ADDED into image / sino.         */
+int rg_phantom_fromdesc(rg_image image, const double *desc, int n, void *stream);
+int rg_radon_fromdesc(rg_image sino, const double *desc, int n, void *stream);
+
+/* ----------------------------------------------------------------------
+ * Host-pointer convenience wrappers, the shape of the reference's GPU entry
+ * points (raft/raft_radon_gpu.h:8, raft/raft_backprojection_gpu.h:8,
+ * raft/raft_em_gpu.cu:20): float host buffers, default [-1,1]^2 image, views
+ * on [0, pi) and rays on [-1, 1]; allocate, copy, run, copy back, free.
+ * Unlike the reference they return a status and do not reset the device.
+ * The backprojection wrapper computes the C slant-stack backprojection
+ * (not the reference GPU kernel's nearest-sample, x-flipped variant).       */
+int rg_radon_slantstack_host(float *h_output, const float *h_input,
+                             int size_image, int nrays, int nangles);
+int rg_backprojection_slantstack_host(float *h_image, const float *h_sino,
+                                      int size_image, int nrays, int nangles);
+int rg_em_host(float *h_output, const float *h_sino, int size_image,
+               int nrays, int nangles, int niter);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RAFTGB_H */

@@ -104,6 +104,30 @@ def backprojection_slantstack(sino, size, img_corners=IMG_CORNERS,
     return out
 
 
+def backprojection_rows(sino, size, row0, row1, img_corners=IMG_CORNERS,
+                        sino_corners=SINO_CORNERS, threads=None):
+    """Rows [row0, row1) of backprojection_slantstack (CPU timing sample)."""
+    sino = np.ascontiguousarray(sino, dtype=np.float64)
+    out = np.zeros((size, size))
+    I, S = _img(out, img_corners), _img(sino, sino_corners)
+    lib().orc_backprojection_slantstack_rows(ctypes.byref(S), ctypes.byref(I), ctypes.c_int(row0),
+                                             ctypes.c_int(row1),
+                                             ctypes.c_int(threads or nthreads()))
+    return out
+
+
+def ramlak_views(sino, dt, nv, threads=None):
+    """Ram-Lak of the first nv views only (CPU timing sample)."""
+    sino = np.ascontiguousarray(sino, dtype=np.float64)
+    out = np.zeros_like(sino)
+    rc = lib().orc_ramlak_views(sino.ctypes.data_as(_dp), out.ctypes.data_as(_dp),
+                                ctypes.c_int(sino.shape[0]), ctypes.c_int(sino.shape[1]),
+                                ctypes.c_int(nv), ctypes.c_double(dt),
+                                ctypes.c_int(threads or nthreads()))
+    assert rc == 0
+    return out
+
+
 def radon_bresenham(img, nrays, nviews, img_corners=IMG_CORNERS,
                     sino_corners=SINO_CORNERS, threads=None):
     """restates raft/raft_radon_bresenham.cpp:16-105"""

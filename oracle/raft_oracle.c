@@ -264,6 +264,22 @@ void orc_backprojection_slantstack(const orc_img *sino, orc_img *img, int nthrea
     orc_parallel(img->lines * img->lines, nthreads, ss_bp_body, &c);
 }
 
+/* Rows [row0, row1) only (a bounded sample for CPU timing). */
+typedef struct { bp_ctx c; int off; } bp_rows_ctx;
+
+static void ss_bp_rows_body(void *vctx, int lo, int hi, int worker)
+{
+    bp_rows_ctx *r = (bp_rows_ctx *)vctx;
+    ss_bp_body(&r->c, lo + r->off, hi + r->off, worker);
+}
+
+void orc_backprojection_slantstack_rows(const orc_img *sino, orc_img *img, int row0, int row1,
+                                        int nthreads)
+{
+    bp_rows_ctx r = {{sino, img}, row0 * img->lines};
+    orc_parallel((row1 - row0) * img->lines, nthreads, ss_bp_rows_body, &r);
+}
+
 /* ------------------------------------------------------------------------ */
 /* DDA (Bresenham-like) pixel walk.  Restates raft_ddaiterator
  * (raft/raft_ddaiterator.c:16-257, struct raft/raft_ddaiterator.h:10-47):
@@ -630,6 +646,19 @@ void orc_ramlak_taps(double *taps, int R, double dt)
         else h = -1.0 / (pi * pi * (double)m * (double)m * dt * dt);
         taps[m + R - 1] = h * dt;
     }
+}
+
+/* Ram-Lak on the first `nv` views only (a bounded sample for CPU timing). */
+int orc_ramlak_views(const double *in, double *out, int R, int V, int nv, double dt,
+                     int nthreads)
+{
+    double *taps = (double *)malloc((size_t)(2 * R - 1) * sizeof(double));
+    if (!taps) return -1;
+    orc_ramlak_taps(taps, R, dt);
+    rl_ctx c = {in, out, R, V, dt, taps, 0};
+    orc_parallel(nv, nthreads, conv_body, &c);
+    free(taps);
+    return 0;
 }
 
 int orc_ramlak(const double *in, double *out, int R, int V, double dt, int nthreads)

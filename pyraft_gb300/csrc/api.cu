@@ -1,0 +1,725 @@
+// api.cu -- the C ABI of libraftgb (declared in include/raftgb.h).
+//
+// Each entry point validates its rg_image arguments, looks up (or builds and
+// caches) the plan of per-view constants for the geometry, takes its scratch
+// from the caller's workspace or from stream-ordered memory, and queues the
+// kernels on the caller's stream.  No entry point synchronises, except the
+// *_host wrappers and rg_dda_trace.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <complex>
+#include <list>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "rg_internal.cuh"
+
+namespace rg {
+
+// ----------------------------------------------------------------------------
+// Errors
+
+static thread_local std::string g_err;
+
+int set_error(int code, const char *fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+int cuda_error(cudaError_t e, const char *what)
+{
+    return set_error(RG_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+// ----------------------------------------------------------------------------
+// Scratch
+
+int scratch_begin(Scratch &s, void *ws, size_t ws_bytes, size_t need, cudaStream_t st)
+{
+    s.stream = st;
+    s.off = 0;
+    s.owned = false;
+    s.base = nullptr;
+    s.size = 0;
+    if (need == 0) return RG_OK;
+    if (ws) {
+        if (((uintptr_t)ws & 255) != 0)
+            return set_error(RG_EINVAL, "workspace must be 256-byte aligned");
+        if (ws_bytes < need)
+            return set_error(RG_EWORKSPACE, "workspace of %zu bytes, %zu needed", ws_bytes, need);
+        s.base = (char *)ws;
+        s.size = ws_bytes;
+        return RG_OK;
+    }
+    cudaError_t e = cudaMallocAsync((void **)&s.base, need, st);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(RG_ENOMEM, "stream-ordered allocation of %zu bytes failed: %s", need,
+                         cudaGetErrorString(e));
+    }
+    s.size = need;
+    s.owned = true;
+    return RG_OK;
+}
+
+void scratch_end(Scratch &s)
+{
+    if (s.owned && s.base) cudaFreeAsync(s.base, s.stream);
+    s.base = nullptr;
+    s.owned = false;
+}
+
+// Sum of pieces as Scratch::take lays them out.
+static size_t ws_total(std::initializer_list<size_t> pieces)
+{
+    size_t t = 0;
+    for (size_t p : pieces) t = Scratch::align(t) + p;
+    return t ? Scratch::align(t) : 0;
+}
+
+// ----------------------------------------------------------------------------
+// Caches (per device, keyed by the raw bytes of the geometry).
+
+template <class T>
+struct Cache {
+    std::mutex mu;
+    std::list<std::pair<std::string, std::shared_ptr<T>>> items;   // MRU first
+    size_t cap = 64;
+    std::shared_ptr<T> find(const std::string &k)
+    {
+        for (auto it = items.begin(); it != items.end(); ++it)
+            if (it->first == k) {
+                items.splice(items.begin(), items, it);
+                return items.front().second;
+            }
+        return nullptr;
+    }
+    void put(const std::string &k, std::shared_ptr<T> v)
+    {
+        items.emplace_front(k, std::move(v));
+        while (items.size() > cap) items.pop_back();
+    }
+};
+
+struct KeyBuilder {
+    std::string s;
+    template <class T> KeyBuilder &add(const T &v)
+    {
+        s.append(reinterpret_cast<const char *>(&v), sizeof v);
+        return *this;
+    }
+};
+
+static int current_device()
+{
+    int d = 0;
+    cudaGetDevice(&d);
+    return d;
+}
+
+struct PlanHolder {
+    SSPlan p;
+    ~PlanHolder() { ss_plan_free(p); }
+};
+
+static Cache<PlanHolder> g_plans;
+
+// Plan over views {first, first + stride, ...} of the geometry.
+static int get_plan(const SSGeom &g, int stride, int first, std::shared_ptr<PlanHolder> &out)
+{
+    KeyBuilder kb;
+    kb.add(current_device()).add(g.N).add(g.R).add(g.A).add(g.itl_x).add(g.itl_y).add(g.ibr_x)
+        .add(g.ibr_y).add(g.stl_x).add(g.stl_y).add(g.sbr_x).add(g.sbr_y).add(stride).add(first);
+    std::lock_guard<std::mutex> lock(g_plans.mu);
+    out = g_plans.find(kb.s);
+    if (out) return RG_OK;
+    std::vector<int> views;
+    for (int j = first; j < g.A; j += stride) views.push_back(j);
+    auto h = std::make_shared<PlanHolder>();
+    int rc = ss_plan_build(h->p, g, views.data(), (int)views.size());
+    if (rc != RG_OK) return rc;
+    g_plans.put(kb.s, h);
+    out = h;
+    return RG_OK;
+}
+
+struct DevTable {
+    void *p = nullptr;
+    ~DevTable() { if (p) cudaFree(p); }
+};
+static Cache<DevTable> g_tables;
+
+// Device copy of a host table, cached by key.
+static int get_table(const std::string &key, const void *host, size_t bytes,
+                     std::shared_ptr<DevTable> &out)
+{
+    KeyBuilder kb;
+    kb.add(current_device());
+    kb.s += key;
+    std::lock_guard<std::mutex> lock(g_tables.mu);
+    out = g_tables.find(kb.s);
+    if (out) return RG_OK;
+    auto t = std::make_shared<DevTable>();
+    RG_CK(cudaMalloc(&t->p, bytes));
+    RG_CK(cudaMemcpy(t->p, host, bytes, cudaMemcpyHostToDevice));
+    g_tables.put(kb.s, t);
+    out = t;
+    return RG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// Validation helpers
+
+static int check_image(const rg_image &im, const char *what)
+{
+    if (!im.data) return set_error(RG_EINVAL, "%s: null data pointer", what);
+    if (im.lines < 1 || im.columns < 1)
+        return set_error(RG_EINVAL, "%s: empty (%d x %d)", what, im.lines, im.columns);
+    if (im.line_stride == 0 || im.column_stride == 0)
+        return set_error(RG_EINVAL, "%s: zero stride", what);
+    if (!(std::isfinite(im.tl_x) && std::isfinite(im.tl_y) && std::isfinite(im.br_x) &&
+          std::isfinite(im.br_y)))
+        return set_error(RG_EINVAL, "%s: non-finite corner", what);
+    return RG_OK;
+}
+
+static SSGeom ss_geom(const rg_image &img, const rg_image &sino)
+{
+    SSGeom g;
+    g.N = img.lines;
+    g.itl_x = img.tl_x; g.itl_y = img.tl_y; g.ibr_x = img.br_x; g.ibr_y = img.br_y;
+    g.R = sino.lines;
+    g.A = sino.columns;
+    g.stl_x = sino.tl_x; g.stl_y = sino.tl_y; g.sbr_x = sino.br_x; g.sbr_y = sino.br_y;
+    return g;
+}
+
+static int check_ss(const rg_image &img, const rg_image &sino)
+{
+    int rc;
+    if ((rc = check_image(img, "image")) != RG_OK) return rc;
+    if ((rc = check_image(sino, "sinogram")) != RG_OK) return rc;
+    if (img.lines != img.columns)
+        return set_error(RG_EINVAL, "slant-stack images are square (got %d x %d)", img.lines,
+                         img.columns);
+    if (img.lines < 2 || sino.lines < 2)
+        return set_error(RG_EINVAL, "slant-stack needs size >= 2 and nrays >= 2");
+    return RG_OK;
+}
+
+int check_ws(const void *ws)
+{
+    if (ws && ((uintptr_t)ws & 255) != 0)
+        return set_error(RG_EINVAL, "workspace must be 256-byte aligned");
+    return RG_OK;
+}
+
+static bool is_view_major(const rg_image &s)
+{
+    return s.column_stride == 1 && s.line_stride == s.lines;
+}
+
+// Helpers for em.cu: hand out plans with an opaque owner handle
+// (a heap-allocated std::shared_ptr<void>, released by release_holder).
+int get_ss_plan(const SSGeom &g, int stride, int first, const SSPlan **out, void **holder)
+{
+    std::shared_ptr<PlanHolder> ph;
+    int rc = get_plan(g, stride, first, ph);
+    if (rc) return rc;
+    *out = &ph->p;
+    *holder = new std::shared_ptr<void>(ph);
+    return RG_OK;
+}
+
+void release_holder(void *holder)
+{
+    delete static_cast<std::shared_ptr<void> *>(holder);
+}
+
+size_t ws_sum(std::initializer_list<size_t> pieces) { return ws_total(pieces); }
+
+}  // namespace rg
+
+using namespace rg;
+
+// ============================================================================
+// C ABI
+
+extern "C" {
+
+const char *rg_last_error(void) { return g_err.c_str(); }
+int rg_version(void) { return 100; }
+
+// ---------------------------------------------------------------- Radon
+size_t rg_radon_slantstack_workspace(rg_image phantom, rg_image radon)
+{
+    const int N = phantom.lines;
+    return ws_total({radon_pairs_bytes(N), radon_pairs_bytes(N),
+                     (size_t)radon.lines * radon.columns * sizeof(float)});
+}
+
+int rg_radon_slantstack(rg_image phantom, rg_image radon, void *ws, size_t wsb, void *stream)
+{
+    int rc = check_ss(phantom, radon);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(phantom, radon), 1, 0, ph))) return rc;
+    const int N = phantom.lines, R = radon.lines, A = radon.columns;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_radon_slantstack_workspace(phantom, radon), st))) return rc;
+    float2 *prow = (float2 *)s.take(radon_pairs_bytes(N));
+    float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N));
+    float *out_am = (float *)s.take((size_t)R * A * sizeof(float));
+    const bool direct = is_view_major(radon);
+    if (!(rc = launch_line_pairs(phantom.data, phantom.column_stride, phantom.line_stride, N,
+                                 prow, pcol, st)))
+        rc = launch_radon(ph->p, prow, pcol, direct ? radon.data : out_am, R, nullptr, 0, st);
+    if (!rc && !direct)
+        rc = launch_from_am(out_am, R, A, radon.data, radon.column_stride, radon.line_stride, st);
+    scratch_end(s);
+    return rc;
+}
+
+// ---------------------------------------------------------------- gathers
+static size_t gather_ws(const rg_image &sino)
+{
+    return is_view_major(sino) ? 0 : ws_total({(size_t)sino.lines * sino.columns * sizeof(float)});
+}
+
+static int run_gather(int mode, rg_image sino, rg_image img, void *ws, size_t wsb, void *stream)
+{
+    int rc = check_ss(img, sino);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(img, sino), 1, 0, ph))) return rc;
+    const int R = sino.lines, A = sino.columns;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, gather_ws(sino), st))) return rc;
+    const float *s_am = sino.data;
+    if (!is_view_major(sino)) {
+        float *t = (float *)s.take((size_t)R * A * sizeof(float));
+        rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, t, st);
+        s_am = t;
+    }
+    if (!rc)
+        rc = launch_gather(ph->p, mode, s_am, R, img.data, img.column_stride, img.line_stride,
+                           nullptr, nullptr, nullptr, st);
+    scratch_end(s);
+    return rc;
+}
+
+size_t rg_backprojection_slantstack_workspace(rg_image sino, rg_image bp)
+{
+    (void)bp;
+    return gather_ws(sino);
+}
+
+int rg_backprojection_slantstack(rg_image sino, rg_image bp, void *ws, size_t wsb, void *stream)
+{
+    return run_gather(0, sino, bp, ws, wsb, stream);
+}
+
+size_t rg_radon_transpose_slantstack_workspace(rg_image sino, rg_image img)
+{
+    (void)img;
+    return gather_ws(sino);
+}
+
+int rg_radon_transpose_slantstack(rg_image sino, rg_image img, void *ws, size_t wsb, void *stream)
+{
+    return run_gather(1, sino, img, ws, wsb, stream);
+}
+
+// ---------------------------------------------------------------- filters
+static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable> &out)
+{
+    const int R = sino.lines;
+    const double tmin = sino.br_y, tmax = sino.tl_y;
+    const double dt = (tmax - tmin) / (R - 1);
+    if (!(std::isfinite(dt)) || dt == 0.0) return set_error(RG_EINVAL, "degenerate t extent");
+    KeyBuilder kb;
+    kb.add(kind).add(R).add(tmin).add(tmax);
+    std::vector<float> taps(2 * (size_t)R - 1);
+    if (kind == RG_FILTER_RAMLAK) {
+        const double pi = 3.14159265358979323846;
+        for (int m = -(R - 1); m <= R - 1; ++m) {
+            double h;
+            if (m == 0) h = 1.0 / (4.0 * dt * dt);
+            else if (m % 2 == 0) h = 0.0;
+            else h = -1.0 / (pi * pi * (double)m * (double)m * dt * dt);
+            taps[m + R - 1] = (float)(h * dt);
+        }
+    } else if (kind == RG_FILTER_LOWPASS) {
+        // g = Re(ifft(fftshift(|w| cos(pi w dt)))), w = linspace(-wc, wc, R), wc = 1/(2 dt):
+        // applying g by circular convolution equals the FFT filter of
+        // pyraft/filters/filters.py:13-68 (real part of the filtered data).
+        const double pi = 3.14159265358979323846;
+        const double wc = 1.0 / (2.0 * dt);
+        std::vector<double> h(R), G(R), g(R), ctab(R);
+        const double step = (R > 1) ? (2.0 * wc) / (R - 1) : 0.0;
+        for (int i = 0; i < R; ++i) {
+            double w = (i == R - 1) ? wc : -wc + i * step;
+            h[i] = fabs(w) * cos(pi * w * dt);
+        }
+        const int sh = R / 2;              // fftshift: G[k] = h[(k + R/2) mod R]... numpy
+        for (int k = 0; k < R; ++k) G[k] = h[(k + (R - sh)) % R];
+        for (int k = 0; k < R; ++k) ctab[k] = cos(2.0 * pi * (double)k / (double)R);
+        for (int m = 0; m < R; ++m) {
+            double acc = 0.0;
+            for (int k = 0; k < R; ++k) acc += G[k] * ctab[(size_t)k * m % R];
+            g[m] = acc / R;
+        }
+        for (int m = -(R - 1); m <= R - 1; ++m) taps[m + R - 1] = (float)g[((m % R) + R) % R];
+    } else {
+        return set_error(RG_EINVAL, "unknown filter kind %d", kind);
+    }
+    return get_table(std::string("taps") + kb.s, taps.data(), taps.size() * sizeof(float), out);
+}
+
+size_t rg_filter_workspace(rg_image sino, int kind)
+{
+    (void)kind;
+    const size_t b = (size_t)sino.lines * sino.columns * sizeof(float);
+    return ws_total({b, b});
+}
+
+int rg_filter(rg_image in, rg_image out, int kind, void *ws, size_t wsb, void *stream)
+{
+    int rc;
+    if ((rc = check_image(in, "input sinogram")) || (rc = check_image(out, "output sinogram")))
+        return rc;
+    if (in.lines != out.lines || in.columns != out.columns)
+        return set_error(RG_EINVAL, "filter input and output shapes differ");
+    if (in.lines < 2) return set_error(RG_EINVAL, "filter needs nrays >= 2");
+    if ((rc = check_ws(ws))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::shared_ptr<DevTable> taps;
+    if ((rc = filter_taps(in, kind, taps))) return rc;
+    const int R = in.lines, A = in.columns;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_filter_workspace(in, kind), st))) return rc;
+    float *a = (float *)s.take((size_t)R * A * sizeof(float));
+    float *b = (float *)s.take((size_t)R * A * sizeof(float));
+    if (!(rc = launch_to_am(in.data, in.column_stride, in.line_stride, R, A, a, st)) &&
+        !(rc = launch_conv_rows(a, b, R, A, (const float *)taps->p, st)))
+        rc = launch_from_am(b, R, A, out.data, out.column_stride, out.line_stride, st);
+    scratch_end(s);
+    return rc;
+}
+
+size_t rg_fbp_workspace(rg_image sino, rg_image image, int kind)
+{
+    (void)image;
+    return rg_filter_workspace(sino, kind);
+}
+
+int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *stream)
+{
+    int rc = check_ss(image, sino);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::shared_ptr<DevTable> taps;
+    if ((rc = filter_taps(sino, kind, taps))) return rc;
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(image, sino), 1, 0, ph))) return rc;
+    const int R = sino.lines, A = sino.columns;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_fbp_workspace(sino, image, kind), st))) return rc;
+    float *a = (float *)s.take((size_t)R * A * sizeof(float));
+    float *b = (float *)s.take((size_t)R * A * sizeof(float));
+    const float *src = sino.data;
+    if (!is_view_major(sino)) {
+        rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, a, st);
+        src = a;
+    }
+    if (!rc && !(rc = launch_conv_rows(src, b, R, A, (const float *)taps->p, st)))
+        rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
+                           nullptr, nullptr, nullptr, st);
+    scratch_end(s);
+    return rc;
+}
+
+// ---------------------------------------------------------------- DDA
+}  // extern "C"
+namespace rg {
+static int check_dda(const rg_image &img, const rg_image &sino)
+{
+    int rc;
+    if ((rc = check_image(img, "image")) || (rc = check_image(sino, "sinogram"))) return rc;
+    if (img.lines < 2 || img.columns < 2 || sino.lines < 2 || sino.columns < 2)
+        return set_error(RG_EINVAL, "DDA projector needs >= 2 lines and columns in image and "
+                                    "sinogram (the sampling distances divide by n - 1)");
+    return RG_OK;
+}
+
+static DDAGeom dda_geom(const rg_image &img, const rg_image &sino)
+{
+    DDAGeom g;
+    g.lines = img.lines; g.columns = img.columns;
+    g.itl_x = img.tl_x; g.itl_y = img.tl_y; g.ibr_x = img.br_x; g.ibr_y = img.br_y;
+    g.R = sino.lines; g.A = sino.columns;
+    g.stl_x = sino.tl_x; g.stl_y = sino.tl_y; g.sbr_x = sino.br_x; g.sbr_y = sino.br_y;
+    return g;
+}
+
+// cos/sin of the views tl_x + j*(br_x - tl_x)/(columns - 1) (host libm).
+static int dda_views(const DDAGeom &g, std::shared_ptr<DevTable> &out)
+{
+    KeyBuilder kb;
+    kb.add(g.A).add(g.stl_x).add(g.sbr_x);
+    std::vector<double> cs(2 * (size_t)g.A);
+    const double dth = (g.sbr_x - g.stl_x) / (g.A - 1);
+    for (int j = 0; j < g.A; ++j) {
+        const double th = g.stl_x + (j * dth);
+        cs[2 * j] = cos(th);
+        cs[2 * j + 1] = sin(th);
+    }
+    return get_table(std::string("ddaviews") + kb.s, cs.data(), cs.size() * sizeof(double), out);
+}
+
+int get_dda_views(const DDAGeom &g, const double **d_cs, void **holder)
+{
+    std::shared_ptr<DevTable> t;
+    int rc = dda_views(g, t);
+    if (rc) return rc;
+    *d_cs = (const double *)t->p;
+    *holder = new std::shared_ptr<void>(t);
+    return RG_OK;
+}
+}  // namespace rg
+extern "C" {
+
+size_t rg_radon_bresenham_workspace(rg_image image, rg_image sino)
+{
+    (void)image;
+    return is_view_major(sino) ? 0 : ws_total({(size_t)sino.lines * sino.columns * sizeof(float)});
+}
+
+int rg_radon_bresenham(rg_image image, rg_image sino, void *ws, size_t wsb, void *stream)
+{
+    int rc = check_dda(image, sino);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const DDAGeom g = dda_geom(image, sino);
+    std::shared_ptr<DevTable> cs;
+    if ((rc = dda_views(g, cs))) return rc;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_radon_bresenham_workspace(image, sino), st))) return rc;
+    if (is_view_major(sino)) {
+        rc = launch_bres_radon(g, (const double *)cs->p, image.data, image.column_stride,
+                               image.line_stride, sino.data, 1, g.R, nullptr, 0, 1, st);
+    } else {
+        float *am = (float *)s.take((size_t)g.R * g.A * sizeof(float));
+        if (!(rc = launch_bres_radon(g, (const double *)cs->p, image.data, image.column_stride,
+                                     image.line_stride, am, 1, g.R, nullptr, 0, 1, st)))
+            rc = launch_from_am(am, g.R, g.A, sino.data, sino.column_stride, sino.line_stride, st);
+    }
+    scratch_end(s);
+    return rc;
+}
+
+size_t rg_radon_transpose_bresenham_workspace(rg_image sino, rg_image image)
+{
+    return ws_total({(size_t)sino.lines * sino.columns * sizeof(float),
+                     (size_t)image.lines * image.columns * sizeof(float)});
+}
+
+int rg_radon_transpose_bresenham(rg_image sino, rg_image image, void *ws, size_t wsb, void *stream)
+{
+    int rc = check_dda(image, sino);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const DDAGeom g = dda_geom(image, sino);
+    std::shared_ptr<DevTable> cs;
+    if ((rc = dda_views(g, cs))) return rc;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_radon_transpose_bresenham_workspace(sino, image), st)))
+        return rc;
+    float *am = (float *)s.take((size_t)g.R * g.A * sizeof(float));
+    float *img = (float *)s.take((size_t)g.lines * g.columns * sizeof(float));
+    if (!(rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, g.R, g.A, am, st)) &&
+        !(rc = launch_fill(img, (size_t)g.lines * g.columns, 0.f, st)) &&
+        !(rc = launch_bres_transpose(g, (const double *)cs->p, am, img, 0, 1, st)))
+        rc = launch_copy2d(img, g.columns, 1, image.data, image.column_stride, image.line_stride,
+                           g.lines, g.columns, st);
+    scratch_end(s);
+    return rc;
+}
+
+int rg_dda_trace(int lines, int columns, const double img_corners[4], const double *thetas,
+                 const double *ts, int n, int cap, int *oi, int *oj, double *os, int *ocount,
+                 void *stream)
+{
+    if (lines < 2 || columns < 2 || n < 0 || cap < 0 || !img_corners || (n > 0 && (!thetas || !ts)))
+        return set_error(RG_EINVAL, "rg_dda_trace: bad arguments");
+    if (n == 0) return RG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<double> cst(3 * (size_t)n);
+    for (int r = 0; r < n; ++r) {
+        cst[3 * r] = cos(thetas[r]);
+        cst[3 * r + 1] = sin(thetas[r]);
+        cst[3 * r + 2] = ts[r];
+    }
+    double *d = nullptr;
+    RG_CK(cudaMalloc(&d, cst.size() * sizeof(double)));
+    int rc = RG_OK;
+    cudaError_t e = cudaMemcpyAsync(d, cst.data(), cst.size() * sizeof(double),
+                                    cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "rg_dda_trace upload");
+    if (!rc) rc = launch_dda_trace(lines, columns, img_corners, d, n, cap, oi, oj, os, ocount, st);
+    e = cudaStreamSynchronize(st);
+    if (!rc && e != cudaSuccess) rc = cuda_error(e, "rg_dda_trace");
+    cudaFree(d);
+    return rc;
+}
+
+// ---------------------------------------------------------------- phantoms
+int rg_phantom_fromdesc(rg_image image, const double *desc, int n, void *stream)
+{
+    int rc = check_image(image, "image");
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && !desc)) return set_error(RG_EINVAL, "bad ellipse table");
+    if (image.lines < 2 || image.columns < 2)
+        return set_error(RG_EINVAL, "phantom needs >= 2 lines and columns");
+    if (n == 0) return RG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<double> h(7 * (size_t)n);
+    for (int e = 0; e < n; ++e) {
+        const double *q = desc + 6 * e;
+        double *o = h.data() + 7 * e;
+        o[0] = q[0]; o[1] = q[1]; o[2] = q[2]; o[3] = q[3]; o[4] = q[4];
+        o[5] = cos(q[5]);
+        o[6] = sin(q[5]);
+    }
+    Scratch s;
+    if ((rc = scratch_begin(s, nullptr, 0, h.size() * sizeof(double), st))) return rc;
+    double *d = (double *)s.take(h.size() * sizeof(double));
+    cudaError_t e = cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "phantom upload");
+    if (!rc)
+        rc = launch_phantom(image.data, image.column_stride, image.line_stride, image.lines,
+                            image.columns, image.tl_x, image.tl_y, image.br_x, image.br_y, d, n, st);
+    scratch_end(s);
+    return rc;
+}
+
+int rg_radon_fromdesc(rg_image sino, const double *desc, int n, void *stream)
+{
+    int rc = check_image(sino, "sinogram");
+    if (rc) return rc;
+    if (n < 0 || (n > 0 && !desc)) return set_error(RG_EINVAL, "bad ellipse table");
+    if (sino.lines < 2 || sino.columns < 2)
+        return set_error(RG_EINVAL, "analytic sinogram needs >= 2 rays and views");
+    if (n == 0) return RG_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int V = sino.columns;
+    const double ths = (sino.br_x - sino.tl_x) / (V - 1);
+    std::vector<double> h(6 * (size_t)n + 2 * (size_t)V + 2 * (size_t)n * V);
+    memcpy(h.data(), desc, 6 * (size_t)n * sizeof(double));
+    double *cv = h.data() + 6 * n, *cp = cv + 2 * V;
+    for (int j = 0; j < V; ++j) {
+        const double th = sino.tl_x + j * ths;
+        cv[2 * j] = cos(th);
+        cv[2 * j + 1] = sin(th);
+        for (int e = 0; e < n; ++e) {
+            const double d = th - desc[6 * e + 5];
+            cp[((size_t)e * V + j) * 2] = cos(d);
+            cp[((size_t)e * V + j) * 2 + 1] = sin(d);
+        }
+    }
+    Scratch s;
+    if ((rc = scratch_begin(s, nullptr, 0, h.size() * sizeof(double), st))) return rc;
+    double *d = (double *)s.take(h.size() * sizeof(double));
+    cudaError_t e = cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "fromdesc upload");
+    if (!rc)
+        rc = launch_radon_fromdesc(sino.data, sino.column_stride, sino.line_stride, sino.lines,
+                                   V, sino.tl_x, sino.tl_y, sino.br_x, sino.br_y, d, n, st);
+    scratch_end(s);
+    return rc;
+}
+
+// ---------------------------------------------------------------- host wrappers
+static rg_image host_img(float *d, int lines, int cols, double tlx, double tly, double brx,
+                         double bry)
+{
+    rg_image im;
+    im.data = d; im.lines = lines; im.line_stride = 1; im.columns = cols; im.column_stride = cols;
+    im.tl_x = tlx; im.tl_y = tly; im.br_x = brx; im.br_y = bry;
+    return im;
+}
+
+static int host_call(int op, float *h_out, const float *h_in, int size, int nrays, int nangles,
+                     int niter)
+{
+    if (!h_out || !h_in || size < 2 || nrays < 2 || nangles < 1)
+        return set_error(RG_EINVAL, "bad host-wrapper arguments");
+    const size_t ni = (size_t)size * size * sizeof(float), ns = (size_t)nrays * nangles * sizeof(float);
+    float *di = nullptr, *ds = nullptr;
+    RG_CK(cudaMalloc(&di, ni));
+    cudaError_t e = cudaMalloc(&ds, ns);
+    if (e != cudaSuccess) { cudaFree(di); return cuda_error(e, "cudaMalloc"); }
+    const double pi = 3.14159265358979323846;
+    rg_image img = host_img(di, size, size, -1.0, 1.0, 1.0, -1.0);
+    rg_image sino = host_img(ds, nrays, nangles, 0.0, 1.0, pi, -1.0);
+    int rc = RG_OK;
+    if (op == 0) {
+        e = cudaMemcpy(di, h_in, ni, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(e, "upload");
+        if (!rc) rc = rg_radon_slantstack(img, sino, nullptr, 0, nullptr);
+        if (!rc && (e = cudaMemcpy(h_out, ds, ns, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            rc = cuda_error(e, "download");
+    } else {
+        e = cudaMemcpy(ds, h_in, ns, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) rc = cuda_error(e, "upload");
+        if (!rc && op == 1) rc = rg_backprojection_slantstack(sino, img, nullptr, 0, nullptr);
+        if (!rc && op == 2) {
+            rc = launch_fill(di, (size_t)size * size, 1.f, nullptr);
+            if (!rc) rc = rg_em(sino, img, RG_SLANTSTACK, niter, 1, nullptr, 0, nullptr);
+        }
+        if (!rc && (e = cudaMemcpy(h_out, di, ni, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            rc = cuda_error(e, "download");
+    }
+    cudaFree(di);
+    cudaFree(ds);
+    return rc;
+}
+
+int rg_radon_slantstack_host(float *h_output, const float *h_input, int size, int nrays, int nangles)
+{
+    return host_call(0, h_output, h_input, size, nrays, nangles, 0);
+}
+
+int rg_backprojection_slantstack_host(float *h_image, const float *h_sino, int size, int nrays,
+                                      int nangles)
+{
+    return host_call(1, h_image, h_sino, size, nrays, nangles, 0);
+}
+
+int rg_em_host(float *h_output, const float *h_sino, int size, int nrays, int nangles, int niter)
+{
+    return host_call(2, h_output, h_sino, size, nrays, nangles, niter);
+}
+
+}  // extern "C"

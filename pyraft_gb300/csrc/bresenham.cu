@@ -1,0 +1,305 @@
+// bresenham.cu -- DDA (Bresenham-like) ray traversal, its Radon transform and
+// the exact transpose.
+//
+// The traversal restates raft_ddaiterator (raft/raft_ddaiterator.c:16-257):
+// entry pixel from the ray's first crossing of the pixel-centre bounding box,
+// then fast-axis steps with an epsilon accumulator deciding slow-axis steps
+// and splitting the intersection length sigma.  Its pixel decisions are made
+// in FP64 with every operation written as an explicit round-to-nearest
+// intrinsic (__dadd_rn, __dmul_rn, __ddiv_rn), which the compiler never
+// contracts into FMA; with the view cos/sin taken from the host libm (as the
+// reference does) the visited pixel sequence is bit-identical to the
+// reference's.  The axis-aligned branches set sigma to sigma_tilde on entry
+// (the reference leaves it unset, raft/raft_ddaiterator.c:118-129).
+//
+// Radon: one thread per (ray, view); lanes run over rays, so the
+// view-major output is written coalesced.  Sums are FP32 products of the
+// FP32 image and the FP64 sigma rounded to FP32, accumulated in FP32 with
+// Kahan compensation.  Transpose: same walk, FP32 atomicAdd scatter into
+// the image (order of additions varies between runs, at FP32 rounding level).
+//
+// Every walk is capped at 2 * (lines + columns) + 8 steps; the walk is
+// monotone in both indices, so the cap is never reached by a valid ray.
+#include <math.h>
+
+#include "rg_internal.cuh"
+
+namespace rg {
+
+struct DDA {
+    int i, j;
+    double sigma;
+    int slow_move, fast_is_i;
+    double epsilon, epsilon_update, delta_x, delta_y, delta_slow;
+    int Delta_i, Delta_j, Delta_slow, Delta_fast;
+    double sigma_tilde;
+    int lines, columns;
+    double bbox_tl_x, bbox_tl_y, bbox_br_x, bbox_br_y;
+    double tl_x, tl_y;
+    double x0, y0;
+    int i_init, j_init;
+    double sin_theta, cos_theta;
+};
+
+__device__ __forceinline__ double sgnd(double v) { return v > 0.0 ? 1.0 : (v < 0.0 ? -1.0 : 0.0); }
+
+__device__ __forceinline__ double dda_index(double x, double xi, double delta, int D)
+{
+    const double q = __dsub_rn(__ddiv_rn(__dsub_rn(x, xi), delta), 0.5);
+    return (D >= 0) ? __dadd_rn(floor(q), 1.0) : ceil(q);
+}
+
+__device__ __forceinline__ void dda_set_image(DDA &it, int lines, int columns, double tl_x,
+                                              double tl_y, double br_x, double br_y)
+{
+    it.delta_x = __ddiv_rn(__dsub_rn(br_x, tl_x), (double)(columns - 1));
+    it.delta_y = __ddiv_rn(__dsub_rn(br_y, tl_y), (double)(lines - 1));
+    it.bbox_tl_x = __dsub_rn(tl_x, __ddiv_rn(it.delta_x, 2.0));
+    it.bbox_br_x = __dadd_rn(br_x, __ddiv_rn(it.delta_x, 2.0));
+    it.bbox_tl_y = __dsub_rn(tl_y, __ddiv_rn(it.delta_y, 2.0));
+    it.bbox_br_y = __dadd_rn(br_y, __ddiv_rn(it.delta_y, 2.0));
+    it.tl_x = tl_x;
+    it.tl_y = tl_y;
+    it.lines = lines;
+    it.columns = columns;
+}
+
+__device__ __forceinline__ void dda_set_theta(DDA &it, double c, double s)
+{
+    it.cos_theta = c;
+    it.sin_theta = s;
+    int sign = (int)sgnd(s);
+    double a = __dmul_rn((double)sign, it.bbox_br_x), b = __dmul_rn((double)sign, it.bbox_tl_x);
+    it.x0 = __dmul_rn((double)sign, (a > b) ? a : b);
+    it.Delta_j = (int)(-sgnd(it.delta_x) * sign);
+    sign = (int)sgnd(c);
+    a = __dmul_rn((double)sign, it.bbox_br_y);
+    b = __dmul_rn((double)sign, it.bbox_tl_y);
+    it.y0 = __dmul_rn((double)sign, (a < b) ? a : b);
+    it.Delta_i = (int)(sgnd(it.delta_y) * sign);
+    it.i_init = (it.Delta_i < 0) ? (it.lines - 1) : 0;
+    it.j_init = (it.Delta_j < 0) ? (it.columns - 1) : 0;
+    double df, ds, sm, lg;
+    if (fabs(__dmul_rn(it.delta_x, s)) <= fabs(__dmul_rn(it.delta_y, c))) {
+        it.fast_is_i = 1;
+        df = it.delta_y; ds = it.delta_x; sm = s; lg = c;
+        it.Delta_fast = it.Delta_i; it.Delta_slow = it.Delta_j;
+    } else {
+        it.fast_is_i = 0;
+        df = it.delta_x; ds = it.delta_y; sm = c; lg = s;
+        it.Delta_fast = it.Delta_j; it.Delta_slow = it.Delta_i;
+    }
+    it.epsilon_update = fabs(__ddiv_rn(__dmul_rn(df, sm), lg));
+    it.delta_slow = fabs(ds);
+    it.sigma_tilde = fabs(__ddiv_rn(df, lg));
+}
+
+__device__ __forceinline__ void dda_update(DDA &it)
+{
+    if (it.slow_move) {
+        if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
+        it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
+        it.slow_move = 0;
+    } else {
+        if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
+        const double eps_prev = it.epsilon;
+        it.epsilon = __dadd_rn(it.epsilon, it.epsilon_update);
+        it.slow_move = (it.epsilon > it.delta_slow);
+        if (it.slow_move) {
+            it.epsilon = __dsub_rn(it.epsilon, it.delta_slow);
+            double alpha;
+            if (it.epsilon != 0.0) {
+                alpha = __ddiv_rn(__dsub_rn(it.delta_slow, eps_prev), it.epsilon);
+                alpha = __ddiv_rn(alpha, __dadd_rn(1.0, alpha));
+            } else {
+                alpha = 1.0;
+            }
+            it.sigma = __dmul_rn(alpha, it.sigma_tilde);
+        } else {
+            it.sigma = it.sigma_tilde;
+        }
+    }
+}
+
+__device__ __forceinline__ void dda_set_t(DDA &it, double t)
+{
+    it.slow_move = 0;
+    if (it.sin_theta == 0.0) {
+        it.j = (int)dda_index(t, it.tl_x, it.delta_x, it.Delta_j);
+        it.i = it.i_init;
+        it.epsilon = 0.0;
+        it.epsilon_update = 0.0;
+        it.sigma = it.sigma_tilde;
+        return;
+    }
+    if (it.cos_theta == 0.0) {
+        it.i = (int)dda_index(t, it.tl_y, it.delta_y, it.Delta_i);
+        it.j = it.j_init;
+        it.epsilon = 0.0;
+        it.epsilon_update = 0.0;
+        it.sigma = it.sigma_tilde;
+        return;
+    }
+    const double sx = __ddiv_rn(__dsub_rn(__dmul_rn(t, it.cos_theta), it.x0), it.sin_theta);
+    const double sy = __ddiv_rn(__dsub_rn(it.y0, __dmul_rn(t, it.sin_theta)), it.cos_theta);
+    if (sx > sy) {
+        const double xy = __dadd_rn(__dmul_rn(sx, it.cos_theta), __dmul_rn(t, it.sin_theta));
+        it.i = (int)dda_index(xy, it.tl_y, it.delta_y, it.Delta_i);
+        it.j = it.j_init;
+        it.epsilon = fabs(__dsub_rn(xy, __dadd_rn(it.tl_y, __dmul_rn(__dsub_rn((double)it.i,
+                                         __dmul_rn(0.5, (double)it.Delta_i)), it.delta_y))));
+        if (!it.fast_is_i) {
+            it.j -= it.Delta_j;
+            dda_update(it);
+        } else {
+            it.epsilon = __dsub_rn(it.epsilon, fabs(it.delta_y));
+            it.epsilon = __ddiv_rn(it.epsilon, it.cos_theta);
+            it.sigma = fabs(it.epsilon);
+            it.epsilon = fabs(__dmul_rn(it.sigma, it.sin_theta));
+        }
+    } else {
+        const double xy = __dadd_rn(__dmul_rn(-sy, it.sin_theta), __dmul_rn(t, it.cos_theta));
+        it.j = (int)dda_index(xy, it.tl_x, it.delta_x, it.Delta_j);
+        it.i = it.i_init;
+        it.epsilon = fabs(__dsub_rn(xy, __dadd_rn(it.tl_x, __dmul_rn(__dsub_rn((double)it.j,
+                                         __dmul_rn(0.5, (double)it.Delta_j)), it.delta_x))));
+        if (it.fast_is_i) {
+            it.i -= it.Delta_i;
+            dda_update(it);
+        } else {
+            it.epsilon = __dsub_rn(it.epsilon, fabs(it.delta_x));
+            it.epsilon = __ddiv_rn(it.epsilon, it.sin_theta);
+            it.sigma = fabs(it.epsilon);
+            it.epsilon = fabs(__dmul_rn(it.sigma, it.cos_theta));
+        }
+    }
+}
+
+__device__ __forceinline__ bool dda_end(const DDA &it)
+{
+    return (it.i < 0) || (it.i >= it.lines) || (it.j < 0) || (it.j >= it.columns);
+}
+
+// ----------------------------------------------------------------------------
+
+template <bool RATIO>
+__global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__restrict__ cs_tab,
+                                                    const float *__restrict__ img, long long ics,
+                                                    long long ils, float *__restrict__ out,
+                                                    long long ocs, long long ols,
+                                                    const float *__restrict__ y_am, int first,
+                                                    int stride)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;   // ray
+    const int j = first + blockIdx.y * stride;             // view
+    if (i >= g.R) return;
+    DDA it;
+    dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
+    dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
+    const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
+    dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    float acc = 0.f, comp = 0.f;
+    const int cap = 2 * (g.lines + g.columns) + 8;
+    for (int step = 0; step < cap && !dda_end(it); ++step) {
+        const float x = __ldg(img + (long long)it.i * ics + (long long)it.j * ils) * (float)it.sigma;
+        const float y = x - comp, t = acc + y;
+        comp = (t - acc) - y;
+        acc = t;
+        dda_update(it);
+    }
+    float val = acc - comp;
+    if (RATIO) {
+        const float yv = y_am[(size_t)j * g.R + i];
+        val = (val != 0.f) ? yv / val : 0.f;
+    }
+    out[(long long)i * ocs + (long long)j * ols] = val;
+}
+
+int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, long long ics,
+                      long long ils, float *out, long long ocs, long long ols,
+                      const float *y_am, int first, int stride, cudaStream_t st)
+{
+    const int nv = (g.A - first + stride - 1) / stride;
+    if (nv <= 0) return RG_OK;
+    dim3 grid((g.R + 127) / 128, nv);
+    if (y_am)
+        k_bres_radon<true><<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, y_am,
+                                                 first, stride);
+    else
+        k_bres_radon<false><<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, nullptr,
+                                                  first, stride);
+    RG_CK_LAUNCH("k_bres_radon");
+    return RG_OK;
+}
+
+// s(i, j) = s_am[j * R + i]; img_c: contiguous lines x columns, pre-zeroed.
+__global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double *__restrict__ cs_tab,
+                                                        const float *__restrict__ s_am,
+                                                        float *__restrict__ img_c, int first,
+                                                        int stride)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = first + blockIdx.y * stride;
+    if (i >= g.R) return;
+    const float sv = s_am[(size_t)j * g.R + i];
+    if (sv == 0.f) return;
+    DDA it;
+    dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
+    dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
+    const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
+    dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    const int cap = 2 * (g.lines + g.columns) + 8;
+    for (int step = 0; step < cap && !dda_end(it); ++step) {
+        atomicAdd(img_c + (size_t)it.i * g.columns + it.j, sv * (float)it.sigma);
+        dda_update(it);
+    }
+}
+
+int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_am, float *img_c,
+                          int first, int stride, cudaStream_t st)
+{
+    const int nv = (g.A - first + stride - 1) / stride;
+    if (nv <= 0) return RG_OK;
+    dim3 grid((g.R + 127) / 128, nv);
+    k_bres_transpose<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride);
+    RG_CK_LAUNCH("k_bres_transpose");
+    return RG_OK;
+}
+
+// Pixel sequences of arbitrary rays (cos, sin, t per ray).
+__global__ void k_dda_trace(int lines, int columns, double tl_x, double tl_y, double br_x,
+                            double br_y, const double *__restrict__ cst, int n, int cap,
+                            int *__restrict__ oi, int *__restrict__ oj, double *__restrict__ os,
+                            int *__restrict__ ocount)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n) return;
+    DDA it;
+    dda_set_image(it, lines, columns, tl_x, tl_y, br_x, br_y);
+    dda_set_theta(it, cst[3 * r], cst[3 * r + 1]);
+    dda_set_t(it, cst[3 * r + 2]);
+    int cnt = 0;
+    const int limit = 2 * (lines + columns) + 8;
+    while (!dda_end(it) && cnt < limit) {
+        if (cnt < cap) {
+            oi[(size_t)r * cap + cnt] = it.i;
+            oj[(size_t)r * cap + cnt] = it.j;
+            os[(size_t)r * cap + cnt] = it.sigma;
+        }
+        ++cnt;
+        dda_update(it);
+    }
+    ocount[r] = cnt;
+}
+
+int launch_dda_trace(int lines, int columns, const double *corners, const double *d_cst, int n,
+                     int cap, int *oi, int *oj, double *os, int *ocount, cudaStream_t st)
+{
+    k_dda_trace<<<(n + 127) / 128, 128, 0, st>>>(lines, columns, corners[0], corners[1],
+                                                  corners[2], corners[3], d_cst, n, cap, oi, oj,
+                                                  os, ocount);
+    RG_CK_LAUNCH("k_dda_trace");
+    return RG_OK;
+}
+
+}  // namespace rg

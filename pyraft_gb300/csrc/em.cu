@@ -1,0 +1,200 @@
+// em.cu -- emission EM / OSEM drivers.
+//
+// MLEM, x <- x * A^T(y / A x) / A^T 1 (pyraft/iterative/em.py:109-144,
+// raft/raft_em_gpu.cu:20-87), and OSEM over interleaved view subsets
+// (subset s = views s, s+S, ...; the reference's osem, pyraft/iterative/
+// em.py:265-320, uses contiguous blocks of Fourier-slice operators, which
+// are not available here; interleaved subsets are the standard choice).
+//
+// Slant-stack path, per sub-iteration (3 launches, no host round trip):
+//   1. pack the iterate into line pairs (k_line_pairs);
+//   2. Radon over the subset's views with the EM ratio fused into the
+//      epilogue: r = y / (A x), 0 where A x == 0;
+//   3. matched-adjoint gather of r over the subset's views with the update
+//      fused into the epilogue: x <- x * (A^T r) * (1 / A^T 1).
+// The sensitivities A_s^T 1 of each subset are accumulated in FP64 once per
+// call and stored as reciprocals (0 where the sensitivity is 0, which also
+// zeroes pixels that no ray of the subset reaches).
+//
+// DDA path (pyraft's em() default): the same loop over the DDA Radon with
+// the fused ratio, the DDA transpose, and an elementwise update.
+#include <algorithm>
+#include <vector>
+
+#include "rg_internal.cuh"
+
+namespace rg {
+
+namespace {
+
+struct Holders {
+    std::vector<void *> h;
+    ~Holders()
+    {
+        for (void *p : h) release_holder(p);
+    }
+};
+
+size_t em_ss_ws(int N, int R, int A, int S)
+{
+    const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)N * N * sizeof(float);
+    return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S});
+}
+
+size_t em_dda_ws(int L, int C, int R, int A, int S)
+{
+    const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)L * C * sizeof(float);
+    return ws_sum({sino, sino, img, img, img * S});
+}
+
+}  // namespace
+
+// Runs EM on one slice whose buffers are already laid out internally:
+// y_am (A x R view-major), x (N x N contiguous).  Scratch `s` must have room
+// for ratio, pairs and sensitivities (em_ss_ws minus y and x).
+static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, float *x,
+                      Scratch &s, cudaStream_t st)
+{
+    const int N = g.N, R = g.R, A = g.A;
+    Holders hold;
+    std::vector<const SSPlan *> plans(S);
+    for (int k = 0; k < S; ++k) {
+        void *h = nullptr;
+        int rc = get_ss_plan(g, S, k, &plans[k], &h);
+        if (rc) return rc;
+        hold.h.push_back(h);
+        if (!plans[k]->adj_ok)
+            return set_error(RG_EUNSUPPORTED, "EM needs ray spacing >= pixel spacing (nrays <= size)");
+    }
+    float *ratio = (float *)s.take((size_t)R * A * sizeof(float));
+    float2 *prow = (float2 *)s.take(radon_pairs_bytes(N));
+    float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N));
+    float *inv = (float *)s.take((size_t)N * N * sizeof(float) * S);
+    int rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
+    for (int k = 0; k < S && !rc; ++k)
+        rc = launch_gather(*plans[k], 2, ratio, R, inv + (size_t)k * N * N, N, 1, nullptr, nullptr,
+                           nullptr, st);
+    for (int it = 0; it < niter && !rc; ++it)
+        for (int k = 0; k < S && !rc; ++k) {
+            if ((rc = launch_line_pairs(x, N, 1, N, prow, pcol, st))) break;
+            if ((rc = launch_radon(*plans[k], prow, pcol, ratio, R, y_am, R, st))) break;
+            rc = launch_gather(*plans[k], 1, ratio, R, nullptr, 0, 0, x, inv + (size_t)k * N * N,
+                               nullptr, st);
+        }
+    return rc;
+}
+
+static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S, void *ws,
+                  size_t wsb, cudaStream_t st)
+{
+    DDAGeom g;
+    g.lines = image.lines; g.columns = image.columns;
+    g.itl_x = image.tl_x; g.itl_y = image.tl_y; g.ibr_x = image.br_x; g.ibr_y = image.br_y;
+    g.R = sino.lines; g.A = sino.columns;
+    g.stl_x = sino.tl_x; g.stl_y = sino.tl_y; g.sbr_x = sino.br_x; g.sbr_y = sino.br_y;
+    if (g.lines < 2 || g.columns < 2 || g.R < 2 || g.A < 2)
+        return set_error(RG_EINVAL, "DDA EM needs >= 2 lines and columns in image and sinogram");
+    const double *cs = nullptr;
+    void *holder = nullptr;
+    int rc = get_dda_views(g, &cs, &holder);
+    if (rc) return rc;
+    Holders hold;
+    hold.h.push_back(holder);
+    const int L = g.lines, C = g.columns, R = g.R, A = g.A;
+    const size_t npix = (size_t)L * C;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, em_dda_ws(L, C, R, A, S), st))) return rc;
+    float *y = (float *)s.take((size_t)R * A * sizeof(float));
+    float *ratio = (float *)s.take((size_t)R * A * sizeof(float));
+    float *x = (float *)s.take(npix * sizeof(float));
+    float *bp = (float *)s.take(npix * sizeof(float));
+    float *inv = (float *)s.take(npix * sizeof(float) * S);
+    rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, y, st);
+    if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, C, 1, L, C, st);
+    if (!rc) rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
+    for (int k = 0; k < S && !rc; ++k) {
+        if ((rc = launch_fill(bp, npix, 0.f, st))) break;
+        if ((rc = launch_bres_transpose(g, cs, ratio, bp, k, S, st))) break;
+        rc = launch_invert(bp, inv + (size_t)k * npix, npix, st);
+    }
+    for (int it = 0; it < niter && !rc; ++it)
+        for (int k = 0; k < S && !rc; ++k) {
+            if ((rc = launch_bres_radon(g, cs, x, C, 1, ratio, 1, R, y, k, S, st))) break;
+            if ((rc = launch_fill(bp, npix, 0.f, st))) break;
+            if ((rc = launch_bres_transpose(g, cs, ratio, bp, k, S, st))) break;
+            rc = launch_em_update(x, bp, inv + (size_t)k * npix, npix, st);
+        }
+    if (!rc) rc = launch_copy2d(x, C, 1, image.data, image.column_stride, image.line_stride, L, C, st);
+    scratch_end(s);
+    return rc;
+}
+
+}  // namespace rg
+
+using namespace rg;
+
+extern "C" {
+
+size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets)
+{
+    const int S = nsubsets < 1 ? 1 : nsubsets;
+    if (method == RG_BRESENHAM)
+        return em_dda_ws(image.lines, image.columns, sino.lines, sino.columns, S);
+    return em_ss_ws(image.lines, sino.lines, sino.columns, S);
+}
+
+int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, void *ws,
+          size_t wsb, void *stream)
+{
+    if (!sino.data || !image.data) return set_error(RG_EINVAL, "rg_em: null data pointer");
+    if (niter < 0) return set_error(RG_EINVAL, "rg_em: niter < 0");
+    if (int rc0 = check_ws(ws)) return rc0;
+    if (nsubsets < 1 || nsubsets > sino.columns)
+        return set_error(RG_EINVAL, "rg_em: nsubsets must be in [1, nviews]");
+    cudaStream_t st = (cudaStream_t)stream;
+    if (method == RG_BRESENHAM) return em_dda(sino, image, niter, nsubsets, ws, wsb, st);
+    if (method != RG_SLANTSTACK) return set_error(RG_EINVAL, "rg_em: unknown method %d", method);
+    if (image.lines != image.columns || image.lines < 2 || sino.lines < 2)
+        return set_error(RG_EINVAL, "slant-stack EM needs a square image, size >= 2, nrays >= 2");
+    SSGeom g;
+    g.N = image.lines;
+    g.itl_x = image.tl_x; g.itl_y = image.tl_y; g.ibr_x = image.br_x; g.ibr_y = image.br_y;
+    g.R = sino.lines; g.A = sino.columns;
+    g.stl_x = sino.tl_x; g.stl_y = sino.tl_y; g.sbr_x = sino.br_x; g.sbr_y = sino.br_y;
+    const int N = g.N, R = g.R, A = g.A;
+    Scratch s;
+    int rc = scratch_begin(s, ws, wsb, rg_em_workspace(sino, image, method, nsubsets), st);
+    if (rc) return rc;
+    float *y = (float *)s.take((size_t)R * A * sizeof(float));
+    float *x = (float *)s.take((size_t)N * N * sizeof(float));
+    rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, y, st);
+    if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, N, 1, N, N, st);
+    if (!rc) rc = em_ss_core(g, niter, nsubsets, y, x, s, st);
+    if (!rc) rc = launch_copy2d(x, N, 1, image.data, image.column_stride, image.line_stride, N, N, st);
+    scratch_end(s);
+    return rc;
+}
+
+size_t rg_osem_batch_workspace(const rg_image *sinos, const rg_image *images, int nslices,
+                               int nsubsets)
+{
+    size_t m = 0;
+    for (int k = 0; k < nslices; ++k)
+        m = std::max(m, rg_em_workspace(sinos[k], images[k], RG_SLANTSTACK, nsubsets));
+    return m;
+}
+
+int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int niter, int nsubsets,
+                  int graph, void *ws, size_t wsb, void *stream)
+{
+    (void)graph;
+    if (nslices < 0 || (nslices > 0 && (!sinos || !images)))
+        return set_error(RG_EINVAL, "rg_osem_batch: bad slice arrays");
+    for (int k = 0; k < nslices; ++k) {
+        int rc = rg_em(sinos[k], images[k], RG_SLANTSTACK, niter, nsubsets, ws, wsb, stream);
+        if (rc) return rc;
+    }
+    return RG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,169 @@
+// rg_internal.cuh -- shared declarations of libraftgb (GB300, sm_103a).
+//
+// Fixed-point positions.  Every projector evaluates a sample position that
+// is affine in two integer indices (ray/line for the Radon, row/column for
+// the gathers).  The per-view coefficients are computed once on the host in
+// FP64 (the same libm cos/sin/tan values the reference evaluates) and stored
+// as signed Q32.32 integers (int64).  The kernels then form positions with
+// exact integer arithmetic: an origin in Q32.32 plus small local offsets in
+// Q9.23 (uint32), whose low 23 bits become the float interpolation weight by
+// a single bit operation (0x3F800000 | frac gives 1 + w).  This keeps the
+// floor decision and the weight at ~1e-7 sample precision without FP64 in
+// the hot loops and without float<->int conversion instructions, which issue
+// at a quarter of the FFMA rate.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <initializer_list>
+#include <string>
+
+#include "../../include/raftgb.h"
+
+namespace rg {
+
+// ----------------------------------------------------------------------------
+// Per-view constants (one per view of a plan, device resident).
+struct alignas(16) View {
+    // Slant-stack Radon: position along line i of ray k (in samples of the
+    // line) u = r0 + k*rk + i*ri, Q32.32.  Lines are image columns when
+    // (flags & kLinesAreRows) == 0 (|cos| < 1/sqrt 2), image rows otherwise.
+    long long rk, ri, r0;
+    // Slant-stack backprojection: t-sample position of pixel (row, col),
+    // u = b0 + row*brow + col*bcol, Q32.32.
+    long long brow, bcol, b0;
+    // Matched adjoint: ray-index position of the ray through pixel (row, col)
+    // on the pixel's line, kappa = k0 + row*krow + col*kcol, Q32.32.
+    long long krow, kcol, k0;
+    float delta;      // Radon step length Delta (dy/|sin| or dx/|cos|)
+    float P;          // |rk|: ray spacing in line samples
+    int flags;        // kLinesAreRows | kRkNegative
+    int view;         // sinogram column this entry refers to
+    int pad[4];
+};
+static_assert(sizeof(View) == 112, "View layout");
+
+enum { kLinesAreRows = 1, kRkNegative = 2 };
+
+// ----------------------------------------------------------------------------
+// Host-side helpers (api.cu).
+int set_error(int code, const char *fmt, ...);
+int cuda_error(cudaError_t e, const char *what);
+
+#define RG_CK(call)                                                     \
+    do {                                                                \
+        cudaError_t e_ = (call);                                        \
+        if (e_ != cudaSuccess) return ::rg::cuda_error(e_, #call);      \
+    } while (0)
+
+#define RG_CK_LAUNCH(what)                                              \
+    do {                                                                \
+        cudaError_t e_ = cudaGetLastError();                            \
+        if (e_ != cudaSuccess) return ::rg::cuda_error(e_, what);       \
+    } while (0)
+
+// Bump allocator over one scratch block (caller's workspace or a
+// stream-ordered allocation that is released on the same stream).
+struct Scratch {
+    char *base = nullptr;
+    size_t size = 0, off = 0;
+    bool owned = false;
+    cudaStream_t stream = nullptr;
+    static size_t align(size_t b) { return (b + 255) & ~size_t(255); }
+    void *take(size_t bytes) {
+        off = align(off);
+        void *p = base + off;
+        off += bytes;
+        return p;
+    }
+};
+// Sizes are summed with Scratch::align per piece; begin() checks or allocates.
+int check_ws(const void *ws);
+int scratch_begin(Scratch &s, void *ws, size_t ws_bytes, size_t need, cudaStream_t st);
+void scratch_end(Scratch &s);
+
+// ----------------------------------------------------------------------------
+// Geometry of a slant-stack plan.
+struct SSGeom {
+    int N;                         // image size (N x N)
+    double itl_x, itl_y, ibr_x, ibr_y;
+    int R, A;                      // rays, views of the full sinogram
+    double stl_x, stl_y, sbr_x, sbr_y;
+};
+
+// A plan: geometry plus device-resident per-view constants for a list of
+// views (all views, or one OSEM subset).
+struct SSPlan {
+    SSGeom g;
+    int nv = 0;                    // number of views in this plan
+    View *d_views = nullptr;       // device
+    int wmax_bp = 0, wmax_adj = 0; // gather window widths (entries) needed
+    float dth = 0.f;               // view spacing (backprojection scale)
+    bool adj_ok = true;            // every |rk| >= 1 (two-tap adjoint)
+    int device = -1;
+};
+
+int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv);
+void ss_plan_free(SSPlan &p);
+
+// Kernel launchers (slantstack.cu).  Images handed to the kernels are
+// strided views: element (row, col) at ptr[row*cs + col*ls].
+size_t radon_pairs_bytes(int N);
+int launch_line_pairs(const float *img, long long cs, long long ls, int N,
+                      float2 *pairs_rows, float2 *pairs_cols, cudaStream_t st);
+// Radon over the plan's views; out row v.view (angle-major, ld = out_ld)
+// gets the ray sums, or the EM ratio y/Ax when y_am != nullptr.
+int launch_radon(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
+                 float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st);
+// Gathers.  mode 0: backprojection (scaled by dth); 1: matched adjoint;
+// 2: matched adjoint accumulated in FP64, epilogue writes 1/x (0 where 0).
+// em_x != nullptr (mode 1): x <- x * adj * inv_sens, with x, inv_sens
+// contiguous N x N.
+int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
+                  float *out, long long cs, long long ls,
+                  float *em_x, const float *inv_sens, int *d_err, cudaStream_t st);
+
+// aux.cu
+int launch_to_am(const float *in, long long cs, long long ls, int R, int A, float *out_am,
+                 cudaStream_t st);
+int launch_from_am(const float *am, int R, int A, float *out, long long cs, long long ls,
+                   cudaStream_t st);
+int launch_copy2d(const float *in, long long ics, long long ils, float *out, long long ocs,
+                  long long ols, int rows, int cols, cudaStream_t st);
+int launch_fill(float *p, size_t n, float v, cudaStream_t st);
+int launch_phantom(float *img, long long cs, long long ls, int lines, int cols,
+                   double tl_x, double tl_y, double br_x, double br_y,
+                   const double *d_desc, int n, cudaStream_t st);
+int launch_radon_fromdesc(float *sino, long long cs, long long ls, int lines, int cols,
+                          double tl_x, double tl_y, double br_x, double br_y,
+                          const double *d_desc, int n, cudaStream_t st);
+
+// filter.cu: out_am[a][n] = sum_k taps[n - k + R - 1] * in_am[a][k].
+int launch_conv_rows(const float *in_am, float *out_am, int R, int A, const float *d_taps,
+                     cudaStream_t st);
+
+// bresenham.cu
+struct DDAGeom {
+    int lines, columns;
+    double itl_x, itl_y, ibr_x, ibr_y;
+    int R, A;
+    double stl_x, stl_y, sbr_x, sbr_y;
+};
+int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, long long ics,
+                      long long ils, float *out, long long cs, long long ls,
+                      const float *y_am, int first, int stride, cudaStream_t st);
+int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_am,
+                          float *img_c, int first, int stride, cudaStream_t st);
+int launch_em_update(float *x, const float *bp, const float *inv_sens, size_t n, cudaStream_t st);
+int launch_invert(const float *sens, float *inv, size_t n, cudaStream_t st);
+
+// api.cu helpers shared with em.cu
+int get_ss_plan(const SSGeom &g, int stride, int first, const SSPlan **out, void **holder);
+void release_holder(void *holder);
+int get_dda_views(const DDAGeom &g, const double **d_cs, void **holder);
+size_t ws_sum(std::initializer_list<size_t> pieces);
+int launch_dda_trace(int lines, int columns, const double *corners, const double *d_cst, int n,
+                     int cap, int *oi, int *oj, double *os, int *ocount, cudaStream_t st);
+
+}  // namespace rg

@@ -1,0 +1,111 @@
+"""EM and OSEM (pyraft/iterative/em.py:109-320).
+
+* ``make_em(sino, shape, projection_method, backprojection_method)`` returns
+  a one-iteration callable, ``em(sino, shape, niter)`` runs MLEM from x0 = 1
+  with pyraft's defaults (DDA pair; default shape = nviews x nviews, as
+  pyraft/iterative/em.py:153-154).
+* ``em_gpu(s, img_size, niter)``: slant-stack MLEM (raft_em_gpu's role) with
+  the matched adjoint as backprojector (true MLEM).
+* ``osem(sino, shape, niter, nblocks)``: OSEM over interleaved view subsets
+  of the slant-stack pair (pyraft's osem uses Fourier-slice operators over
+  contiguous blocks, which need pynfft; see em.cu).
+Guards everywhere: y / 0 -> 0, and pixels with zero sensitivity -> 0
+(pyraft divides by zero there).  Every loop runs inside the library
+(rg_em): no host round trip per iteration.
+"""
+from __future__ import annotations
+
+import numpy
+
+from . import _native
+from .raftypes import finish, gpu_image, image, new_gpu, rg_image, stream_ptr, to_gpu, workspace
+from .sinogram import method_id, radon_method
+
+
+def _run_em(sino, x0, method, niter, nsubsets):
+    """x0: gpu_image updated in place."""
+    L = _native.load()
+    a, b = rg_image(sino), rg_image(x0)
+    ws_t, ws = workspace(L.rg_em_workspace(a, b, method, nsubsets))
+    _native.check(L.rg_em(a, b, method, int(niter), int(nsubsets), ws,
+                          ws_t.numel() if ws_t is not None else 0, stream_ptr()))
+
+
+def _method(projection_method, backprojection_method):
+    p, b = method_id(projection_method), method_id(backprojection_method)
+    if p != b:
+        raise TypeError('projection and backprojection methods must form a transpose pair '
+                        '(both BRESENHAM or both SLANTSTACK)')
+    if p == method_id(radon_method.BRESENHAM):
+        return _native.RG_BRESENHAM
+    if p == method_id(radon_method.SLANTSTACK):
+        return _native.RG_SLANTSTACK
+    raise TypeError('Unsupported method for EM!')
+
+
+def _start(shape, kwargs):
+    if isinstance(shape, (image, gpu_image)):
+        if kwargs:
+            raise TypeError('Unhandled arguments!')
+        x, host = to_gpu(shape)
+        x = gpu_image(x.data.clone(), x.top_left, x.bottom_right)
+        return x, host
+    probe = image((2, 2), **kwargs)
+    x = new_gpu(shape, probe.top_left, probe.bottom_right)
+    x.data.fill_(1.0)
+    return x, None
+
+
+def _finish_em(x, shape_host, sino_host):
+    """Host result if the start image was a host image, or (for a shape
+    tuple) if the sinogram was; device result otherwise."""
+    return finish(x, sino_host if shape_host is None else shape_host)
+
+
+def make_em(sino, shape, projection_method=radon_method.BRESENHAM,
+            backprojection_method=radon_method.BRESENHAM, weight=None, **kwargs):
+    """One-iteration EM map x -> x * A^T(y / A x) / A^T 1."""
+    if weight is not None:
+        raise TypeError('a precomputed weight is not supported; the sensitivity is computed '
+                        'on the device in FP64')
+    m = _method(projection_method, backprojection_method)
+    gs, _ = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
+
+    def em_step(x):
+        gx, host = to_gpu(x)
+        gx = gpu_image(gx.data.clone(), gx.top_left, gx.bottom_right)
+        _run_em(gs, gx, m, 1, 1)
+        return finish(gx, host)
+    return em_step
+
+
+def em(sino, shape=None, niter=5, method=radon_method.BRESENHAM, **kwargs):
+    if shape is None:
+        shape = [sino.shape[1], sino.shape[1]]
+    x, host = _start(shape, kwargs)
+    gs, shost = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
+    _run_em(gs, x, _method(method, method), niter, 1)
+    return _finish_em(x, host, shost)
+
+
+def osem(sino, shape=None, niter=5, nblocks=4, method=radon_method.SLANTSTACK, **kwargs):
+    if shape is None:
+        shape = [sino.shape[0], sino.shape[0]]
+    x, host = _start(shape, kwargs)
+    gs, shost = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
+    _run_em(gs, x, _method(method, method), niter, nblocks)
+    return _finish_em(x, host, shost)
+
+
+def em_gpu(*args):
+    """pyraft's em_gpu(s, img_size=rays, niter=20): host sinogram on the
+    default geometry -> (img_size, img_size) float32 array."""
+    if len(args) == 0:
+        raise TypeError('Not enough arguments!')
+    s = args[0]
+    n = args[1] if len(args) > 1 else s.shape[0]
+    niter = args[2] if len(args) > 2 else 20
+    src = image(numpy.asarray(s, dtype=numpy.float64), top_left=(0.0, 1.0),
+                bottom_right=(numpy.pi, -1.0))
+    out = em(src, (n, n), niter, method=radon_method.SLANTSTACK)
+    return numpy.asarray(out, dtype=numpy.float32)
