@@ -114,7 +114,8 @@ __global__ void k_phantom(float *__restrict__ img, long long cs, long long ls, i
 {
     const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
     if (j >= cols) return;
-    float acc = img[(long long)i * cs + (long long)j * ls];
+    // FP64 accumulation as the reference's double image, rounded once.
+    double acc = img[(long long)i * cs + (long long)j * ls];
     for (int e = 0; e < n; ++e) {
         const double *q = d + 7 * e;
         const double alpha = q[0], a = q[1], b = q[2], x0 = q[3], y0 = q[4], c = q[5], s = q[6];
@@ -128,9 +129,9 @@ __global__ void k_phantom(float *__restrict__ img, long long cs, long long ls, i
         tmp = __dmul_rn(tmp, tmp);
         val = __dadd_rn(val, tmp);
         val = __dsqrt_rn(val);
-        if (val <= 1.0) acc += (float)alpha;
+        if (val <= 1.0) acc = __dadd_rn(acc, alpha);
     }
-    img[(long long)i * cs + (long long)j * ls] = acc;
+    img[(long long)i * cs + (long long)j * ls] = (float)acc;
 }
 
 int launch_phantom(float *img, long long cs, long long ls, int lines, int cols, double tl_x,
@@ -157,7 +158,7 @@ __global__ void k_radon_fromdesc(float *__restrict__ sino, long long cs, long lo
     if (i >= lines) return;
     const double *cv = d + 6 * n;                  // [cols][2] view cos/sin
     const double *cp = cv + 2 * cols;              // [n][cols][2] cos/sin(theta - theta_e)
-    float acc = sino[(long long)i * cs + (long long)j * ls];
+    double acc = sino[(long long)i * cs + (long long)j * ls];
     const double c = cv[2 * j], s = cv[2 * j + 1];
     for (int e = 0; e < n; ++e) {
         const double *q = d + 6 * e;
@@ -172,9 +173,9 @@ __global__ void k_radon_fromdesc(float *__restrict__ sino, long long cs, long lo
         mab = __dmul_rn(mab, tss);
         double tp = __dsub_rn(__dmul_rn(mab, (double)i), delt);
         tp = __dmul_rn(tp, tp);
-        if (tp <= 1.0) acc += (float)__dmul_rn(m, __dsqrt_rn(__dsub_rn(1.0, tp)));
+        if (tp <= 1.0) acc = __dadd_rn(acc, __dmul_rn(m, __dsqrt_rn(__dsub_rn(1.0, tp))));
     }
-    sino[(long long)i * cs + (long long)j * ls] = acc;
+    sino[(long long)i * cs + (long long)j * ls] = (float)acc;
 }
 
 int launch_radon_fromdesc(float *sino, long long cs, long long ls, int lines, int cols,

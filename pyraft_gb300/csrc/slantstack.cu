@@ -99,7 +99,14 @@ int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
         bool ok = to_q32(rk, v.rk) && to_q32(ri, v.ri) && to_q32(r0, v.r0) &&
                   to_q32(brow, v.brow) && to_q32(bcol, v.bcol) && to_q32(b0, v.b0) &&
                   to_q32(krow, v.krow) && to_q32(kcol, v.kcol) && to_q32(k0, v.k0);
-        if (!ok) return set_error(RG_EUNSUPPORTED, "view %d: position coefficients overflow", j);
+        // Every position the kernels form (origin + index * step, in Q32.32)
+        // must stay far inside int64: bound them by 2^30 samples.
+        const double lim = 1073741824.0;
+        ok = ok && fabs(r0) + (g.R - 1) * fabs(rk) + (g.N - 1) * fabs(ri) < lim &&
+             fabs(b0) + (g.N - 1) * (fabs(brow) + fabs(bcol)) < lim &&
+             fabs(k0) + (g.N - 1) * (fabs(krow) + fabs(kcol)) < lim;
+        if (!ok) return set_error(RG_EUNSUPPORTED, "view %d: positions exceed 2^30 samples "
+                                                   "(image and sinogram extents too different)", j);
         v.delta = (float)delta;
         v.P = (float)fabs(rk);
         v.view = j;
@@ -230,6 +237,11 @@ __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
         lo = (int)ceilf(tlo);
         hi = (int)floorf(thi);
     }
+    // Exact check of the ends (positions are monotone in i): every sample
+    // index used stays in [-1, N-1], i.e. inside the padded line.
+    const long long ulo = -(1LL << 32), uhi = (long long)N << 32;
+    while (lo <= hi && (u0 + (long long)lo * q < ulo || u0 + (long long)lo * q >= uhi)) ++lo;
+    while (hi >= lo && (u0 + (long long)hi * q < ulo || u0 + (long long)hi * q >= uhi)) --hi;
 
     float acc = 0.f, comp = 0.f;
     if (lo <= hi) {
