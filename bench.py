@@ -242,6 +242,29 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (bp_ms * 1e-3) / 1e9
 
+    # ---- the other operators of the path at the same size (one call each)
+    def timed(fn, reps=5):
+        out = []
+        for k in range(warm + reps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            if k >= warm:
+                out.append(a.elapsed_time(b))
+        return statistics.mean(out)
+    src = torch.flip(img, dims=[0]).contiguous()
+    sino_out = torch.empty((A, R), dtype=torch.float32, device="cuda")
+    SO = rg_image(rg.gpu_image(sino_out.t(), (0.0, 1.0), (math.pi, -1.0)))
+    RI = rg_image(rg.gpu_image(src))
+    rws = L.rg_radon_slantstack_workspace(RI, SO)
+    rwsb = torch.empty(rws, dtype=torch.uint8, device="cuda")
+    radon_ms = timed(lambda: _native.check(L.rg_radon_slantstack(RI, SO, rwsb.data_ptr(), rws,
+                                                                 sp)))
+    adj_ms = timed(lambda: _native.check(L.rg_radon_transpose_slantstack(FA, I, None, 0, sp)))
+
     # ---- end to end: pinned host sinogram in, image out, through rg_fbp
     h_in = torch.empty((R, A), dtype=torch.float32).pin_memory()
     h_in.copy_(sino.cpu())
@@ -296,6 +319,12 @@ def main():
                      "algorithmic_bytes": alg_bytes, "kernel_ms": round(bp_ms, 4),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "model": "8 B per (pixel, view) update + image and sinogram bytes once"},
+        "ops": {"radon_gups": round(R * A * N / (radon_ms * 1e-3) / 1e9, 1),
+                "radon_ms": round(radon_ms, 4),
+                "adjoint_gups": round(UPDATES / (adj_ms * 1e-3) / 1e9, 1),
+                "adjoint_ms": round(adj_ms, 4),
+                "backprojection_gups": round(UPDATES / (bp_ms * 1e-3) / 1e9, 1),
+                "note": "single calls at 2048^2 x 1800 (view-major sinogram), L2 flushed"},
         "gpu_launches": 3 * args.steps,
         "clocks": clk,
         "wall_s_timed_region": round(wall, 3),

@@ -81,6 +81,21 @@ size_t rg_radon_slantstack_workspace(rg_image phantom, rg_image radon);
 int rg_radon_slantstack(rg_image phantom, rg_image radon,
                         void *workspace, size_t workspace_bytes, void *stream);
 
+/* Same Radon transform for callers that cannot allocate device memory (no
+ * counterpart in the reference): code running inside a stream capture,
+ * where allocation calls are not allowed, or a process whose device memory
+ * is already committed to another pool.  All scratch (per-view table, line
+ * pairs, result staging) lives in one static 32 MiB device array that every
+ * GPU loading the library holds until exit; the call makes no cudaMalloc,
+ * cudaFree or other allocation.  Geometries needing more scratch (about
+ * size 1200 with 1800 views and as many rays) or more than 4096 views are
+ * rejected with RG_EINVAL.  The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress): make it before any stream capture.
+ * Calls share the array, so calls that overlap on the GPU race; each call
+ * rewrites all the scratch it reads, so nothing needs clearing between
+ * calls.                                                                     */
+int rg_radon_slantstack_noalloc(rg_image phantom, rg_image radon, void *stream);
+
 /* Pixel-driven backprojection with linear interpolation in t, scaled by
  * the view spacing.  Replaces raft_backprojection_slantstack
  * (raft/raft_backprojection_slantstack.c:43; bound at pyraft/raftypes.py:161).

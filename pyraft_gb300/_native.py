@@ -49,6 +49,7 @@ _SIGS = {
     "rg_version": ([], _c_int),
     "rg_radon_slantstack_workspace": ([_IMG, _IMG], _size_t),
     "rg_radon_slantstack": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
+    "rg_radon_slantstack_noalloc": ([_IMG, _IMG, _vp], _c_int),
     "rg_backprojection_slantstack_workspace": ([_IMG, _IMG], _size_t),
     "rg_backprojection_slantstack": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
     "rg_radon_transpose_slantstack_workspace": ([_IMG, _IMG], _size_t),

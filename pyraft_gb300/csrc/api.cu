@@ -221,6 +221,9 @@ static int check_ss(const rg_image &img, const rg_image &sino)
     return RG_OK;
 }
 
+int validate_ss(const rg_image &img, const rg_image &sino) { return check_ss(img, sino); }
+SSGeom make_ss_geom(const rg_image &img, const rg_image &sino) { return ss_geom(img, sino); }
+
 int check_ws(const void *ws)
 {
     if (ws && ((uintptr_t)ws & 255) != 0)

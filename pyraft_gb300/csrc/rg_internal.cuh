@@ -105,6 +105,10 @@ struct SSPlan {
 };
 
 int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv);
+int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View *hv);
+// Argument checks of the slant-stack entry points (api.cu).
+int validate_ss(const rg_image &img, const rg_image &sino);
+SSGeom make_ss_geom(const rg_image &img, const rg_image &sino);
 void ss_plan_free(SSPlan &p);
 
 // Kernel launchers (slantstack.cu).  Images handed to the kernels are

@@ -54,7 +54,9 @@ static bool to_q32(double v, long long &out)
     return true;
 }
 
-int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
+// Fills hv[0..nv) with the per-view constants and p's metadata (no device
+// work).  Shared by the cached plans and the no-allocation Radon entry point.
+int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View *hv)
 {
     if (g.N < 2 || g.R < 2 || g.A < 1)
         return set_error(RG_EINVAL, "slant-stack geometry needs size >= 2, nrays >= 2, "
@@ -68,7 +70,6 @@ int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
         return set_error(RG_EINVAL, "degenerate or non-finite corners");
     const double tol = 1.0 / sqrt(2);
 
-    std::vector<View> hv(nv);
     double wbp = 0.0, wadj = 0.0;
     bool adj_ok = true;
     for (int e = 0; e < nv; ++e) {
@@ -121,6 +122,14 @@ int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
     p.adj_ok = adj_ok;
     p.wmax_bp = (int)ceil(wbp + 1e-6) + 4;
     p.wmax_adj = (int)ceil(wadj + 1e-6) + 4;
+    return RG_OK;
+}
+
+int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
+{
+    std::vector<View> hv(nv > 0 ? nv : 1);
+    int rc = ss_views_compute(p, g, views, nv, hv.data());
+    if (rc) return rc;
     RG_CK(cudaGetDevice(&p.device));
     if (nv > 0) {
         RG_CK(cudaMalloc(&p.d_views, sizeof(View) * nv));
