@@ -39,8 +39,8 @@ METRIC = "FBP GUPS (2048^2 image, 1800 views, 2048 rays; Ram-Lak + slant-stack B
 UNIT = "GUPS"
 UPDATES = N * N * A
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) of one backprojection
-# launch at this size; profiles/bp_2048x1800_ncu.md.  None until captured.
-BP_TRAFFIC_BYTES = None
+# launch at this size (profiles/bp_2048x1800_ncu.md).
+BP_TRAFFIC_BYTES = 14957312
 
 
 def env_rank():
