@@ -149,18 +149,110 @@ def make_sinogram(torch, rg, seed):
     return s.contiguous()
 
 
+def make_osem_batch(torch, rg, nslices, seed):
+    """Config-5 style batch: N uniform over {256, 512, 1024, 2048}, views
+    uniform in [180, 1800], rays = N, random-ellipse emission phantoms,
+    Poisson counts with mean 50 per bin.  Returns (sinos, sizes) on the GPU
+    (sinograms as (rays, views) tensors)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    sinos, sizes = [], []
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    for k in range(nslices):
+        n = int(rng.choice([256, 512, 1024, 2048]))
+        a = int(rng.integers(180, 1801))
+        desc = rg.random_ellipses(12, rng)
+        ph = rg.phantom_fromdesc((n, n), desc, device=True)
+        ph = rg.gpu_image(torch.flip(ph.data, dims=[0]).abs().contiguous())
+        p = rg.radon(ph, (n, a), rg.radon_method.SLANTSTACK).data
+        lam = p.clamp(min=0) * (50.0 / max(float(p.mean()), 1e-9))
+        sinos.append(torch.poisson(lam, generator=gen).contiguous())
+        sizes.append((n, a))
+    return sinos, sizes
+
+
+def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7):
+    """Batched graph-captured OSEM vs the plain one-slice-per-call form on
+    the same slices.  The plain form is timed on the first `plain_slices`
+    slices (all, if None) and reported per slice."""
+    import numpy as np
+    from pyraft_gb300 import _native
+    from pyraft_gb300.raftypes import rg_image, workspace
+    L = _native.load()
+    sinos, sizes = make_osem_batch(torch, rg, nslices, seed)
+    S = (_native.RG_IMAGE * nslices)(*[rg_image(rg.gpu_image(s, (0.0, 1.0), (math.pi, -1.0)))
+                                        for s in sinos])
+    xs = [torch.ones((n, n), dtype=torch.float32, device="cuda") for n, _ in sizes]
+    I = (_native.RG_IMAGE * nslices)(*[rg_image(rg.gpu_image(x)) for x in xs])
+    wsb = L.rg_osem_batch_workspace(S, I, nslices, nsubsets)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    sp = torch.cuda.current_stream().cuda_stream
+
+    def run_batch(it):
+        for x in xs:
+            x.fill_(1.0)
+        _native.check(L.rg_osem_batch(S, I, nslices, it, nsubsets, 1, ws.data_ptr(), wsb, sp))
+    run_batch(1)                                     # warm-up (plans, graph path)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    run_batch(niter)
+    b.record()
+    b.synchronize()
+    t_batch = a.elapsed_time(b) * 1e-3
+    upd = sum(2.0 * n * n * v for n, v in sizes) * niter
+    m = nslices if plain_slices is None else min(plain_slices, nslices)
+    host = [s.cpu().numpy() for s in sinos[:m]]
+    out = np.zeros((2048, 2048), dtype=np.float32)
+    t0 = time.perf_counter()
+    for k in range(m):
+        n, v = sizes[k]
+        _native.check(L.rg_em_plain_host(out.ctypes.data, host[k].ctypes.data, n, n, v, niter,
+                                         nsubsets))
+    t_plain = time.perf_counter() - t0
+    frac = sum(sizes[k][0] ** 2 * sizes[k][1] for k in range(m)) / \
+        sum(n * n * v for n, v in sizes)
+    t_plain_all = t_plain / frac if m < nslices else t_plain
+    return {
+        "slices": nslices, "iterations": niter, "subsets": nsubsets,
+        "batched_slices_per_s": round(nslices / t_batch, 3),
+        "batched_s": round(t_batch, 3),
+        "batched_gups": round(upd / t_batch / 1e9, 1),
+        "plain_slices_per_s": round(nslices / t_plain_all, 3),
+        "plain_s": round(t_plain_all, 3),
+        "plain_timed_slices": m,
+        "plain_note": ("all slices timed" if m == nslices else
+                       f"first {m} slices timed, scaled by their share of N^2*views"),
+        "speedup": round(t_plain_all / t_batch, 2),
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="fbp", choices=["fbp", "osem"],
+                    help="fbp: the headline FBP line; osem: batched uneven OSEM "
+                         "(256 slices, 10 subsets x 20 iterations) vs the plain form")
+    ap.add_argument("--slices", type=int, default=256)
+    ap.add_argument("--iters", type=int, default=20)
+    ap.add_argument("--plain-slices", type=int, default=None)
     args = ap.parse_args()
     rank, world, local = env_rank()
     warm = max(3, args.warmup)
 
     if args.impl == "reference":
         return reference_arm(args, rank, world, warm)
+    if args.workload == "osem":
+        import torch
+        import pyraft_gb300 as rg
+        torch.cuda.set_device(local)
+        res = osem_compare(torch, rg, args.slices, args.iters, 10, args.plain_slices)
+        print(json.dumps({"workload": "batched uneven OSEM vs plain per-call form", **res}))
+        return
 
     import numpy as np
     import torch

@@ -178,15 +178,32 @@ int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets,
 
 /* ----------------------------------------------------------------------
  * Batched uneven OSEM: nslices independent reconstructions of different
- * sizes and view counts in one persistent launch per sub-iteration over a
- * (slice, tile) work queue.  Each slice s reads sinos[s] and updates
- * images[s] in place.  Work runs on `stream`; with graph != 0 the
- * iterations are captured once into a CUDA graph and replayed.           */
+ * sizes and view counts.  Each sub-iteration is three persistent launches
+ * (line pairs, Radon + ratio, adjoint + update) over (slice, tile) work
+ * queues.  Each slice k reads sinos[k] and updates images[k] in place
+ * (images hold x0 on entry).  Work runs on `stream`; with graph != 0 one
+ * iteration is captured into a CUDA graph on a private stream and replayed
+ * niter times on `stream` (do not call it while `stream` is itself being
+ * captured).  1 <= nsubsets <= 64, nsubsets <= every slice's view count.
+ * Replaces the reference's Python loop radon_3d_stack / per-slice em calls
+ * (pyraft/sinogram/sino.py:284-311, pyraft/iterative/em.py:151-169).       */
 size_t rg_osem_batch_workspace(const rg_image *sinos, const rg_image *images,
                                int nslices, int nsubsets);
 int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices,
                   int niter, int nsubsets, int graph,
                   void *workspace, size_t workspace_bytes, void *stream);
+
+/* The plain one-slice-per-call form the batched path is measured against:
+ * one slice (host float buffers, default geometry as the *_host wrappers),
+ * OSEM with nsubsets interleaved subsets (1 = plain EM), handled the way
+ * the reference's GPU EM handles a slice (raft/raft_em_gpu.cu:20-87): per
+ * call allocation and upload, then per sub-iteration separate Radon, ratio,
+ * backprojection, divide and multiply launches, each followed by a device
+ * synchronisation, with one-thread-per-output kernels (float positions,
+ * global loads); download and free.  Same operators (slant-stack Radon and
+ * matched adjoint) as rg_osem_batch.  h_out receives the iterate from x0 = 1. */
+int rg_em_plain_host(float *h_out, const float *h_sino, int size_image, int nrays,
+                     int nangles, int niter, int nsubsets);
 
 /* ----------------------------------------------------------------------
  * Ellipse phantoms (test inputs; replace raft_image_phantom_fromdesc,

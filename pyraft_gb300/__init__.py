@@ -10,7 +10,7 @@ from .sinogram import radon, radon_gpu, radon_method
 from .backprojection import backprojection, backprojection_gpu, backprojection_plan, radon_transpose
 from .filters import lowpassino_fbp, ramlak
 from .inversion import fbp, fbp_gpu
-from .iterative import em, em_gpu, make_em, osem
+from .iterative import em, em_gpu, em_plain, make_em, osem, osem_batch
 from .phantom import random_ellipses, shepplogan, phantom_fromdesc
 
 __version__ = "0.1.0"

@@ -69,6 +69,7 @@ _SIGS = {
     "rg_em": ([_IMG, _IMG, _c_int, _c_int, _c_int, _vp, _size_t, _vp], _c_int),
     "rg_osem_batch_workspace": ([_PI, _PI, _c_int, _c_int], _size_t),
     "rg_osem_batch": ([_PI, _PI, _c_int, _c_int, _c_int, _c_int, _vp, _size_t, _vp], _c_int),
+    "rg_em_plain_host": ([_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int], _c_int),
     "rg_phantom_fromdesc": ([_IMG, ctypes.POINTER(_c_double), _c_int, _vp], _c_int),
     "rg_radon_fromdesc": ([_IMG, ctypes.POINTER(_c_double), _c_int, _vp], _c_int),
     "rg_radon_slantstack_host": ([_vp, _vp, _c_int, _c_int, _c_int], _c_int),

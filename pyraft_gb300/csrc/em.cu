@@ -175,26 +175,4 @@ int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, vo
     return rc;
 }
 
-size_t rg_osem_batch_workspace(const rg_image *sinos, const rg_image *images, int nslices,
-                               int nsubsets)
-{
-    size_t m = 0;
-    for (int k = 0; k < nslices; ++k)
-        m = std::max(m, rg_em_workspace(sinos[k], images[k], RG_SLANTSTACK, nsubsets));
-    return m;
-}
-
-int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int niter, int nsubsets,
-                  int graph, void *ws, size_t wsb, void *stream)
-{
-    (void)graph;
-    if (nslices < 0 || (nslices > 0 && (!sinos || !images)))
-        return set_error(RG_EINVAL, "rg_osem_batch: bad slice arrays");
-    for (int k = 0; k < nslices; ++k) {
-        int rc = rg_em(sinos[k], images[k], RG_SLANTSTACK, niter, nsubsets, ws, wsb, stream);
-        if (rc) return rc;
-    }
-    return RG_OK;
-}
-
 }  // extern "C"

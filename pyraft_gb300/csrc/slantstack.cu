@@ -39,7 +39,7 @@
 #include <algorithm>
 #include <vector>
 
-#include "rg_internal.cuh"
+#include "ss_tiles.cuh"
 
 namespace rg {
 
@@ -150,47 +150,12 @@ void ss_plan_free(SSPlan &p)
 
 size_t radon_pairs_bytes(int N) { return (size_t)N * (N + 2) * sizeof(float2); }
 
-__device__ __forceinline__ float2 make_pair(float s0, float s1, bool valid)
-{
-    float d = s1 - s0;
-    return valid ? make_float2(s0 - d, d) : make_float2(0.f, 0.f);
-}
-
-// One CTA packs a 32 x 32 image tile into both orientations.
 __global__ __launch_bounds__(256) void k_line_pairs(const float *__restrict__ img, long long cs,
                                                     long long ls, int N,
                                                     float2 *__restrict__ prow,
                                                     float2 *__restrict__ pcol)
 {
-    __shared__ float t[33][33];
-    const int r0 = blockIdx.y * 32, c0 = blockIdx.x * 32;
-    const int pitch = N + 2;
-    for (int e = threadIdx.x; e < 33 * 33; e += 256) {
-        int y = e / 33, x = e % 33;
-        int r = r0 + y, c = c0 + x;
-        t[y][x] = (r < N && c < N) ? img[(long long)r * cs + (long long)c * ls] : 0.f;
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int y = w; y < 32; y += 8) {        // rows: consecutive lanes = columns
-        int r = r0 + y, c = c0 + lane;
-        if (r < N && c < N)
-            prow[(size_t)r * pitch + 1 + c] = make_pair(t[y][lane], t[y][lane + 1], c <= N - 2);
-    }
-    for (int x = w; x < 32; x += 8) {        // columns: consecutive lanes = rows
-        int c = c0 + x, r = r0 + lane;
-        if (r < N && c < N)
-            pcol[(size_t)c * pitch + 1 + r] = make_pair(t[lane][x], t[lane + 1][x], r <= N - 2);
-    }
-    // zero pads of the lines this tile starts / ends
-    if (c0 == 0 && threadIdx.x < 32 && r0 + lane < N) {
-        prow[(size_t)(r0 + lane) * pitch] = make_float2(0.f, 0.f);
-        prow[(size_t)(r0 + lane) * pitch + N + 1] = make_float2(0.f, 0.f);
-    }
-    if (r0 == 0 && threadIdx.x < 32 && c0 + lane < N) {
-        pcol[(size_t)(c0 + lane) * pitch] = make_float2(0.f, 0.f);
-        pcol[(size_t)(c0 + lane) * pitch + N + 1] = make_float2(0.f, 0.f);
-    }
+    line_pairs_tile(img, cs, ls, N, prow, pcol, blockIdx.x, blockIdx.y);
 }
 
 int launch_line_pairs(const float *img, long long cs, long long ls, int N, float2 *prow,
@@ -202,17 +167,6 @@ int launch_line_pairs(const float *img, long long cs, long long ls, int N, float
     return RG_OK;
 }
 
-// ============================================================================
-// Radon: CTA = 32 rays x 4 views (one warp per view).
-
-__device__ __forceinline__ void kahan_add(float &sum, float &c, float x)
-{
-    float y = x - c;
-    float t = sum + y;
-    c = (t - sum) - y;
-    sum = t;
-}
-
 template <bool RATIO>
 __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                const float2 *__restrict__ pcol, int N,
@@ -220,64 +174,8 @@ __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                float *__restrict__ out_am, int out_ld,
                                                const float *__restrict__ y_am, int y_ld)
 {
-    const int k = blockIdx.x * 32 + (threadIdx.x & 31);
-    const int e = blockIdx.y * 4 + (threadIdx.x >> 5);
-    if (e >= nv || k >= R) return;
-    const View v = views[e];
-    const int pitch = N + 2;
-    const float2 *__restrict__ base = (v.flags & kLinesAreRows) ? prow : pcol;
-
-    // Position on line 0 and per-line step, Q32.32.
-    const long long u0 = v.r0 + (long long)k * v.rk;
-    const long long q = v.ri;
-    // Lines whose sample lies in [-0.5, N - 0.5]: a superset of the valid
-    // samples [0, N-1) with half a sample of margin, and every index stays in
-    // [-1, N-1] (the pads).  Float error here is < 1e-3 samples.
-    const float uf0 = (float)u0 * 2.3283064365386963e-10f;
-    const float qf = (float)q * 2.3283064365386963e-10f;
-    int lo, hi;
-    if (fabsf(qf) < 1e-20f) {
-        bool in = uf0 >= -0.5f && uf0 <= (float)N - 0.5f;
-        lo = in ? 0 : 1;
-        hi = in ? N - 1 : 0;
-    } else {
-        float t1 = (-0.5f - uf0) / qf, t2 = ((float)N - 0.5f - uf0) / qf;
-        float tlo = fmaxf(fminf(t1, t2), 0.f), thi = fminf(fmaxf(t1, t2), (float)(N - 1));
-        lo = (int)ceilf(tlo);
-        hi = (int)floorf(thi);
-    }
-    // Exact check of the ends (positions are monotone in i): every sample
-    // index used stays in [-1, N-1], i.e. inside the padded line.
-    const long long ulo = -(1LL << 32), uhi = (long long)N << 32;
-    while (lo <= hi && (u0 + (long long)lo * q < ulo || u0 + (long long)lo * q >= uhi)) ++lo;
-    while (hi >= lo && (u0 + (long long)hi * q < ulo || u0 + (long long)hi * q >= uhi)) --hi;
-
-    float acc = 0.f, comp = 0.f;
-    if (lo <= hi) {
-        long long u = u0 + (long long)lo * q;
-        const float2 *__restrict__ line = base + (size_t)lo * pitch + 1;
-        int i = lo;
-        while (i <= hi) {
-            const int iend = min(hi, i + 31);
-            float part = 0.f;
-#pragma unroll 4
-            for (; i <= iend; ++i) {
-                const int n = (int)(u >> 32);
-                const float w1 = __uint_as_float(((unsigned)u >> 9) | 0x3F800000u);
-                const float2 pr = __ldg(line + n);
-                part += fmaf(w1, pr.y, pr.x);
-                u += q;
-                line += pitch;
-            }
-            kahan_add(acc, comp, part);
-        }
-    }
-    float val = (acc - comp) * v.delta;
-    if (RATIO) {
-        const float y = y_am[(size_t)v.view * y_ld + k];
-        val = (val != 0.f) ? y / val : 0.f;
-    }
-    out_am[(size_t)v.view * out_ld + k] = val;
+    radon_tile<RATIO>(prow, pcol, N, views, nv, R, out_am, out_ld, y_am, y_ld, blockIdx.x,
+                      blockIdx.y);
 }
 
 int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float *out_am,
@@ -295,78 +193,6 @@ int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float 
     return RG_OK;
 }
 
-// ============================================================================
-// Gathers (backprojection / matched adjoint).
-
-constexpr int kTile = 32;    // pixels per tile side
-constexpr int kSlots = 32;   // views per staged chunk
-constexpr int kRows = 4;     // rows per thread (8 warps x 4 = 32)
-
-struct SlotInfo {
-    unsigned base;   // Q9.23 position of the tile origin within the window
-    int a;           // Q9.23 step per column
-    int b;           // Q9.23 step per row
-    int nlo;         // first staged sample index (INT_MIN: empty slot)
-};
-
-// Inner loop over the staged views of one chunk for one thread's 4 pixels.
-//
-// Adjoint weights: with kappa the ray-index position of the pixel's ray,
-// k0 = floor(kappa), f = kappa - k0, the rays k0 and k0+1 sample the pixel's
-// line at u - m = -p f and p (1 - f); their hat weights are 1 - P f and
-// 1 - P (1 - f), clipped at 0 (P = |p| >= 1, so no other ray reaches the
-// pixel).  At line positions m = 0 and m = N-1 the Radon drops samples with
-// u < 0 and u >= N-1; BORDER applies exactly that rule.
-template <int MODE, int WMAX, bool BORDER, typename Acc>
-__device__ __forceinline__ void accumulate(Acc (&part)[kRows], const float2 *__restrict__ pairs,
-                                           const SlotInfo *slot, const float *slotP,
-                                           const int *slotFlags, int nslot, int lane, int warp,
-                                           int col, int myrow, int N)
-{
-    for (int s = 0; s < nslot; ++s) {
-        const SlotInfo si = slot[s];
-        if (si.nlo == INT_MIN) continue;
-        const float2 *__restrict__ pw = pairs + s * WMAX;
-        unsigned vpos = si.base + (unsigned)(lane * si.a) + (unsigned)(warp * kRows * si.b);
-        if (MODE == 0) {
-#pragma unroll
-            for (int r = 0; r < kRows; ++r) {
-                const float w1 = __uint_as_float((vpos & 0x7FFFFFu) | 0x3F800000u);
-                const float2 pr = pw[vpos >> 23];
-                part[r] += fmaf(w1, pr.y, pr.x);
-                vpos += (unsigned)si.b;
-            }
-        } else {
-            const float P = slotP[s];
-            const float c0 = 1.f + P, c1 = 1.f - 2.f * P;
-            int fl = 0;
-            if (BORDER) fl = slotFlags[s];
-            const bool pneg = (fl & kRkNegative) != 0;
-#pragma unroll
-            for (int r = 0; r < kRows; ++r) {
-                const float w1 = __uint_as_float((vpos & 0x7FFFFFu) | 0x3F800000u);
-                const float2 pr = pw[vpos >> 23];
-                float wa = fmaxf(0.f, fmaf(-P, w1, c0));
-                float wb = fmaxf(0.f, fmaf(P, w1, c1));
-                if (BORDER) {
-                    const int m = (fl & kLinesAreRows) ? col : (myrow + r);
-                    const bool f0 = (w1 == 1.0f);
-                    if (m == 0) {                       // drop u < 0
-                        if (!pneg && !f0) wa = 0.f;
-                        if (pneg) wb = 0.f;
-                    } else if (m == N - 1) {            // drop u >= N-1
-                        if (pneg || f0) wa = 0.f;
-                        if (!pneg) wb = 0.f;
-                    }
-                }
-                part[r] += (Acc)fmaf(pr.x, wa, pr.y * wb);
-                vpos += (unsigned)si.b;
-            }
-        }
-    }
-}
-
-// MODE 0: backprojection; 1: adjoint (FP32 accumulate); 2: adjoint, FP64.
 template <int MODE, int WMAX, bool EM>
 __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, int s_ld, int R,
                                                 const View *__restrict__ views, int nv, int N,
@@ -377,122 +203,8 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
                                                 int *__restrict__ err)
 {
     extern __shared__ float2 pairs[];          // [kSlots][WMAX]
-    __shared__ SlotInfo slot[kSlots];
-    __shared__ float slotP[kSlots];
-    __shared__ int slotFlags[kSlots];
-    using Acc = typename std::conditional<MODE == 2, double, float>::type;
-
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int row0 = blockIdx.y * kTile, col0 = blockIdx.x * kTile;
-    const int col = col0 + lane;
-    const int myrow = row0 + warp * kRows;
-    const bool border = row0 == 0 || col0 == 0 || row0 + kTile >= N || col0 + kTile >= N;
-
-    Acc acc[kRows], comp[kRows];
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) { acc[r] = 0; comp[r] = 0; }
-
-    for (int chunk = 0; chunk < nv; chunk += kSlots) {
-        const int nslot = min(kSlots, nv - chunk);
-        if (warp == 0) {
-            SlotInfo si = {0u, 0, 0, INT_MIN};
-            float P = 0.f;
-            int flags = 0;
-            if (lane < nslot) {
-                const View v = views[chunk + lane];
-                long long cr, cc, c0;
-                if (MODE == 0) { cr = v.brow; cc = v.bcol; c0 = v.b0; }
-                else           { cr = v.krow; cc = v.kcol; c0 = v.k0; }
-                const long long origin = c0 + (long long)row0 * cr + (long long)col0 * cc;
-                const long long dr = 31LL * cr, dc = 31LL * cc;
-                const long long mn = origin + min(0LL, dr) + min(0LL, dc);
-                const long long mx = origin + max(0LL, dr) + max(0LL, dc);
-                const int nlo = (int)(mn >> 32) - 1;
-                const int nhi = (int)(mx >> 32) + 1;
-                if (nhi - nlo + 1 <= WMAX) {
-                    si.nlo = nlo;
-                    si.base = (unsigned)((origin - ((long long)nlo << 32)) >> 9);
-                    si.a = (int)((cc + 256) >> 9);
-                    si.b = (int)((cr + 256) >> 9);
-                } else if (err) {
-                    atomicOr(err, 1);
-                }
-                P = v.P;
-                flags = v.flags;
-            }
-            slot[lane] = si;
-            slotP[lane] = P;
-            slotFlags[lane] = flags;
-        }
-        __syncthreads();
-
-        // Stage the windows.
-        for (int e = threadIdx.x; e < nslot * WMAX; e += 256) {
-            const int s = e / WMAX, w = e - s * WMAX;
-            const int nlo = slot[s].nlo;
-            float2 pr = make_float2(0.f, 0.f);
-            if (nlo != INT_MIN) {
-                const View &v = views[chunk + s];
-                const float *__restrict__ row = s_am + (size_t)v.view * s_ld;
-                const int n = nlo + w;
-                if (MODE == 0) {
-                    if (n >= 0 && n <= R - 2) {
-                        const float s0 = __ldg(row + n), s1 = __ldg(row + n + 1);
-                        pr = make_pair(s0, s1, true);
-                    }
-                } else {
-                    const float d = v.delta;
-                    const float s0 = (n >= 0 && n < R) ? __ldg(row + n) : 0.f;
-                    const float s1 = (n + 1 >= 0 && n + 1 < R) ? __ldg(row + n + 1) : 0.f;
-                    pr = make_float2(s0 * d, s1 * d);
-                }
-            }
-            pairs[e] = pr;
-        }
-        __syncthreads();
-
-        // Accumulate.  Border tiles of the adjoint apply the reference's
-        // sample validity at positions 0 and N-1 of a line (CTA-uniform branch).
-        Acc part[kRows];
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) part[r] = 0;
-        if (MODE != 0 && border)
-            accumulate<MODE, WMAX, true, Acc>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                              warp, col, myrow, N);
-        else
-            accumulate<MODE, WMAX, false, Acc>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                               warp, col, myrow, N);
-#pragma unroll
-        for (int r = 0; r < kRows; ++r) {
-            if (MODE == 2) {
-                acc[r] += part[r];
-            } else {
-                float a = acc[r], c = comp[r];
-                kahan_add(a, c, (float)part[r]);
-                acc[r] = a; comp[r] = c;
-            }
-        }
-        __syncthreads();
-    }
-
-    if (col >= N) return;
-#pragma unroll
-    for (int r = 0; r < kRows; ++r) {
-        const int row = myrow + r;
-        if (row >= N) break;
-        if (MODE == 2) {
-            const double sv = (double)acc[r];
-            out[(long long)row * cs + (long long)col * ls] = (sv > 0.0) ? (float)(1.0 / sv) : 0.f;
-        } else {
-            const float val = ((float)acc[r] - (float)comp[r]) * scale;
-            if (EM) {
-                const size_t idx = (size_t)row * N + col;
-                em_x[idx] = em_x[idx] * val * inv_sens[idx];
-            } else {
-                out[(long long)row * cs + (long long)col * ls] = val;
-            }
-        }
-    }
+    gather_tile<MODE, WMAX, EM>(s_am, s_ld, R, views, nv, N, scale, out, cs, ls, em_x, inv_sens,
+                                err, blockIdx.x, blockIdx.y, pairs);
 }
 
 template <int MODE, int WMAX, bool EM>

@@ -109,3 +109,48 @@ def em_gpu(*args):
                 bottom_right=(numpy.pi, -1.0))
     out = em(src, (n, n), niter, method=radon_method.SLANTSTACK)
     return numpy.asarray(out, dtype=numpy.float32)
+
+
+def osem_batch(sinos, shapes=None, niter=5, nsubsets=10, graph=True, x0=None):
+    """OSEM of many independent slices of uneven size in one batched call.
+
+    sinos: list of (nrays_k, nviews_k) sinograms (image or gpu_image, corners
+    as for osem).  shapes: list of (N_k, N_k) (default nrays_k) or None.
+    x0: optional list of start images (default ones).  Every sub-iteration is
+    three persistent launches over all slices; with graph=True one iteration
+    is captured into a CUDA graph and replayed niter times.  Returns a list
+    of results of the same kinds as the inputs."""
+    import ctypes
+    import torch
+    L = _native.load()
+    gs, hosts, xs = [], [], []
+    for k, s in enumerate(sinos):
+        g, host = to_gpu(s, (0.0, 1.0), (numpy.pi, -1.0))
+        gs.append(g)
+        hosts.append(host)
+        n = (shapes[k][0] if shapes is not None else g.shape[0])
+        if x0 is not None:
+            xg, _ = to_gpu(x0[k])
+            xs.append(gpu_image(xg.data.clone(), xg.top_left, xg.bottom_right))
+        else:
+            x = new_gpu((n, n), (-1.0, 1.0), (1.0, -1.0))
+            x.data.fill_(1.0)
+            xs.append(x)
+    n = len(gs)
+    S = (_native.RG_IMAGE * max(n, 1))(*[rg_image(g) for g in gs])
+    I = (_native.RG_IMAGE * max(n, 1))(*[rg_image(x) for x in xs])
+    ws_t, ws = workspace(L.rg_osem_batch_workspace(S, I, n, nsubsets))
+    _native.check(L.rg_osem_batch(S, I, n, int(niter), int(nsubsets), 1 if graph else 0, ws,
+                                  ws_t.numel() if ws_t is not None else 0, stream_ptr()))
+    return [finish(x, h) for x, h in zip(xs, hosts)]
+
+
+def em_plain(sino, size=None, niter=5, nsubsets=1):
+    """The plain one-slice-per-call GPU form (rg_em_plain_host): host
+    sinogram on the default geometry -> (size, size) float32 array."""
+    s = numpy.ascontiguousarray(numpy.asarray(sino), dtype=numpy.float32)
+    n = size or s.shape[0]
+    out = numpy.zeros((n, n), dtype=numpy.float32)
+    _native.check(_native.load().rg_em_plain_host(
+        out.ctypes.data, s.ctypes.data, n, s.shape[0], s.shape[1], int(niter), int(nsubsets)))
+    return out
