@@ -228,13 +228,45 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7):
     }
 
 
+def tvls_run(torch, rg, nslices=64, n=512, nviews=360, steps=200, seed=11):
+    """Config-4 workload: 64 random-ellipse slices of 512^2, 360 views, 512
+    rays, Gaussian noise sigma = 1% of max; TV-regularised least squares
+    (lambda 1e-3) with 200 Adam steps through the autograd Radon pair."""
+    import numpy as np
+    from pyraft_gb300 import autograd as AG, recon
+    rng = np.random.default_rng(seed)
+    xs = []
+    for _ in range(nslices):
+        ph = rg.phantom_fromdesc((n, n), rg.random_ellipses(40, rng), device=True)
+        xs.append(torch.flip(ph.data, dims=[0]))
+    x_true = torch.stack(xs).contiguous()
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    y = AG.radon_forward(x_true, n, nviews)
+    y = y + 0.01 * float(y.max()) * torch.randn(y.shape, device="cuda", generator=gen)
+    recon.tv_ls(y, n, niter=3)                                   # warm-up / plans
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    x, losses = recon.tv_ls(y, n, niter=steps, lam=1e-3, lr=2e-2)
+    b.record()
+    b.synchronize()
+    t = a.elapsed_time(b) * 1e-3
+    upd = 2.0 * nslices * n * n * nviews * steps                  # forward + adjoint per step
+    err = float(torch.linalg.norm(x - x_true) / torch.linalg.norm(x_true))
+    return {"slices": nslices, "size": n, "views": nviews, "steps": steps,
+            "seconds": round(t, 3), "ms_per_step": round(1e3 * t / steps, 3),
+            "operator_gups": round(upd / t / 1e9, 1), "final_loss": losses[-1],
+            "loss_ratio": losses[-1] / losses[0], "rel_error_vs_truth": round(err, 4)}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fbp", choices=["fbp", "osem"],
+    ap.add_argument("--workload", default="fbp", choices=["fbp", "osem", "tvls"],
                     help="fbp: the headline FBP line; osem: batched uneven OSEM "
                          "(256 slices, 10 subsets x 20 iterations) vs the plain form")
     ap.add_argument("--slices", type=int, default=256)
@@ -246,6 +278,13 @@ def main():
 
     if args.impl == "reference":
         return reference_arm(args, rank, world, warm)
+    if args.workload == "tvls":
+        import torch
+        import pyraft_gb300 as rg
+        torch.cuda.set_device(local)
+        print(json.dumps({"workload": "TV-regularised LS, 64 x 512^2, 360 views, 200 Adam steps",
+                          **tvls_run(torch, rg)}))
+        return
     if args.workload == "osem":
         import torch
         import pyraft_gb300 as rg

@@ -112,6 +112,34 @@ size_t rg_radon_transpose_slantstack_workspace(rg_image sinogram, rg_image image
 int rg_radon_transpose_slantstack(rg_image sinogram, rg_image image,
                                   void *workspace, size_t workspace_bytes, void *stream);
 
+/* Stacks of equal-geometry problems in one launch per kernel (grid z).
+ * phantom/image/radon/sino describe the first member; consecutive members
+ * are *_stride floats apart.  Same results as nstack separate calls.  Used
+ * by the batched autograd operator (no reference counterpart: the
+ * reference loops over slices in Python, pyraft/sinogram/sino.py:307-310). */
+size_t rg_radon_slantstack_stack_workspace(rg_image phantom, rg_image radon, int nstack);
+int rg_radon_slantstack_stack(rg_image phantom, long long phantom_stride, rg_image radon,
+                              long long radon_stride, int nstack,
+                              void *workspace, size_t workspace_bytes, void *stream);
+size_t rg_radon_transpose_slantstack_stack_workspace(rg_image sino, rg_image image, int nstack);
+int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg_image image,
+                                        long long image_stride, int nstack,
+                                        void *workspace, size_t workspace_bytes, void *stream);
+
+/* FP64 slant-stack Radon and its exact transpose (same sample positions,
+ * FP64 weights and sums; the transpose scatters with FP64 atomics into a
+ * contiguous image it zeroes first).  For float64 gradient checks of the
+ * autograd operator; the FP32 entry points above are the fast path.  The
+ * layout is rg_image's with double data.  (The reference's C path is FP64,
+ * raft/raft_radon_slantstack.c:122-214; no transpose exists there.)        */
+typedef struct {
+    double *data;
+    int lines, line_stride, columns, column_stride;
+    double tl_x, tl_y, br_x, br_y;
+} rg_image_f64;
+int rg_radon_slantstack_f64(rg_image_f64 phantom, rg_image_f64 radon, void *stream);
+int rg_radon_transpose_slantstack_f64(rg_image_f64 sino, rg_image_f64 image, void *stream);
+
 /* ----------------------------------------------------------------------
  * DDA (Bresenham) projector pair (rectangular images, top-down rows).
  * -------------------------------------------------------------------- */

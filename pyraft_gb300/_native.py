@@ -42,7 +42,17 @@ class RG_IMAGE(ctypes.Structure):
                 ("br_x", _c_double), ("br_y", _c_double)]
 
 
+class RG_IMAGE_F64(ctypes.Structure):
+    """rg_image_f64: rg_image over device doubles."""
+    _fields_ = [("data", _vp), ("lines", _c_int), ("line_stride", _c_int),
+                ("columns", _c_int), ("column_stride", _c_int),
+                ("tl_x", _c_double), ("tl_y", _c_double),
+                ("br_x", _c_double), ("br_y", _c_double)]
+
+
 _IMG = RG_IMAGE
+_IMG64 = RG_IMAGE_F64
+_ll = ctypes.c_longlong
 _PI = ctypes.POINTER(RG_IMAGE)
 _SIGS = {
     "rg_last_error": ([], ctypes.c_char_p),
@@ -50,6 +60,13 @@ _SIGS = {
     "rg_radon_slantstack_workspace": ([_IMG, _IMG], _size_t),
     "rg_radon_slantstack": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
     "rg_radon_slantstack_noalloc": ([_IMG, _IMG, _vp], _c_int),
+    "rg_radon_slantstack_stack_workspace": ([_IMG, _IMG, _c_int], _size_t),
+    "rg_radon_slantstack_stack": ([_IMG, _ll, _IMG, _ll, _c_int, _vp, _size_t, _vp], _c_int),
+    "rg_radon_transpose_slantstack_stack_workspace": ([_IMG, _IMG, _c_int], _size_t),
+    "rg_radon_transpose_slantstack_stack": ([_IMG, _ll, _IMG, _ll, _c_int, _vp, _size_t, _vp],
+                                            _c_int),
+    "rg_radon_slantstack_f64": ([_IMG64, _IMG64, _vp], _c_int),
+    "rg_radon_transpose_slantstack_f64": ([_IMG64, _IMG64, _vp], _c_int),
     "rg_backprojection_slantstack_workspace": ([_IMG, _IMG], _size_t),
     "rg_backprojection_slantstack": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
     "rg_radon_transpose_slantstack_workspace": ([_IMG, _IMG], _size_t),

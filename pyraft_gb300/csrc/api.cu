@@ -9,6 +9,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -236,6 +237,81 @@ static bool is_view_major(const rg_image &s)
     return s.column_stride == 1 && s.line_stride == s.lines;
 }
 
+// ----------------------------------------------------------------------------
+// Autotuner for the gather tile height (rows per thread: 4 -> 32x32 tiles,
+// 8 -> 32x64 tiles).  The first out-of-place backprojection or adjoint of a
+// geometry times both variants on the caller's own buffers (two timed runs
+// each, CUDA events on the caller's stream; this first call synchronises)
+// and keeps the faster one for the process.  Calls made while the stream
+// is being captured never tune; they use the cached choice or 4.  The
+// environment variable RG_GATHER_ROWS=4|8 forces a choice.
+
+static std::mutex g_tune_mu;
+static std::map<std::string, int> g_tune;
+
+static std::string tune_key(const SSPlan &p, int mode)
+{
+    KeyBuilder kb;
+    kb.add(current_device()).add(mode == 2 ? 1 : mode).add(p.g.N).add(p.g.R).add(p.nv)
+        .add(p.wmax_bp[0]).add(p.wmax_adj[0]);
+    return kb.s;
+}
+
+static int env_rows()
+{
+    const char *e = getenv("RG_GATHER_ROWS");
+    if (!e) return 0;
+    const int v = atoi(e);
+    return (v == 4 || v == 8) ? v : 0;
+}
+
+int tuned_rows(const SSPlan &p, int mode)
+{
+    if (int v = env_rows()) return v;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune.find(tune_key(p, mode));
+    return it == g_tune.end() ? 4 : it->second;
+}
+
+static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
+                           long long cs, long long ls, cudaStream_t st)
+{
+    if (env_rows()) return RG_OK;
+    const std::string key = tune_key(p, mode);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        if (g_tune.count(key)) return RG_OK;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    RG_CK(cudaStreamIsCapturing(st, &cap));
+    if (cap != cudaStreamCaptureStatusNone) return RG_OK;
+    cudaEvent_t a, b;
+    RG_CK(cudaEventCreate(&a));
+    RG_CK(cudaEventCreate(&b));
+    float best = 1e30f;
+    int pick = 4, rc = RG_OK;
+    for (int rows : {4, 8}) {
+        float tsum = 0.f;
+        for (int rep = 0; rep < 3 && !rc; ++rep) {
+            cudaEventRecord(a, st);
+            rc = launch_gather(p, mode, s_am, s_ld, out, cs, ls, nullptr, nullptr, nullptr, st, rows);
+            cudaEventRecord(b, st);
+            cudaError_t e = cudaEventSynchronize(b);
+            if (!rc && e != cudaSuccess) rc = cuda_error(e, "autotune");
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, a, b);
+            if (rep > 0) tsum += ms;
+        }
+        if (!rc && tsum < best) { best = tsum; pick = rows; }
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (rc) return rc;
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune[key] = pick;
+    return RG_OK;
+}
+
 // Helpers for em.cu: hand out plans with an opaque owner handle
 // (a heap-allocated std::shared_ptr<void>, released by release_holder).
 int get_ss_plan(const SSGeom &g, int stride, int first, const SSPlan **out, void **holder)
@@ -299,6 +375,127 @@ int rg_radon_slantstack(rg_image phantom, rg_image radon, void *ws, size_t wsb, 
     return rc;
 }
 
+// ---------------------------------------------------------------- stacks
+size_t rg_radon_slantstack_stack_workspace(rg_image phantom, rg_image radon, int nstack)
+{
+    const int N = phantom.lines;
+    const size_t am = is_view_major(radon) ? 0 : (size_t)radon.lines * radon.columns * sizeof(float);
+    return ws_total({radon_pairs_bytes(N) * (size_t)nstack, radon_pairs_bytes(N) * (size_t)nstack,
+                     am * (size_t)nstack});
+}
+
+int rg_radon_slantstack_stack(rg_image phantom, long long phantom_stride, rg_image radon,
+                              long long radon_stride, int nstack, void *ws, size_t wsb,
+                              void *stream)
+{
+    int rc = check_ss(phantom, radon);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    if (nstack < 1 || nstack > 65535) return set_error(RG_EINVAL, "stack size must be in [1, 65535]");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(phantom, radon), 1, 0, ph))) return rc;
+    const int N = phantom.lines, R = radon.lines, A = radon.columns;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_radon_slantstack_stack_workspace(phantom, radon, nstack), st)))
+        return rc;
+    const long long zp = (long long)N * (N + 2);
+    float2 *prow = (float2 *)s.take(radon_pairs_bytes(N) * (size_t)nstack);
+    float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N) * (size_t)nstack);
+    const bool direct = is_view_major(radon);
+    float *out_am = direct ? radon.data : (float *)s.take((size_t)R * A * sizeof(float) * nstack);
+    const long long zo = direct ? radon_stride : (long long)R * A;
+    if (!(rc = launch_line_pairs(phantom.data, phantom.column_stride, phantom.line_stride, N, prow,
+                                 pcol, st, nstack, phantom_stride, zp)))
+        rc = launch_radon(ph->p, prow, pcol, out_am, R, nullptr, 0, st, nstack, zp, zo);
+    for (int z = 0; z < nstack && !rc && !direct; ++z)
+        rc = launch_from_am(out_am + (size_t)z * R * A, R, A, radon.data + z * radon_stride,
+                            radon.column_stride, radon.line_stride, st);
+    scratch_end(s);
+    return rc;
+}
+
+size_t rg_radon_transpose_slantstack_stack_workspace(rg_image sino, rg_image image, int nstack)
+{
+    (void)image;
+    return is_view_major(sino) ? 0
+                               : ws_total({(size_t)sino.lines * sino.columns * sizeof(float) * nstack});
+}
+
+int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg_image image,
+                                        long long image_stride, int nstack, void *ws, size_t wsb,
+                                        void *stream)
+{
+    int rc = check_ss(image, sino);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    if (nstack < 1 || nstack > 65535) return set_error(RG_EINVAL, "stack size must be in [1, 65535]");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(image, sino), 1, 0, ph))) return rc;
+    const int R = sino.lines, A = sino.columns;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_radon_transpose_slantstack_stack_workspace(sino, image, nstack), st)))
+        return rc;
+    const float *s_am = sino.data;
+    long long zs = sino_stride;
+    if (!is_view_major(sino)) {
+        float *t = (float *)s.take((size_t)R * A * sizeof(float) * nstack);
+        for (int z = 0; z < nstack && !rc; ++z)
+            rc = launch_to_am(sino.data + z * sino_stride, sino.column_stride, sino.line_stride, R,
+                              A, t + (size_t)z * R * A, st);
+        s_am = t;
+        zs = (long long)R * A;
+    }
+    Stack zz;
+    zz.n = nstack;
+    zz.in = zs;
+    zz.out = image_stride;
+    if (!rc)
+        rc = launch_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
+                           nullptr, nullptr, nullptr, st, 0, zz);
+    scratch_end(s);
+    return rc;
+}
+
+// ---------------------------------------------------------------- FP64 pair
+static rg_image as_f32_view(const rg_image_f64 &d)
+{
+    rg_image im;
+    im.data = (float *)d.data;
+    im.lines = d.lines; im.line_stride = d.line_stride;
+    im.columns = d.columns; im.column_stride = d.column_stride;
+    im.tl_x = d.tl_x; im.tl_y = d.tl_y; im.br_x = d.br_x; im.br_y = d.br_y;
+    return im;
+}
+
+int rg_radon_slantstack_f64(rg_image_f64 phantom, rg_image_f64 radon, void *stream)
+{
+    const rg_image a = as_f32_view(phantom), b = as_f32_view(radon);
+    int rc = check_ss(a, b);
+    if (rc) return rc;
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(a, b), 1, 0, ph))) return rc;
+    return launch_radon_f64(ph->p, phantom.data, phantom.column_stride, phantom.line_stride,
+                            radon.data, radon.column_stride, radon.line_stride,
+                            (cudaStream_t)stream);
+}
+
+int rg_radon_transpose_slantstack_f64(rg_image_f64 sino, rg_image_f64 image, void *stream)
+{
+    const rg_image a = as_f32_view(image), b = as_f32_view(sino);
+    int rc = check_ss(a, b);
+    if (rc) return rc;
+    if (image.column_stride != image.columns || image.line_stride != 1)
+        return set_error(RG_EINVAL, "FP64 transpose writes a contiguous image");
+    std::shared_ptr<PlanHolder> ph;
+    if ((rc = get_plan(ss_geom(a, b), 1, 0, ph))) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    RG_CK(cudaMemsetAsync(image.data, 0, sizeof(double) * image.lines * image.columns, st));
+    return launch_radon_transpose_f64(ph->p, sino.data, sino.column_stride, sino.line_stride,
+                                      image.data, st);
+}
+
 // ---------------------------------------------------------------- gathers
 static size_t gather_ws(const rg_image &sino)
 {
@@ -322,6 +519,8 @@ static int run_gather(int mode, rg_image sino, rg_image img, void *ws, size_t ws
         rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, t, st);
         s_am = t;
     }
+    if (!rc)
+        rc = autotune_gather(ph->p, mode, s_am, R, img.data, img.column_stride, img.line_stride, st);
     if (!rc)
         rc = launch_gather(ph->p, mode, s_am, R, img.data, img.column_stride, img.line_stride,
                            nullptr, nullptr, nullptr, st);
@@ -454,7 +653,8 @@ int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *
         rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, a, st);
         src = a;
     }
-    if (!rc && !(rc = launch_conv_rows(src, b, R, A, (const float *)taps->p, st)))
+    if (!rc && !(rc = launch_conv_rows(src, b, R, A, (const float *)taps->p, st)) &&
+        !(rc = autotune_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride, st)))
         rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
                            nullptr, nullptr, nullptr, st);
     scratch_end(s);

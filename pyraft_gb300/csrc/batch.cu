@@ -81,6 +81,8 @@ __global__ __launch_bounds__(256) void k_batch_pairs(const BatchSlice *__restric
     }
 }
 
+// VPT: views per thread (radon_tile with 4 views per CTA, or radon_tile2 with 8).
+template <int VPT>
 __global__ __launch_bounds__(128) void k_batch_radon(const BatchSlice *__restrict__ d, int n,
                                                      int total, int *counter)
 {
@@ -89,12 +91,19 @@ __global__ __launch_bounds__(128) void k_batch_radon(const BatchSlice *__restric
         if (item >= total) break;
         const BatchSlice &b = d[find_slice(d, n, item, kRadon)];
         const int local = item - b.begin[kRadon], rb = (b.R + 31) / 32;
-        radon_tile<true>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am, b.R,
-                         local % rb, local / rb);
+        if (VPT == 2)
+            radon_tile2<true>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
+                              b.R, local % rb, local / rb);
+        else
+            radon_tile<true>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
+                             b.R, local % rb, local / rb);
     }
 }
 
 // MODE 1: adjoint with the EM update; MODE 2: FP64 sensitivity -> inv_sens.
+// Tiles are 32 columns x 8*kBatchRows rows.
+constexpr int kBatchRows = 4;
+
 template <int MODE, int WMAX>
 __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restrict__ d, int n,
                                                       int total, int *counter)
@@ -106,13 +115,13 @@ __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restri
         const BatchSlice &b = d[find_slice(d, n, item, kGather)];
         const int local = item - b.begin[kGather], tiles = (b.N + 31) / 32;
         if (MODE == 1)
-            gather_tile<1, WMAX, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f, nullptr, 0,
-                                       0, b.x, b.inv_sens, nullptr, local % tiles, local / tiles,
-                                       pairs);
+            gather_tile<1, WMAX, kBatchRows, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
+                                                   nullptr, 0, 0, b.x, b.inv_sens, nullptr,
+                                                   local % tiles, local / tiles, pairs);
         else
-            gather_tile<2, WMAX, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
-                                        b.inv_sens, b.N, 1, nullptr, nullptr, nullptr,
-                                        local % tiles, local / tiles, pairs);
+            gather_tile<2, WMAX, kBatchRows, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
+                                                    b.inv_sens, b.N, 1, nullptr, nullptr, nullptr,
+                                                    local % tiles, local / tiles, pairs);
     }
 }
 
@@ -129,7 +138,7 @@ int persistent_grid(K kernel, int threads, size_t smem, int items, int *out)
 }
 
 struct BatchRun {
-    int n = 0, S = 0, wmax = 64;
+    int n = 0, S = 0, wmax = 64, vpt = 2;
     int total[3][64] = {};            // [kind][subset] item counts (subset 0 for pairs)
     int grid[4][64] = {};             // persistent grids: pairs, radon[s], gather1, gather2
     BatchSlice *d_desc = nullptr;     // S x n descriptors (device, in scratch)
@@ -143,7 +152,8 @@ int prepare_grids(BatchRun &br)
     const size_t smem = (size_t)kSlots * WMAX * sizeof(float2);
     if (int rc = persistent_grid(k_batch_pairs, 256, 0, br.total[kLP][0], &br.grid[0][0])) return rc;
     for (int s = 0; s < br.S; ++s)
-        if (int rc = persistent_grid(k_batch_radon, 128, 0, br.total[kRadon][s], &br.grid[1][s]))
+        if (int rc = persistent_grid(br.vpt == 2 ? k_batch_radon<2> : k_batch_radon<1>, 128, 0,
+                                     br.total[kRadon][s], &br.grid[1][s]))
             return rc;
     if (int rc = persistent_grid(k_batch_gather<1, WMAX>, 256, smem, br.total[kGather][0],
                                  &br.grid[2][0]))
@@ -162,7 +172,12 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
         k_batch_pairs<<<br.grid[0][0], 256, 0, st>>>(d, br.n, br.total[kLP][0], br.counter);
         RG_CK_LAUNCH("k_batch_pairs");
         RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
-        k_batch_radon<<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s], br.counter);
+        if (br.vpt == 2)
+            k_batch_radon<2><<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s],
+                                                            br.counter);
+        else
+            k_batch_radon<1><<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s],
+                                                            br.counter);
         RG_CK_LAUNCH("k_batch_radon");
         RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
         k_batch_gather<1, WMAX><<<br.grid[2][0], 256, smem, st>>>(d, br.n, br.total[kGather][0],
@@ -387,12 +402,14 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
             const SSPlan *p = plans[(size_t)q * S + s];
             if (!p->adj_ok)
                 return set_error(RG_EUNSUPPORTED, "slice %d: nrays must not exceed the image size", k);
-            wneed = std::max(wneed, p->wmax_adj);
+            wneed = std::max(wneed, p->wmax_adj[kBatchRows == 8 ? 1 : 0]);
         }
     }
     BatchRun br;
     br.n = nslices;
     br.S = S;
+    br.vpt = radon_views_per_thread(*plans[0]);
+    const int vpb = br.vpt == 2 ? 8 : 4;   // views per Radon item
     br.wmax = wneed <= 64 ? 64 : wneed <= 128 ? 128 : wneed <= 256 ? 256 : 512;
     if (wneed > 512) return set_error(RG_EUNSUPPORTED, "gather window of %d exceeds 512", wneed);
 
@@ -422,7 +439,7 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
         rc = launch_to_am(si.data, si.column_stride, si.line_stride, R, A, y, st);
         if (!rc) rc = launch_copy2d(im.data, im.column_stride, im.line_stride, x, N, 1, N, N, st);
         if (!rc) rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
-        const int tiles = (N + 31) / 32;
+        const int tiles = (N + 31) / 32, tiles_y = (N + 8 * kBatchRows - 1) / (8 * kBatchRows);
         for (int s = 0; s < S; ++s) {
             BatchSlice &d = hd[(size_t)s * nslices + q];
             const SSPlan *p = plans[(size_t)q * S + s];
@@ -439,10 +456,10 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
             d.begin[kLP] = items_lp;
             d.begin[kRadon] = items_r[s];
             d.begin[kGather] = items_g;
-            items_r[s] += ((R + 31) / 32) * ((p->nv + 3) / 4);
+            items_r[s] += ((R + 31) / 32) * ((p->nv + vpb - 1) / vpb);
         }
         items_lp += tiles * tiles;
-        items_g += tiles * tiles;
+        items_g += tiles * tiles_y;
     }
     br.total[kLP][0] = items_lp;
     br.total[kGather][0] = items_g;

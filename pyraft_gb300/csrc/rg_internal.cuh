@@ -40,7 +40,8 @@ struct alignas(16) View {
     float P;          // |rk|: ray spacing in line samples
     int flags;        // kLinesAreRows | kRkNegative
     int view;         // sinogram column this entry refers to
-    int pad[4];
+    double delta64;   // Delta in FP64 (FP64 operator pair)
+    int pad[2];
 };
 static_assert(sizeof(View) == 112, "View layout");
 
@@ -98,9 +99,12 @@ struct SSPlan {
     SSGeom g;
     int nv = 0;                    // number of views in this plan
     View *d_views = nullptr;       // device
-    int wmax_bp = 0, wmax_adj = 0; // gather window widths (entries) needed
+    // gather window widths (entries) needed for 32-column tiles of 32 rows
+    // (index 0, 4 rows per thread) and 64 rows (index 1, 8 rows per thread)
+    int wmax_bp[2] = {0, 0}, wmax_adj[2] = {0, 0};
     float dth = 0.f;               // view spacing (backprojection scale)
     bool adj_ok = true;            // every |rk| >= 1 (two-tap adjoint)
+    bool contiguous = true;        // views are consecutive (not an OSEM subset)
     int device = -1;
 };
 
@@ -114,19 +118,42 @@ void ss_plan_free(SSPlan &p);
 // Kernel launchers (slantstack.cu).  Images handed to the kernels are
 // strided views: element (row, col) at ptr[row*cs + col*ls].
 size_t radon_pairs_bytes(int N);
+// nz > 1: a stack of nz images, consecutive ones zi floats apart, their
+// line pairs zp pairs apart.
 int launch_line_pairs(const float *img, long long cs, long long ls, int N,
-                      float2 *pairs_rows, float2 *pairs_cols, cudaStream_t st);
+                      float2 *pairs_rows, float2 *pairs_cols, cudaStream_t st,
+                      int nz = 1, long long zi = 0, long long zp = 0);
 // Radon over the plan's views; out row v.view (angle-major, ld = out_ld)
 // gets the ray sums, or the EM ratio y/Ax when y_am != nullptr.
 int launch_radon(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
-                 float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st);
+                 float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,
+                 int nz = 1, long long zp = 0, long long zo = 0);
+// Views per thread of the Radon for this plan: 2 when its views are
+// consecutive (the two share L1 lines), else 1.  RG_RADON_VIEWS=1|2 overrides.
+int radon_views_per_thread(const SSPlan &p);
 // Gathers.  mode 0: backprojection (scaled by dth); 1: matched adjoint;
 // 2: matched adjoint accumulated in FP64, epilogue writes 1/x (0 where 0).
 // em_x != nullptr (mode 1): x <- x * adj * inv_sens, with x, inv_sens
 // contiguous N x N.
+// A stack of n equal-geometry problems in one launch (grid z): consecutive
+// inputs `in` floats apart, outputs `out` floats apart.
+struct Stack {
+    int n = 1;
+    long long in = 0, out = 0;
+};
+// rows: rows per thread (4 or 8; 0 = the tuned choice for this geometry).
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
                   float *out, long long cs, long long ls,
-                  float *em_x, const float *inv_sens, int *d_err, cudaStream_t st);
+                  float *em_x, const float *inv_sens, int *d_err, cudaStream_t st,
+                  int rows = 0, Stack z = Stack());
+// Rows per thread picked for (geometry, mode) by the autotuner (api.cu).
+int tuned_rows(const SSPlan &p, int mode);
+
+// f64.cu: FP64 operator pair (exact transposes), one thread per (ray, view).
+int launch_radon_f64(const SSPlan &p, const double *img, long long ics, long long ils,
+                     double *out, long long ocs, long long ols, cudaStream_t st);
+int launch_radon_transpose_f64(const SSPlan &p, const double *sino, long long scs, long long sls,
+                               double *img_c, cudaStream_t st);
 
 // aux.cu
 int launch_to_am(const float *in, long long cs, long long ls, int R, int A, float *out_am,

@@ -35,6 +35,7 @@
 //    the backprojection, plus the two hat weights for the adjoint.
 #include <math.h>
 #include <stdio.h>
+#include <stdlib.h>
 
 #include <algorithm>
 #include <vector>
@@ -70,7 +71,7 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         return set_error(RG_EINVAL, "degenerate or non-finite corners");
     const double tol = 1.0 / sqrt(2);
 
-    double wbp = 0.0, wadj = 0.0;
+    double wbp[2] = {0.0, 0.0}, wadj[2] = {0.0, 0.0};
     bool adj_ok = true;
     for (int e = 0; e < nv; ++e) {
         int j = views ? views[e] : e;
@@ -109,19 +110,28 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         if (!ok) return set_error(RG_EUNSUPPORTED, "view %d: positions exceed 2^30 samples "
                                                    "(image and sinogram extents too different)", j);
         v.delta = (float)delta;
+        v.delta64 = delta;
         v.P = (float)fabs(rk);
         v.view = j;
         if (fabs(rk) < 1.0 - 1e-9) adj_ok = false;
-        wbp = std::max(wbp, 31.0 * (fabs(brow) + fabs(bcol)));
-        wadj = std::max(wadj, 31.0 * (fabs(krow) + fabs(kcol)));
+        for (int t = 0; t < 2; ++t) {
+            const double th = t ? 63.0 : 31.0;      // tile height - 1
+            wbp[t] = std::max(wbp[t], th * fabs(brow) + 31.0 * fabs(bcol));
+            wadj[t] = std::max(wadj[t], th * fabs(krow) + 31.0 * fabs(kcol));
+        }
         hv[e] = v;
     }
     p.g = g;
     p.nv = nv;
+    p.contiguous = true;
+    for (int e = 1; e < nv; ++e)
+        if ((views ? views[e] : e) != (views ? views[e - 1] : e - 1) + 1) p.contiguous = false;
     p.dth = (float)dth;
     p.adj_ok = adj_ok;
-    p.wmax_bp = (int)ceil(wbp + 1e-6) + 4;
-    p.wmax_adj = (int)ceil(wadj + 1e-6) + 4;
+    for (int t = 0; t < 2; ++t) {
+        p.wmax_bp[t] = (int)ceil(wbp[t] + 1e-6) + 4;
+        p.wmax_adj[t] = (int)ceil(wadj[t] + 1e-6) + 4;
+    }
     return RG_OK;
 }
 
@@ -150,19 +160,22 @@ void ss_plan_free(SSPlan &p)
 
 size_t radon_pairs_bytes(int N) { return (size_t)N * (N + 2) * sizeof(float2); }
 
+// blockIdx.z selects one image of a stack (strides zi in floats, zp in pairs).
 __global__ __launch_bounds__(256) void k_line_pairs(const float *__restrict__ img, long long cs,
                                                     long long ls, int N,
                                                     float2 *__restrict__ prow,
-                                                    float2 *__restrict__ pcol)
+                                                    float2 *__restrict__ pcol, long long zi,
+                                                    long long zp)
 {
-    line_pairs_tile(img, cs, ls, N, prow, pcol, blockIdx.x, blockIdx.y);
+    line_pairs_tile(img + blockIdx.z * zi, cs, ls, N, prow + blockIdx.z * zp,
+                    pcol + blockIdx.z * zp, blockIdx.x, blockIdx.y);
 }
 
 int launch_line_pairs(const float *img, long long cs, long long ls, int N, float2 *prow,
-                      float2 *pcol, cudaStream_t st)
+                      float2 *pcol, cudaStream_t st, int nz, long long zi, long long zp)
 {
-    dim3 grid((N + 31) / 32, (N + 31) / 32);
-    k_line_pairs<<<grid, 256, 0, st>>>(img, cs, ls, N, prow, pcol);
+    dim3 grid((N + 31) / 32, (N + 31) / 32, nz);
+    k_line_pairs<<<grid, 256, 0, st>>>(img, cs, ls, N, prow, pcol, zi, zp);
     RG_CK_LAUNCH("k_line_pairs");
     return RG_OK;
 }
@@ -172,92 +185,134 @@ __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                const float2 *__restrict__ pcol, int N,
                                                const View *__restrict__ views, int nv, int R,
                                                float *__restrict__ out_am, int out_ld,
-                                               const float *__restrict__ y_am, int y_ld)
+                                               const float *__restrict__ y_am, int y_ld,
+                                               long long zp, long long zo)
 {
-    radon_tile<RATIO>(prow, pcol, N, views, nv, R, out_am, out_ld, y_am, y_ld, blockIdx.x,
-                      blockIdx.y);
+    radon_tile<RATIO>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
+                      out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x, blockIdx.y);
+}
+
+template <bool RATIO>
+__global__ __launch_bounds__(128) void k_radon2(const float2 *__restrict__ prow,
+                                                const float2 *__restrict__ pcol, int N,
+                                                const View *__restrict__ views, int nv, int R,
+                                                float *__restrict__ out_am, int out_ld,
+                                                const float *__restrict__ y_am, int y_ld,
+                                                long long zp, long long zo)
+{
+    radon_tile2<RATIO>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
+                       out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x, blockIdx.y);
+}
+
+int radon_views_per_thread(const SSPlan &p)
+{
+    const char *e = getenv("RG_RADON_VIEWS");
+    if (e && (atoi(e) == 1 || atoi(e) == 2)) return atoi(e);
+    return p.contiguous ? 2 : 1;
 }
 
 int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float *out_am,
-                 int out_ld, const float *y_am, int y_ld, cudaStream_t st)
+                 int out_ld, const float *y_am, int y_ld, cudaStream_t st, int nz, long long zp,
+                 long long zo)
 {
     if (p.nv == 0) return RG_OK;
-    dim3 grid((p.g.R + 31) / 32, (p.nv + 3) / 4);
+    if (radon_views_per_thread(p) == 2) {
+        dim3 grid((p.g.R + 31) / 32, (p.nv + 7) / 8, nz);
+        if (y_am)
+            k_radon2<true><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R,
+                                                 out_am, out_ld, y_am, y_ld, zp, zo);
+        else
+            k_radon2<false><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R,
+                                                  out_am, out_ld, nullptr, 0, zp, zo);
+        RG_CK_LAUNCH("k_radon2");
+        return RG_OK;
+    }
+    dim3 grid((p.g.R + 31) / 32, (p.nv + 3) / 4, nz);
     if (y_am)
         k_radon<true><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R, out_am,
-                                            out_ld, y_am, y_ld);
+                                            out_ld, y_am, y_ld, zp, zo);
     else
         k_radon<false><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R, out_am,
-                                             out_ld, nullptr, 0);
+                                             out_ld, nullptr, 0, zp, zo);
     RG_CK_LAUNCH("k_radon");
     return RG_OK;
 }
 
-template <int MODE, int WMAX, bool EM>
+template <int MODE, int WMAX, int ROWS, bool EM>
 __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, int s_ld, int R,
                                                 const View *__restrict__ views, int nv, int N,
                                                 float scale, float *__restrict__ out,
                                                 long long cs, long long ls,
                                                 float *__restrict__ em_x,
                                                 const float *__restrict__ inv_sens,
-                                                int *__restrict__ err)
+                                                int *__restrict__ err, long long zs,
+                                                long long zo)
 {
     extern __shared__ float2 pairs[];          // [kSlots][WMAX]
-    gather_tile<MODE, WMAX, EM>(s_am, s_ld, R, views, nv, N, scale, out, cs, ls, em_x, inv_sens,
-                                err, blockIdx.x, blockIdx.y, pairs);
+    gather_tile<MODE, WMAX, ROWS, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, scale,
+                                      out + blockIdx.z * zo, cs, ls, em_x, inv_sens, err,
+                                      blockIdx.x, blockIdx.y, pairs);
 }
 
-template <int MODE, int WMAX, bool EM>
+template <int MODE, int WMAX, int ROWS, bool EM>
 static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                     long long ls, float *em_x, const float *inv_sens, int *d_err,
-                    cudaStream_t st)
+                    cudaStream_t st, const Stack &z)
 {
     const size_t smem = (size_t)kSlots * WMAX * sizeof(float2);
-    const int tiles = (p.g.N + kTile - 1) / kTile;
-    dim3 grid(tiles, tiles);
+    dim3 grid((p.g.N + kTile - 1) / kTile, (p.g.N + kWarps * ROWS - 1) / (kWarps * ROWS), z.n);
     const float scale = (MODE == 0) ? p.dth : 1.f;
-    auto k = k_gather<MODE, WMAX, EM>;
+    auto k = k_gather<MODE, WMAX, ROWS, EM>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, p.g.N, scale, out, cs, ls,
-                               em_x, inv_sens, d_err);
+                               em_x, inv_sens, d_err, z.in, z.out);
     RG_CK_LAUNCH("k_gather");
     return RG_OK;
 }
 
-template <int MODE, bool EM>
+template <int MODE, int ROWS, bool EM>
 static int gather_mode(const SSPlan &p, int wneed, const float *s_am, int s_ld, float *out,
                        long long cs, long long ls, float *em_x, const float *inv_sens,
-                       int *d_err, cudaStream_t st)
+                       int *d_err, cudaStream_t st, const Stack &z)
 {
-    if (wneed <= 64) return gather_w<MODE, 64, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st);
-    if (wneed <= 128) return gather_w<MODE, 128, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st);
-    if (wneed <= 256) return gather_w<MODE, 256, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st);
-    if (wneed <= 512) return gather_w<MODE, 512, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st);
+    if (wneed <= 64) return gather_w<MODE, 64, ROWS, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
+    if (wneed <= 128) return gather_w<MODE, 128, ROWS, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
+    if (wneed <= 256) return gather_w<MODE, 256, ROWS, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
+    if (wneed <= 512) return gather_w<MODE, 512, ROWS, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
     return set_error(RG_EUNSUPPORTED,
-                     "gather window of %d samples per 32-pixel tile exceeds 512 "
+                     "gather window of %d samples per tile exceeds 512 "
                      "(image much coarser than the ray spacing)", wneed);
+}
+
+template <int MODE, bool EM>
+static int gather_rows(const SSPlan &p, int rows, const float *s_am, int s_ld, float *out,
+                       long long cs, long long ls, float *em_x, const float *inv_sens, int *d_err,
+                       cudaStream_t st, const Stack &z)
+{
+    const int t = rows == 8 ? 1 : 0;
+    const int w = (MODE == 0) ? p.wmax_bp[t] : p.wmax_adj[t];
+    if (rows == 8)
+        return gather_mode<MODE, 8, EM>(p, w, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
+    return gather_mode<MODE, 4, EM>(p, w, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
 }
 
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                   long long cs, long long ls, float *em_x, const float *inv_sens, int *d_err,
-                  cudaStream_t st)
+                  cudaStream_t st, int rows, Stack z)
 {
+    if (rows == 0) rows = tuned_rows(p, mode);
     if (mode == 0)
-        return gather_mode<0, false>(p, p.wmax_bp, s_am, s_ld, out, cs, ls, nullptr, nullptr,
-                                     d_err, st);
+        return gather_rows<0, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
     if (!p.adj_ok)
         return set_error(RG_EUNSUPPORTED,
                          "matched adjoint needs ray spacing >= pixel spacing along each line "
                          "(nrays <= size for the default extents)");
     if (mode == 1) {
         if (em_x)
-            return gather_mode<1, true>(p, p.wmax_adj, s_am, s_ld, out, cs, ls, em_x, inv_sens,
-                                        d_err, st);
-        return gather_mode<1, false>(p, p.wmax_adj, s_am, s_ld, out, cs, ls, nullptr, nullptr,
-                                     d_err, st);
+            return gather_rows<1, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
+        return gather_rows<1, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
     }
-    return gather_mode<2, false>(p, p.wmax_adj, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err,
-                                 st);
+    return gather_rows<2, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
 }
 
 }  // namespace rg

@@ -63,6 +63,33 @@ __device__ __forceinline__ void kahan_add(float &sum, float &c, float x)
     sum = t;
 }
 
+// Lines i (in [0, N-1]) whose sample u0 + i*q lies in [-0.5, N - 0.5]: a
+// superset of the valid samples [0, N-1) with half a sample of margin,
+// checked exactly at both ends so every index used stays in [-1, N-1].
+__device__ __forceinline__ void radon_line_range(long long u0, long long q, int N, int &lo,
+                                                 int &hi)
+{
+    // float error of the estimate is < 1e-3 samples; the ends are then exact
+    const float uf0 = (float)u0 * 2.3283064365386963e-10f;
+    const float qf = (float)q * 2.3283064365386963e-10f;
+    if (fabsf(qf) < 1e-20f) {
+        bool in = uf0 >= -0.5f && uf0 <= (float)N - 0.5f;
+        lo = in ? 0 : 1;
+        hi = in ? N - 1 : 0;
+    } else {
+        float t1 = (-0.5f - uf0) / qf, t2 = ((float)N - 0.5f - uf0) / qf;
+        float tlo = fmaxf(fminf(t1, t2), 0.f), thi = fminf(fmaxf(t1, t2), (float)(N - 1));
+        lo = (int)ceilf(tlo);
+        hi = (int)floorf(thi);
+    }
+    // Exact check of the ends (positions are monotone in i): every sample
+    // index used stays in [-1, N-1], i.e. inside the padded line.
+    const long long ulo = -(1LL << 32), uhi = (long long)N << 32;
+    while (lo <= hi && (u0 + (long long)lo * q < ulo || u0 + (long long)lo * q >= uhi)) ++lo;
+    while (hi >= lo && (u0 + (long long)hi * q < ulo || u0 + (long long)hi * q >= uhi)) --hi;
+
+}
+
 // One CTA (128 threads) = rays [32 bx, 32 bx + 32) of views [4 by, 4 by + 4).
 template <bool RATIO>
 __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
@@ -82,28 +109,8 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
     // Position on line 0 and per-line step, Q32.32.
     const long long u0 = v.r0 + (long long)k * v.rk;
     const long long q = v.ri;
-    // Lines whose sample lies in [-0.5, N - 0.5]: a superset of the valid
-    // samples [0, N-1) with half a sample of margin, and every index stays in
-    // [-1, N-1] (the pads).  Float error here is < 1e-3 samples.
-    const float uf0 = (float)u0 * 2.3283064365386963e-10f;
-    const float qf = (float)q * 2.3283064365386963e-10f;
     int lo, hi;
-    if (fabsf(qf) < 1e-20f) {
-        bool in = uf0 >= -0.5f && uf0 <= (float)N - 0.5f;
-        lo = in ? 0 : 1;
-        hi = in ? N - 1 : 0;
-    } else {
-        float t1 = (-0.5f - uf0) / qf, t2 = ((float)N - 0.5f - uf0) / qf;
-        float tlo = fmaxf(fminf(t1, t2), 0.f), thi = fminf(fmaxf(t1, t2), (float)(N - 1));
-        lo = (int)ceilf(tlo);
-        hi = (int)floorf(thi);
-    }
-    // Exact check of the ends (positions are monotone in i): every sample
-    // index used stays in [-1, N-1], i.e. inside the padded line.
-    const long long ulo = -(1LL << 32), uhi = (long long)N << 32;
-    while (lo <= hi && (u0 + (long long)lo * q < ulo || u0 + (long long)lo * q >= uhi)) ++lo;
-    while (hi >= lo && (u0 + (long long)hi * q < ulo || u0 + (long long)hi * q >= uhi)) --hi;
-
+    radon_line_range(u0, q, N, lo, hi);
     float acc = 0.f, comp = 0.f;
     if (lo <= hi) {
         long long u = u0 + (long long)lo * q;
@@ -132,12 +139,80 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
     out_am[(size_t)v.view * out_ld + k] = val;
 }
 
+// Two views per thread: a CTA (128 threads) covers rays [32 bx, 32 bx + 32) of
+// views [8 by, 8 by + 8); warp w carries views 8 by + 2w and 8 by + 2w + 1.
+// The two views of a thread are adjacent, so their samples on each line lie
+// a few positions apart: the two independent load streams share L1 lines
+// and double the loads in flight per thread.  The loop runs over the union
+// of both views' line ranges; a sample index outside a view's own range is
+// clamped (one unsigned min) onto the line's zero pad at N+1, so it adds 0
+// and never leaves the padded line.
+template <bool RATIO>
+__device__ __forceinline__ void radon_tile2(const float2 *__restrict__ prow,
+                                            const float2 *__restrict__ pcol, int N,
+                                            const View *__restrict__ views, int nv, int R,
+                                            float *__restrict__ out_am, int out_ld,
+                                            const float *__restrict__ y_am, int y_ld, int bx,
+                                            int by)
+{
+    const int k = bx * 32 + (threadIdx.x & 31);
+    const int e0 = by * 8 + 2 * (threadIdx.x >> 5);
+    if (e0 >= nv || k >= R) return;   // no barrier below: early exit is safe
+    const bool two = e0 + 1 < nv;
+    const View va = views[e0];
+    const View vb = two ? views[e0 + 1] : va;
+    const unsigned pitch = (unsigned)(N + 2);
+    const float2 *__restrict__ ba = (va.flags & kLinesAreRows) ? prow : pcol;
+    const float2 *__restrict__ bb = (vb.flags & kLinesAreRows) ? prow : pcol;
+    const long long ua0 = va.r0 + (long long)k * va.rk, ub0 = vb.r0 + (long long)k * vb.rk;
+    int loa, hia, lob, hib;
+    radon_line_range(ua0, va.ri, N, loa, hia);
+    radon_line_range(ub0, vb.ri, N, lob, hib);
+    const int lo = min(loa, lob), hi = max(hia, hib);
+    float acca = 0.f, compa = 0.f, accb = 0.f, compb = 0.f;
+    if (lo <= hi) {
+        long long ua = ua0 + (long long)lo * va.ri, ub = ub0 + (long long)lo * vb.ri;
+        unsigned off = (unsigned)lo * pitch;
+        const unsigned pad = (unsigned)(N + 1);
+        int i = lo;
+        while (i <= hi) {
+            const int iend = min(hi, i + 31);
+            float pa = 0.f, pb = 0.f;
+#pragma unroll 4
+            for (; i <= iend; ++i) {
+                const unsigned ia = min((unsigned)((int)(ua >> 32) + 1), pad);
+                const unsigned ib = min((unsigned)((int)(ub >> 32) + 1), pad);
+                const float2 qa = __ldg(ba + off + ia);
+                const float2 qb = __ldg(bb + off + ib);
+                pa += fmaf(__uint_as_float(((unsigned)ua >> 9) | 0x3F800000u), qa.y, qa.x);
+                pb += fmaf(__uint_as_float(((unsigned)ub >> 9) | 0x3F800000u), qb.y, qb.x);
+                ua += va.ri;
+                ub += vb.ri;
+                off += pitch;
+            }
+            kahan_add(acca, compa, pa);
+            kahan_add(accb, compb, pb);
+        }
+    }
+    float vala = (acca - compa) * va.delta, valb = (accb - compb) * vb.delta;
+    if (RATIO) {
+        const float ya = y_am[(size_t)va.view * y_ld + k];
+        vala = (vala != 0.f) ? ya / vala : 0.f;
+        if (two) {
+            const float yb = y_am[(size_t)vb.view * y_ld + k];
+            valb = (valb != 0.f) ? yb / valb : 0.f;
+        }
+    }
+    out_am[(size_t)va.view * out_ld + k] = vala;
+    if (two) out_am[(size_t)vb.view * out_ld + k] = valb;
+}
+
 // ============================================================================
 // Gathers (backprojection / matched adjoint).
 
-constexpr int kTile = 32;    // pixels per tile side
+constexpr int kTile = 32;    // pixel columns per tile (one warp lane each)
 constexpr int kSlots = 32;   // views per staged chunk
-constexpr int kRows = 4;     // rows per thread (8 warps x 4 = 32)
+constexpr int kWarps = 8;    // 256 threads; warp w owns rows [w*ROWS, (w+1)*ROWS) of the tile
 
 struct SlotInfo {
     unsigned base;   // Q9.23 position of the tile origin within the window
@@ -146,16 +221,34 @@ struct SlotInfo {
     int nlo;         // first staged sample index (INT_MIN: empty slot)
 };
 
-// Inner loop over the staged views of one chunk for one thread's 4 pixels.
+// Position weight 1 + w from the low 23 bits of a Q9.23 position.
+__device__ __forceinline__ float frac_plus_one(unsigned v)
+{
+    return __uint_as_float((v & 0x7FFFFFu) | 0x3F800000u);
+}
+
+// a * b + c, clamped to [0, 1] by the FMA itself (fma.rn.sat).
+__device__ __forceinline__ float fma_sat(float a, float b, float c)
+{
+    float d;
+    asm("fma.rn.sat.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// Inner loop over the staged views of one chunk for one thread's ROWS pixels.
+//
+// Backprojection: the staged pair (s - d, d) at the floor index gives the
+// linear interpolation (s - d) + (1 + w) d.
 //
 // Adjoint weights: with kappa the ray-index position of the pixel's ray,
 // k0 = floor(kappa), f = kappa - k0, the rays k0 and k0+1 sample the pixel's
 // line at u - m = -p f and p (1 - f); their hat weights are 1 - P f and
-// 1 - P (1 - f), clipped at 0 (P = |p| >= 1, so no other ray reaches the
-// pixel).  At line positions m = 0 and m = N-1 the Radon drops samples with
-// u < 0 and u >= N-1; BORDER applies exactly that rule.
-template <int MODE, int WMAX, bool BORDER, typename Acc>
-__device__ __forceinline__ void accumulate(Acc (&part)[kRows], const float2 *__restrict__ pairs,
+// 1 - P (1 - f) clipped to [0, 1] (P = |p| >= 1, so no other ray reaches
+// the pixel); with w1 = 1 + f they are sat(-P w1 + 1 + P) and
+// sat(P w1 + 1 - 2P).  At line positions m = 0 and m = N-1 the Radon drops
+// samples with u < 0 and u >= N-1; BORDER applies exactly that rule.
+template <int MODE, int WMAX, int ROWS, bool BORDER>
+__device__ __forceinline__ void accumulate(float (&part)[ROWS], const float2 *__restrict__ pairs,
                                            const SlotInfo *slot, const float *slotP,
                                            const int *slotFlags, int nslot, int lane, int warp,
                                            int col, int myrow, int N)
@@ -164,13 +257,12 @@ __device__ __forceinline__ void accumulate(Acc (&part)[kRows], const float2 *__r
         const SlotInfo si = slot[s];
         if (si.nlo == INT_MIN) continue;
         const float2 *__restrict__ pw = pairs + s * WMAX;
-        unsigned vpos = si.base + (unsigned)(lane * si.a) + (unsigned)(warp * kRows * si.b);
+        unsigned vpos = si.base + (unsigned)(lane * si.a) + (unsigned)(warp * ROWS * si.b);
         if (MODE == 0) {
 #pragma unroll
-            for (int r = 0; r < kRows; ++r) {
-                const float w1 = __uint_as_float((vpos & 0x7FFFFFu) | 0x3F800000u);
+            for (int r = 0; r < ROWS; ++r) {
                 const float2 pr = pw[vpos >> 23];
-                part[r] += fmaf(w1, pr.y, pr.x);
+                part[r] += fmaf(frac_plus_one(vpos), pr.y, pr.x);
                 vpos += (unsigned)si.b;
             }
         } else {
@@ -180,11 +272,11 @@ __device__ __forceinline__ void accumulate(Acc (&part)[kRows], const float2 *__r
             if (BORDER) fl = slotFlags[s];
             const bool pneg = (fl & kRkNegative) != 0;
 #pragma unroll
-            for (int r = 0; r < kRows; ++r) {
-                const float w1 = __uint_as_float((vpos & 0x7FFFFFu) | 0x3F800000u);
+            for (int r = 0; r < ROWS; ++r) {
+                const float w1 = frac_plus_one(vpos);
                 const float2 pr = pw[vpos >> 23];
-                float wa = fmaxf(0.f, fmaf(-P, w1, c0));
-                float wb = fmaxf(0.f, fmaf(P, w1, c1));
+                float wa = fma_sat(-P, w1, c0);
+                float wb = fma_sat(P, w1, c1);
                 if (BORDER) {
                     const int m = (fl & kLinesAreRows) ? col : (myrow + r);
                     const bool f0 = (w1 == 1.0f);
@@ -196,7 +288,8 @@ __device__ __forceinline__ void accumulate(Acc (&part)[kRows], const float2 *__r
                         if (!pneg) wb = 0.f;
                     }
                 }
-                part[r] += (Acc)fmaf(pr.x, wa, pr.y * wb);
+                part[r] = fmaf(pr.x, wa, part[r]);
+                part[r] = fmaf(pr.y, wb, part[r]);
                 vpos += (unsigned)si.b;
             }
         }
@@ -204,9 +297,9 @@ __device__ __forceinline__ void accumulate(Acc (&part)[kRows], const float2 *__r
 }
 
 // MODE 0: backprojection; 1: adjoint (FP32 accumulate); 2: adjoint, FP64.
-// One CTA (256 threads) = the 32 x 32 pixel tile (tx, ty); `pairs` is
-// kSlots * WMAX float2 of shared memory.
-template <int MODE, int WMAX, bool EM>
+// One CTA (256 threads) = the tile of 32 columns x 8*ROWS rows at tile
+// coordinates (tx, ty); `pairs` is kSlots * WMAX float2 of shared memory.
+template <int MODE, int WMAX, int ROWS, bool EM>
 __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int s_ld, int R,
                                             const View *__restrict__ views, int nv, int N,
                                             float scale, float *__restrict__ out, long long cs,
@@ -215,34 +308,38 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
                                             int *__restrict__ err, int tx, int ty,
                                             float2 *__restrict__ pairs)
 {
+    constexpr int TH = kWarps * ROWS;          // tile height
     __shared__ SlotInfo slot[kSlots];
+    __shared__ int slotW[kSlots];
+    __shared__ int slotView[kSlots];
+    __shared__ float slotDelta[kSlots];
     __shared__ float slotP[kSlots];
     __shared__ int slotFlags[kSlots];
     using Acc = typename std::conditional<MODE == 2, double, float>::type;
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int row0 = ty * kTile, col0 = tx * kTile;
+    const int row0 = ty * TH, col0 = tx * kTile;
     const int col = col0 + lane;
-    const int myrow = row0 + warp * kRows;
-    const bool border = row0 == 0 || col0 == 0 || row0 + kTile >= N || col0 + kTile >= N;
+    const int myrow = row0 + warp * ROWS;
+    const bool border = row0 == 0 || col0 == 0 || row0 + TH >= N || col0 + kTile >= N;
 
-    Acc acc[kRows], comp[kRows];
+    Acc acc[ROWS], comp[ROWS];
 #pragma unroll
-    for (int r = 0; r < kRows; ++r) { acc[r] = 0; comp[r] = 0; }
+    for (int r = 0; r < ROWS; ++r) { acc[r] = 0; comp[r] = 0; }
 
     for (int chunk = 0; chunk < nv; chunk += kSlots) {
         const int nslot = min(kSlots, nv - chunk);
         if (warp == 0) {
             SlotInfo si = {0u, 0, 0, INT_MIN};
-            float P = 0.f;
-            int flags = 0;
+            int W = 0, view = 0, flags = 0;
+            float P = 0.f, delta = 0.f;
             if (lane < nslot) {
-                const View v = views[chunk + lane];
+                const View &v = views[chunk + lane];
                 long long cr, cc, c0;
                 if (MODE == 0) { cr = v.brow; cc = v.bcol; c0 = v.b0; }
                 else           { cr = v.krow; cc = v.kcol; c0 = v.k0; }
                 const long long origin = c0 + (long long)row0 * cr + (long long)col0 * cc;
-                const long long dr = 31LL * cr, dc = 31LL * cc;
+                const long long dr = (long long)(TH - 1) * cr, dc = (long long)(kTile - 1) * cc;
                 const long long mn = origin + min(0LL, dr) + min(0LL, dc);
                 const long long mx = origin + max(0LL, dr) + max(0LL, dc);
                 const int nlo = (int)(mn >> 32) - 1;
@@ -252,58 +349,61 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
                     si.base = (unsigned)((origin - ((long long)nlo << 32)) >> 9);
                     si.a = (int)((cc + 256) >> 9);
                     si.b = (int)((cr + 256) >> 9);
+                    W = nhi - nlo + 1;
                 } else if (err) {
                     atomicOr(err, 1);
                 }
+                view = v.view;
+                delta = v.delta;
                 P = v.P;
                 flags = v.flags;
             }
             slot[lane] = si;
+            slotW[lane] = W;
+            slotView[lane] = view;
+            slotDelta[lane] = delta;
             slotP[lane] = P;
             slotFlags[lane] = flags;
         }
         __syncthreads();
 
-        // Stage the windows.
-        for (int e = threadIdx.x; e < nslot * WMAX; e += 256) {
-            const int s = e / WMAX, w = e - s * WMAX;
-            const int nlo = slot[s].nlo;
-            float2 pr = make_float2(0.f, 0.f);
-            if (nlo != INT_MIN) {
-                const View &v = views[chunk + s];
-                const float *__restrict__ row = s_am + (size_t)v.view * s_ld;
-                const int n = nlo + w;
+        // Stage each view's window (warp w stages slots w, w + 8, ...).
+        for (int s = warp; s < nslot; s += kWarps) {
+            const int nlo = slot[s].nlo, W = slotW[s];
+            const float *__restrict__ row = s_am + (size_t)slotView[s] * s_ld;
+            const float d = slotDelta[s];
+            for (int e = lane; e < W; e += 32) {
+                const int n = nlo + e;
+                float2 pr = make_float2(0.f, 0.f);
                 if (MODE == 0) {
-                    if (n >= 0 && n <= R - 2) {
-                        const float s0 = __ldg(row + n), s1 = __ldg(row + n + 1);
-                        pr = make_pair(s0, s1, true);
-                    }
+                    if (n >= 0 && n <= R - 2) pr = make_pair(__ldg(row + n), __ldg(row + n + 1), true);
                 } else {
-                    const float d = v.delta;
                     const float s0 = (n >= 0 && n < R) ? __ldg(row + n) : 0.f;
                     const float s1 = (n + 1 >= 0 && n + 1 < R) ? __ldg(row + n + 1) : 0.f;
                     pr = make_float2(s0 * d, s1 * d);
                 }
+                pairs[s * WMAX + e] = pr;
             }
-            pairs[e] = pr;
         }
         __syncthreads();
 
         // Accumulate.  Border tiles of the adjoint apply the reference's
         // sample validity at positions 0 and N-1 of a line (CTA-uniform branch).
-        Acc part[kRows];
+        // FP32 partial sums over the chunk (<= 32 views); across chunks they
+        // are added with Kahan compensation (FP32) or in FP64 (MODE 2).
+        float part[ROWS];
 #pragma unroll
-        for (int r = 0; r < kRows; ++r) part[r] = 0;
+        for (int r = 0; r < ROWS; ++r) part[r] = 0.f;
         if (MODE != 0 && border)
-            accumulate<MODE, WMAX, true, Acc>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                              warp, col, myrow, N);
-        else
-            accumulate<MODE, WMAX, false, Acc>(part, pairs, slot, slotP, slotFlags, nslot, lane,
+            accumulate<MODE, WMAX, ROWS, true>(part, pairs, slot, slotP, slotFlags, nslot, lane,
                                                warp, col, myrow, N);
+        else
+            accumulate<MODE, WMAX, ROWS, false>(part, pairs, slot, slotP, slotFlags, nslot, lane,
+                                                warp, col, myrow, N);
 #pragma unroll
-        for (int r = 0; r < kRows; ++r) {
+        for (int r = 0; r < ROWS; ++r) {
             if (MODE == 2) {
-                acc[r] += part[r];
+                acc[r] += (double)part[r];
             } else {
                 float a = acc[r], c = comp[r];
                 kahan_add(a, c, (float)part[r]);
@@ -314,7 +414,7 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
     }
 
 #pragma unroll
-    for (int r = 0; r < kRows; ++r) {
+    for (int r = 0; r < ROWS; ++r) {
         const int row = myrow + r;
         if (row >= N || col >= N) break;
         if (MODE == 2) {
