@@ -160,6 +160,7 @@ static int get_plan(const SSGeom &g, int stride, int first, std::shared_ptr<Plan
 
 struct DevTable {
     void *p = nullptr;
+    float h0 = 0.f;   // Ram-Lak centre tap (filter tables only)
     ~DevTable() { if (p) cudaFree(p); }
 };
 static Cache<DevTable> g_tables;
@@ -239,12 +240,12 @@ static bool is_view_major(const rg_image &s)
 
 // ----------------------------------------------------------------------------
 // Autotuner for the gather tile height (rows per thread: 4 -> 32x32 tiles,
-// 8 -> 32x64 tiles).  The first out-of-place backprojection or adjoint of a
+// 8 -> 32x64 tiles, 16 -> 32x128 tiles).  The first out-of-place backprojection or adjoint of a
 // geometry times both variants on the caller's own buffers (two timed runs
 // each, CUDA events on the caller's stream; this first call synchronises)
 // and keeps the faster one for the process.  Calls made while the stream
 // is being captured never tune; they use the cached choice or 4.  The
-// environment variable RG_GATHER_ROWS=4|8 forces a choice.
+// environment variable RG_GATHER_ROWS=4|8|16 forces a choice.
 
 static std::mutex g_tune_mu;
 static std::map<std::string, int> g_tune;
@@ -262,7 +263,7 @@ static int env_rows()
     const char *e = getenv("RG_GATHER_ROWS");
     if (!e) return 0;
     const int v = atoi(e);
-    return (v == 4 || v == 8) ? v : 0;
+    return (v == 4 || v == 8 || v == 16) ? v : 0;
 }
 
 int tuned_rows(const SSPlan &p, int mode)
@@ -290,7 +291,7 @@ static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_l
     RG_CK(cudaEventCreate(&b));
     float best = 1e30f;
     int pick = 4, rc = RG_OK;
-    for (int rows : {4, 8}) {
+    for (int rows : {4, 8, 16}) {
         float tsum = 0.f;
         for (int rep = 0; rep < 3 && !rc; ++rep) {
             cudaEventRecord(a, st);
@@ -561,14 +562,16 @@ static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable>
     kb.add(kind).add(R).add(tmin).add(tmax);
     std::vector<float> taps(2 * (size_t)R - 1);
     if (kind == RG_FILTER_RAMLAK) {
+        // Odd taps godd[q] = dt h[2q - 2R + 1], q in [0, 2R), then dt h[0]
+        // (the layout k_ramlak_rows reads).
         const double pi = 3.14159265358979323846;
-        for (int m = -(R - 1); m <= R - 1; ++m) {
-            double h;
-            if (m == 0) h = 1.0 / (4.0 * dt * dt);
-            else if (m % 2 == 0) h = 0.0;
-            else h = -1.0 / (pi * pi * (double)m * (double)m * dt * dt);
-            taps[m + R - 1] = (float)(h * dt);
+        taps.assign(2 * (size_t)R + 1, 0.f);
+        for (int q = 0; q < 2 * R; ++q) {
+            const int m = 2 * q - 2 * R + 1;
+            if (m >= -(R - 1) && m <= R - 1)
+                taps[q] = (float)(-dt / (pi * pi * (double)m * (double)m * dt * dt));
         }
+        taps[2 * (size_t)R] = (float)(dt / (4.0 * dt * dt));
     } else if (kind == RG_FILTER_LOWPASS) {
         // g = Re(ifft(fftshift(|w| cos(pi w dt)))), w = linspace(-wc, wc, R), wc = 1/(2 dt):
         // applying g by circular convolution equals the FFT filter of
@@ -593,7 +596,17 @@ static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable>
     } else {
         return set_error(RG_EINVAL, "unknown filter kind %d", kind);
     }
-    return get_table(std::string("taps") + kb.s, taps.data(), taps.size() * sizeof(float), out);
+    int rc = get_table(std::string("taps") + kb.s, taps.data(), taps.size() * sizeof(float), out);
+    if (!rc && kind == RG_FILTER_RAMLAK) out->h0 = taps.back();
+    return rc;
+}
+
+static int filter_rows(int kind, const float *in_am, float *out_am, int R, int A,
+                       const std::shared_ptr<DevTable> &taps, cudaStream_t st)
+{
+    if (kind == RG_FILTER_RAMLAK)     // odd taps + centre tap (parity-split kernel)
+        return launch_ramlak_rows(in_am, out_am, R, A, (const float *)taps->p, taps->h0, st);
+    return launch_conv_rows(in_am, out_am, R, A, (const float *)taps->p, st);
 }
 
 size_t rg_filter_workspace(rg_image sino, int kind)
@@ -621,7 +634,7 @@ int rg_filter(rg_image in, rg_image out, int kind, void *ws, size_t wsb, void *s
     float *a = (float *)s.take((size_t)R * A * sizeof(float));
     float *b = (float *)s.take((size_t)R * A * sizeof(float));
     if (!(rc = launch_to_am(in.data, in.column_stride, in.line_stride, R, A, a, st)) &&
-        !(rc = launch_conv_rows(a, b, R, A, (const float *)taps->p, st)))
+        !(rc = filter_rows(kind, a, b, R, A, taps, st)))
         rc = launch_from_am(b, R, A, out.data, out.column_stride, out.line_stride, st);
     scratch_end(s);
     return rc;
@@ -653,7 +666,7 @@ int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *
         rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, a, st);
         src = a;
     }
-    if (!rc && !(rc = launch_conv_rows(src, b, R, A, (const float *)taps->p, st)) &&
+    if (!rc && !(rc = filter_rows(kind, src, b, R, A, taps, st)) &&
         !(rc = autotune_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride, st)))
         rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
                            nullptr, nullptr, nullptr, st);

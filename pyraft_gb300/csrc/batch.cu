@@ -106,7 +106,8 @@ constexpr int kBatchRows = 4;
 
 template <int MODE, int WMAX>
 __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restrict__ d, int n,
-                                                      int total, int *counter)
+                                                      int total, int *counter,
+                                                      unsigned pair_bytes)
 {
     extern __shared__ float2 pairs[];
     for (;;) {
@@ -117,11 +118,13 @@ __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restri
         if (MODE == 1)
             gather_tile<1, WMAX, kBatchRows, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
                                                    nullptr, 0, 0, b.x, b.inv_sens, nullptr,
-                                                   local % tiles, local / tiles, pairs);
+                                                   local % tiles, local / tiles, pairs,
+                                                   pair_bytes);
         else
             gather_tile<2, WMAX, kBatchRows, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
                                                     b.inv_sens, b.N, 1, nullptr, nullptr, nullptr,
-                                                    local % tiles, local / tiles, pairs);
+                                                    local % tiles, local / tiles, pairs,
+                                                    pair_bytes);
     }
 }
 
@@ -181,7 +184,8 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
         RG_CK_LAUNCH("k_batch_radon");
         RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
         k_batch_gather<1, WMAX><<<br.grid[2][0], 256, smem, st>>>(d, br.n, br.total[kGather][0],
-                                                                  br.counter);
+                                                                  br.counter,
+                                                                  (unsigned)sizeof(float2));
         RG_CK_LAUNCH("k_batch_gather<1>");
     }
     return RG_OK;
@@ -195,7 +199,8 @@ int enqueue_sensitivity(const BatchRun &br, cudaStream_t st)
         const BatchSlice *d = br.d_desc + (size_t)s * br.n;
         RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
         k_batch_gather<2, WMAX><<<br.grid[3][0], 256, smem, st>>>(d, br.n, br.total[kGather][0],
-                                                                  br.counter);
+                                                                  br.counter,
+                                                                  (unsigned)sizeof(float2));
         RG_CK_LAUNCH("k_batch_gather<2>");
     }
     return RG_OK;
@@ -402,7 +407,7 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
             const SSPlan *p = plans[(size_t)q * S + s];
             if (!p->adj_ok)
                 return set_error(RG_EUNSUPPORTED, "slice %d: nrays must not exceed the image size", k);
-            wneed = std::max(wneed, p->wmax_adj[kBatchRows == 8 ? 1 : 0]);
+            wneed = std::max(wneed, p->wmax_adj[kBatchRows == 16 ? 2 : kBatchRows == 8 ? 1 : 0]);
         }
     }
     BatchRun br;

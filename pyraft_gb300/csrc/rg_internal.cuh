@@ -99,9 +99,9 @@ struct SSPlan {
     SSGeom g;
     int nv = 0;                    // number of views in this plan
     View *d_views = nullptr;       // device
-    // gather window widths (entries) needed for 32-column tiles of 32 rows
-    // (index 0, 4 rows per thread) and 64 rows (index 1, 8 rows per thread)
-    int wmax_bp[2] = {0, 0}, wmax_adj[2] = {0, 0};
+    // gather window widths (entries) needed for 32-column tiles of 32, 64 and
+    // 128 rows (index 0, 1, 2: 4, 8, 16 rows per thread)
+    int wmax_bp[3] = {0, 0, 0}, wmax_adj[3] = {0, 0, 0};
     float dth = 0.f;               // view spacing (backprojection scale)
     bool adj_ok = true;            // every |rk| >= 1 (two-tap adjoint)
     bool contiguous = true;        // views are consecutive (not an OSEM subset)
@@ -141,7 +141,7 @@ struct Stack {
     int n = 1;
     long long in = 0, out = 0;
 };
-// rows: rows per thread (4 or 8; 0 = the tuned choice for this geometry).
+// rows: rows per thread (4, 8 or 16; 0 = the tuned choice for this geometry).
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
                   float *out, long long cs, long long ls,
                   float *em_x, const float *inv_sens, int *d_err, cudaStream_t st,
@@ -173,6 +173,10 @@ int launch_radon_fromdesc(float *sino, long long cs, long long ls, int lines, in
 // filter.cu: out_am[a][n] = sum_k taps[n - k + R - 1] * in_am[a][k].
 int launch_conv_rows(const float *in_am, float *out_am, int R, int A, const float *d_taps,
                      cudaStream_t st);
+
+// Ram-Lak only: odd taps godd[q] = h[2q - 2R + 1] (q in [0, 2R)), h0 = h[0].
+int launch_ramlak_rows(const float *in_am, float *out_am, int R, int A, const float *d_godd,
+                       float h0, cudaStream_t st);
 
 // bresenham.cu
 struct DDAGeom {

@@ -71,7 +71,7 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         return set_error(RG_EINVAL, "degenerate or non-finite corners");
     const double tol = 1.0 / sqrt(2);
 
-    double wbp[2] = {0.0, 0.0}, wadj[2] = {0.0, 0.0};
+    double wbp[3] = {0.0, 0.0, 0.0}, wadj[3] = {0.0, 0.0, 0.0};
     bool adj_ok = true;
     for (int e = 0; e < nv; ++e) {
         int j = views ? views[e] : e;
@@ -114,8 +114,8 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         v.P = (float)fabs(rk);
         v.view = j;
         if (fabs(rk) < 1.0 - 1e-9) adj_ok = false;
-        for (int t = 0; t < 2; ++t) {
-            const double th = t ? 63.0 : 31.0;      // tile height - 1
+        for (int t = 0; t < 3; ++t) {
+            const double th = t == 2 ? 127.0 : t ? 63.0 : 31.0;   // tile height - 1
             wbp[t] = std::max(wbp[t], th * fabs(brow) + 31.0 * fabs(bcol));
             wadj[t] = std::max(wadj[t], th * fabs(krow) + 31.0 * fabs(kcol));
         }
@@ -128,7 +128,7 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         if ((views ? views[e] : e) != (views ? views[e - 1] : e - 1) + 1) p.contiguous = false;
     p.dth = (float)dth;
     p.adj_ok = adj_ok;
-    for (int t = 0; t < 2; ++t) {
+    for (int t = 0; t < 3; ++t) {
         p.wmax_bp[t] = (int)ceil(wbp[t] + 1e-6) + 4;
         p.wmax_adj[t] = (int)ceil(wadj[t] + 1e-6) + 4;
     }
@@ -246,12 +246,12 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
                                                 float *__restrict__ em_x,
                                                 const float *__restrict__ inv_sens,
                                                 int *__restrict__ err, long long zs,
-                                                long long zo)
+                                                long long zo, unsigned pair_bytes)
 {
     extern __shared__ float2 pairs[];          // [kSlots][WMAX]
     gather_tile<MODE, WMAX, ROWS, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, scale,
                                       out + blockIdx.z * zo, cs, ls, em_x, inv_sens, err,
-                                      blockIdx.x, blockIdx.y, pairs);
+                                      blockIdx.x, blockIdx.y, pairs, pair_bytes);
 }
 
 template <int MODE, int WMAX, int ROWS, bool EM>
@@ -265,7 +265,7 @@ static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
     auto k = k_gather<MODE, WMAX, ROWS, EM>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, p.g.N, scale, out, cs, ls,
-                               em_x, inv_sens, d_err, z.in, z.out);
+                               em_x, inv_sens, d_err, z.in, z.out, (unsigned)sizeof(float2));
     RG_CK_LAUNCH("k_gather");
     return RG_OK;
 }
@@ -289,8 +289,10 @@ static int gather_rows(const SSPlan &p, int rows, const float *s_am, int s_ld, f
                        long long cs, long long ls, float *em_x, const float *inv_sens, int *d_err,
                        cudaStream_t st, const Stack &z)
 {
-    const int t = rows == 8 ? 1 : 0;
+    const int t = rows == 16 ? 2 : rows == 8 ? 1 : 0;
     const int w = (MODE == 0) ? p.wmax_bp[t] : p.wmax_adj[t];
+    if (rows == 16)
+        return gather_mode<MODE, 16, EM>(p, w, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
     if (rows == 8)
         return gather_mode<MODE, 8, EM>(p, w, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
     return gather_mode<MODE, 4, EM>(p, w, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);

@@ -247,21 +247,34 @@ __device__ __forceinline__ float fma_sat(float a, float b, float c)
 // the pixel); with w1 = 1 + f they are sat(-P w1 + 1 + P) and
 // sat(P w1 + 1 - 2P).  At line positions m = 0 and m = N-1 the Radon drops
 // samples with u < 0 and u >= N-1; BORDER applies exactly that rule.
+// One staged pair from the 32-bit shared address base + idx * pair_bytes.
+// pair_bytes (== 8) arrives as a kernel argument, so the address is an
+// integer multiply-add on the FMA pipe rather than a shift + LEA on the
+// integer ALU pipe, which the inner loops keep busy with the weight bits.
+__device__ __forceinline__ float2 lds_pair(unsigned base, unsigned idx, unsigned pair_bytes)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                 : "=f"(v.x), "=f"(v.y) : "r"(idx * pair_bytes + base));
+    return v;
+}
+
 template <int MODE, int WMAX, int ROWS, bool BORDER>
 __device__ __forceinline__ void accumulate(float (&part)[ROWS], const float2 *__restrict__ pairs,
                                            const SlotInfo *slot, const float *slotP,
                                            const int *slotFlags, int nslot, int lane, int warp,
-                                           int col, int myrow, int N)
+                                           int col, int myrow, int N, unsigned pair_bytes)
 {
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(pairs);
     for (int s = 0; s < nslot; ++s) {
         const SlotInfo si = slot[s];
         if (si.nlo == INT_MIN) continue;
-        const float2 *__restrict__ pw = pairs + s * WMAX;
+        const unsigned pw = sbase + (unsigned)(s * WMAX) * pair_bytes;
         unsigned vpos = si.base + (unsigned)(lane * si.a) + (unsigned)(warp * ROWS * si.b);
         if (MODE == 0) {
 #pragma unroll
             for (int r = 0; r < ROWS; ++r) {
-                const float2 pr = pw[vpos >> 23];
+                const float2 pr = lds_pair(pw, vpos >> 23, pair_bytes);
                 part[r] += fmaf(frac_plus_one(vpos), pr.y, pr.x);
                 vpos += (unsigned)si.b;
             }
@@ -274,7 +287,7 @@ __device__ __forceinline__ void accumulate(float (&part)[ROWS], const float2 *__
 #pragma unroll
             for (int r = 0; r < ROWS; ++r) {
                 const float w1 = frac_plus_one(vpos);
-                const float2 pr = pw[vpos >> 23];
+                const float2 pr = lds_pair(pw, vpos >> 23, pair_bytes);
                 float wa = fma_sat(-P, w1, c0);
                 float wb = fma_sat(P, w1, c1);
                 if (BORDER) {
@@ -306,7 +319,7 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
                                             long long ls, float *__restrict__ em_x,
                                             const float *__restrict__ inv_sens,
                                             int *__restrict__ err, int tx, int ty,
-                                            float2 *__restrict__ pairs)
+                                            float2 *__restrict__ pairs, unsigned pair_bytes)
 {
     constexpr int TH = kWarps * ROWS;          // tile height
     __shared__ SlotInfo slot[kSlots];
@@ -396,10 +409,10 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
         for (int r = 0; r < ROWS; ++r) part[r] = 0.f;
         if (MODE != 0 && border)
             accumulate<MODE, WMAX, ROWS, true>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                               warp, col, myrow, N);
+                                               warp, col, myrow, N, pair_bytes);
         else
             accumulate<MODE, WMAX, ROWS, false>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                                warp, col, myrow, N);
+                                                warp, col, myrow, N, pair_bytes);
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) {
             if (MODE == 2) {
