@@ -228,6 +228,46 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7):
     }
 
 
+def em_run(torch, rg, n=1024, nviews=720, seed=5):
+    """Config-3 workload: 1024^2 emission slice (random ellipses), 720 views,
+    1024 rays, Poisson counts with mean 50 per bin; plain EM 100 iterations
+    vs OSEM 10 interleaved subsets x 10 iterations, x0 = 1, FP64
+    sensitivities.  One slice per call through rg_em."""
+    import numpy as np
+    from pyraft_gb300 import _native
+    from pyraft_gb300.raftypes import rg_image
+    L = _native.load()
+    rng = np.random.default_rng(seed)
+    ph = rg.phantom_fromdesc((n, n), rg.random_ellipses(40, rng), device=True)
+    ph = rg.gpu_image(torch.flip(ph.data, dims=[0]).abs().contiguous())
+    p = rg.radon(ph, (n, nviews), rg.radon_method.SLANTSTACK).data
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    y = torch.poisson(p.clamp(min=0) * (50.0 / float(p.mean())), generator=gen).contiguous()
+    x = torch.ones((n, n), device="cuda")
+    S = rg_image(rg.gpu_image(y, (0.0, 1.0), (math.pi, -1.0)))
+    X = rg_image(rg.gpu_image(x))
+    sp = torch.cuda.current_stream().cuda_stream
+    out = {}
+    for name, it, subsets in (("em_100", 100, 1), ("osem_10x10", 10, 10)):
+        wsb = L.rg_em_workspace(S, X, _native.RG_SLANTSTACK, subsets)
+        ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+        x.fill_(1.0)
+        _native.check(L.rg_em(S, X, _native.RG_SLANTSTACK, 1, subsets, ws.data_ptr(), wsb, sp))
+        x.fill_(1.0)
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        _native.check(L.rg_em(S, X, _native.RG_SLANTSTACK, it, subsets, ws.data_ptr(), wsb, sp))
+        b.record()
+        b.synchronize()
+        t = a.elapsed_time(b) * 1e-3
+        upd = 2.0 * n * n * nviews * it
+        out[name] = {"seconds": round(t, 4), "slices_per_s": round(1.0 / t, 3),
+                     "gups": round(upd / t / 1e9, 1)}
+    return {"size": n, "views": nviews, **out}
+
+
 def tvls_run(torch, rg, nslices=64, n=512, nviews=360, steps=200, seed=11):
     """Config-4 workload: 64 random-ellipse slices of 512^2, 360 views, 512
     rays, Gaussian noise sigma = 1% of max; TV-regularised least squares
@@ -266,7 +306,7 @@ def main():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="fbp", choices=["fbp", "osem", "tvls"],
+    ap.add_argument("--workload", default="fbp", choices=["fbp", "osem", "tvls", "em"],
                     help="fbp: the headline FBP line; osem: batched uneven OSEM "
                          "(256 slices, 10 subsets x 20 iterations) vs the plain form")
     ap.add_argument("--slices", type=int, default=256)
@@ -278,6 +318,13 @@ def main():
 
     if args.impl == "reference":
         return reference_arm(args, rank, world, warm)
+    if args.workload == "em":
+        import torch
+        import pyraft_gb300 as rg
+        torch.cuda.set_device(local)
+        print(json.dumps({"workload": "EM 100 iterations vs OSEM 10x10, 1024^2, 720 views",
+                          **em_run(torch, rg)}))
+        return
     if args.workload == "tvls":
         import torch
         import pyraft_gb300 as rg

@@ -156,6 +156,16 @@ size_t rg_radon_transpose_bresenham_workspace(rg_image sino, rg_image image);
 int rg_radon_transpose_bresenham(rg_image sino, rg_image image,
                                  void *workspace, size_t workspace_bytes, void *stream);
 
+/* Normalised backprojection: per pixel sum(s * sigma) / sum(sigma) over
+ * every ray step through it; 0 where no ray passes (the reference divides
+ * 0 by 0).  Replaces raft_backprojection_bresenham
+ * (raft/raft_backprojection_bresenham.cpp:17-251; bound at
+ * pyraft/raftypes.py:154, called by backprojection(), pyraft/backprojection/
+ * backprojection.py:188-189).                                               */
+size_t rg_backprojection_bresenham_workspace(rg_image sino, rg_image image);
+int rg_backprojection_bresenham(rg_image sino, rg_image image,
+                                void *workspace, size_t workspace_bytes, void *stream);
+
 /* Pixel index sequences of a list of rays, for checking the traversal:
  * replaces stepping raft_ddaiterator_set_theta/_set_t/_update/_end
  * (raft/raft_ddaiterator.h:26-33) by hand.  thetas, ts: nrays_in HOST
@@ -166,6 +176,18 @@ int rg_dda_trace(int lines, int columns, const double img_corners[4],
                  const double *thetas, const double *ts, int nrays_in, int cap,
                  int *out_i, int *out_j, double *out_sigma, int *out_count,
                  void *stream);
+
+/* Slant-stack Radon on an explicit mesh: t (radon.lines host doubles) and
+ * theta (radon.columns host doubles) replace the uniform grids; the corners
+ * of `radon` are not used.  nstack slices in one launch (consecutive ones
+ * *_stride floats apart).  Replaces raft_radon_slantstack_withmesh
+ * (raft/raft_radon_slantstack_withmesh.c:45; bound at pyraft/raftypes.py:176,
+ * called by radon_withmesh / radon_3d_stack, pyraft/sinogram/sino.py:251-311). */
+size_t rg_radon_slantstack_withmesh_workspace(rg_image phantom, rg_image radon, int nstack);
+int rg_radon_slantstack_withmesh(rg_image phantom, long long phantom_stride, rg_image radon,
+                                 long long radon_stride, int nstack, const double *t,
+                                 const double *theta, void *workspace, size_t workspace_bytes,
+                                 void *stream);
 
 /* ----------------------------------------------------------------------
  * Ramp filter step of FBP: row-wise spatial convolution along t.
@@ -203,6 +225,17 @@ int rg_fbp(rg_image sino, rg_image image, int kind,
 size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets);
 int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets,
           void *workspace, size_t workspace_bytes, void *stream);
+
+/* Transmission EM: x <- x * A^T(b exp(-A x)) / A^T y with
+ * y = max(rawsino - dark, 0), b = max(flat - dark, 0) (dark.data may be
+ * NULL: no dark field); slant-stack Radon with the exp fused into its
+ * epilogue, matched adjoint with the update fused.  Replaces raft_tr_em_gpu
+ * (raft/raft_transmission_em.cu:16-77), whose update multiplies twice per
+ * iteration (:57,59) and whose Python caller passes one argument too many
+ * (pyraft/iterative/em.py:246); image holds x0 on entry.                    */
+size_t rg_em_transmission_workspace(rg_image rawsino, rg_image image);
+int rg_em_transmission(rg_image rawsino, rg_image flat, rg_image dark, rg_image image,
+                       int niter, void *workspace, size_t workspace_bytes, void *stream);
 
 /* ----------------------------------------------------------------------
  * Batched uneven OSEM: nslices independent reconstructions of different

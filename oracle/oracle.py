@@ -293,3 +293,44 @@ SHEPP_LOGAN = np.array([
 def shepp_logan(n):
     """Shepp-Logan rasterised like pyraft.shepplogan (top-down rows)."""
     return phantom_fromdesc((n, n), SHEPP_LOGAN)
+
+
+def backprojection_bresenham(sino, shape, img_corners=IMG_CORNERS, sino_corners=SINO_CORNERS,
+                             threads=None):
+    """restates raft/raft_backprojection_bresenham.cpp:17-251 (0 where no
+    ray passes)"""
+    sino = np.ascontiguousarray(sino, dtype=np.float64)
+    out = np.zeros(tuple(shape))
+    I, S = _img(out, img_corners), _img(sino, sino_corners)
+    rc = lib().orc_backprojection_bresenham(ctypes.byref(S), ctypes.byref(I),
+                                            ctypes.c_int(threads or nthreads()))
+    assert rc == 0
+    return out
+
+
+def radon_slantstack_withmesh(img, t, theta, img_corners=IMG_CORNERS, threads=None):
+    """restates raft/raft_radon_slantstack_withmesh.c:45-211"""
+    img = np.ascontiguousarray(img, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    out = np.zeros((len(t), len(theta)))
+    I, S = _img(img, img_corners), _img(out, SINO_CORNERS)
+    lib().orc_radon_slantstack_withmesh(ctypes.byref(I), ctypes.byref(S), t.ctypes.data_as(_dp),
+                                        theta.ctypes.data_as(_dp),
+                                        ctypes.c_int(threads or nthreads()))
+    return out
+
+
+def em_transmission(raw, flat, dark, x0, forward, transpose, niter):
+    """Transmission EM x <- x * A^T(b e^{-Ax}) / A^T y with y = max(raw -
+    dark, 0), b = max(flat - dark, 0) (the update of raft/raft_transmission_em
+    .cu:53-60 with its multiply applied once), guards 0/0 -> 0."""
+    y = np.maximum(np.asarray(raw, float) - np.asarray(dark, float), 0.0)
+    b = np.maximum(np.asarray(flat, float) - np.asarray(dark, float), 0.0)
+    x = np.asarray(x0, dtype=np.float64).copy()
+    den = transpose(y)
+    for _ in range(niter):
+        q = b * np.exp(-forward(x))
+        num = transpose(q)
+        x = np.where(den != 0.0, x * num / np.where(den != 0.0, den, 1.0), 0.0)
+    return x

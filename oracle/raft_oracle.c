@@ -680,3 +680,113 @@ void orc_circular_filter(const double *in, double *out, int R, int V,
     rl_ctx c = {in, out, R, V, 0.0, g, 1};
     orc_parallel(V, nthreads, conv_body, &c);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Normalised DDA backprojection, restating raft_backprojection_bresenham
+ * (raft/raft_backprojection_bresenham.cpp:17-251): per pixel
+ * sum(s * sigma) / sum(sigma) over every ray step that visits it.  Pixels no
+ * ray visits give 0 here (the reference divides 0 by 0).                    */
+typedef struct { const orc_img *in; orc_img *out; double *num, *den; } bn_ctx;
+
+static void bres_norm_body(void *vctx, int lo, int hi, int worker)
+{
+    bn_ctx *c = (bn_ctx *)vctx;
+    const orc_img *s = c->in;
+    orc_img *img = c->out;
+    size_t npix = (size_t)img->lines * img->columns;
+    double *num = c->num + (size_t)worker * npix, *den = c->den + (size_t)worker * npix;
+    orc_dda it;
+    double dth = (s->br_x - s->tl_x) / (s->columns - 1);
+    double dts = (s->br_y - s->tl_y) / (s->lines - 1);
+    memset(num, 0, npix * sizeof(double));
+    memset(den, 0, npix * sizeof(double));
+    orc_dda_set_image(&it, img->lines, img->columns, img->tl_x, img->tl_y, img->br_x, img->br_y);
+    for (int j = lo; j < hi; ++j) {
+        orc_dda_set_theta(&it, s->tl_x + (j * dth));
+        for (int i = 0; i < s->lines; ++i) {
+            double sv = AT(s, i, j);
+            orc_dda_set_t(&it, s->tl_y + (i * dts));
+            while (!orc_dda_end(&it)) {
+                size_t e = (size_t)it.i * img->columns + it.j;
+                num[e] += sv * it.sigma;
+                den[e] += it.sigma;
+                orc_dda_update(&it);
+            }
+        }
+    }
+}
+
+int orc_backprojection_bresenham(const orc_img *sino, orc_img *img, int nthreads)
+{
+    int w = orc_workers(sino->columns, nthreads);
+    size_t npix = (size_t)img->lines * img->columns;
+    double *num = (double *)malloc((size_t)w * npix * sizeof(double));
+    double *den = (double *)malloc((size_t)w * npix * sizeof(double));
+    if (!num || !den) { free(num); free(den); return -1; }
+    bn_ctx c = {sino, img, num, den};
+    orc_parallel(sino->columns, w, bres_norm_body, &c);
+    for (size_t e = 0; e < npix; ++e) {
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < w; ++k) { a += num[(size_t)k * npix + e]; b += den[(size_t)k * npix + e]; }
+        img->p[e] = (b != 0.0) ? a / b : 0.0;
+    }
+    free(num);
+    free(den);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Slant-stack Radon on an explicit (t, theta) mesh, restating
+ * eval_rayintegral_mesh (raft/raft_radon_slantstack_withmesh.c:122-211):
+ * the ray integral of orc_radon_slantstack with theta_j = theta[j] and
+ * t_k = t[k] instead of the uniform grids.  Every output is computed (the
+ * reference's thread split drops the remainder, :65-67).                   */
+typedef struct { const orc_img *img; orc_img *sino; const double *t, *th; } mesh_ctx;
+
+static double mesh_ray(const orc_img *img, double tt, double th)
+{
+    const int size = img->lines;
+    const double tol = 1.0 / sqrt(2);
+    double xmin = img->tl_x, xmax = img->br_x, ymin = img->br_y, ymax = img->tl_y;
+    double dx = (xmax - xmin) / (size - 1), dy = (ymax - ymin) / (size - 1);
+    double cost = cos(th), sint = sin(th), tant = tan(th);
+    double sum = 0.0;
+    if (fabs(cost) < tol) {
+        double Delta = (dy / fabs(sint));
+        for (int i = 0; i < size; ++i) {
+            double x = (double)(xmin + i * dx);
+            double y = (double)(tt / sint - x / tant);
+            int m = (int)floor((y - ymin) / dy);
+            if (m > -1 && m < size - 1)
+                sum += (AT(img, m + 1, i) - AT(img, m, i)) * (y - (ymin + m * dy)) / dy + AT(img, m, i);
+        }
+        return sum * Delta;
+    }
+    double Delta = (dx / fabs(cost));
+    for (int i = 0; i < size; ++i) {
+        double y = (double)(xmin + i * dy);
+        double x = (double)(tt / cost - y * tant);
+        int m = (int)floor((x - xmin) / dx);
+        if (m > -1 && m < size - 1)
+            sum += (AT(img, i, m + 1) - AT(img, i, m)) * (x - (xmin + m * dx)) / dx + AT(img, i, m);
+    }
+    return sum * Delta;
+}
+
+static void mesh_body(void *vctx, int lo, int hi, int worker)
+{
+    mesh_ctx *c = (mesh_ctx *)vctx;
+    orc_img *s = c->sino;
+    (void)worker;
+    for (int w = lo; w < hi; ++w) {
+        int j = w / s->lines, k = w % s->lines;
+        AT(s, k, j) = mesh_ray(c->img, c->t[k], c->th[j]);
+    }
+}
+
+void orc_radon_slantstack_withmesh(const orc_img *img, orc_img *sino, const double *t,
+                                   const double *theta, int nthreads)
+{
+    mesh_ctx c = {img, sino, t, theta};
+    orc_parallel(sino->lines * sino->columns, nthreads, mesh_body, &c);
+}

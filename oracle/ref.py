@@ -28,6 +28,10 @@ class RAFT_IMAGE(ctypes.Structure):
                 ("br_x", ctypes.c_double), ("br_y", ctypes.c_double)]
 
 
+class RAFT_VECTOR(ctypes.Structure):
+    _fields_ = [("p_data", _dp), ("size", ctypes.c_int), ("stride", ctypes.c_int)]
+
+
 class RAFT_DDA(ctypes.Structure):
     """raft_ddaiterator (raft/raft_ddaiterator.h:10-47)."""
     _fields_ = [("i", ctypes.c_int), ("j", ctypes.c_int), ("sigma", ctypes.c_double),
@@ -59,9 +63,13 @@ def lib():
     if _lib is None:
         _lib = ctypes.CDLL(_o.REF_SO)
         for name in ("raft_radon_slantstack", "raft_backprojection_slantstack",
-                     "raft_radon_bresenham", "raft_radon_transpose_bresenham"):
+                     "raft_radon_bresenham", "raft_radon_transpose_bresenham",
+                     "raft_backprojection_bresenham"):
             getattr(_lib, name).argtypes = [RAFT_IMAGE, RAFT_IMAGE, ctypes.c_int]
             getattr(_lib, name).restype = None
+        _lib.raft_radon_slantstack_withmesh.argtypes = [RAFT_IMAGE, RAFT_IMAGE, RAFT_VECTOR,
+                                                        RAFT_VECTOR, ctypes.c_int]
+        _lib.raft_radon_slantstack_withmesh.restype = None
         _lib.raft_image_phantom_fromdesc.argtypes = [RAFT_IMAGE, RAFT_MATRIX]
         _lib.raft_radon_fromdesc.argtypes = [RAFT_IMAGE, RAFT_MATRIX]
         _lib.raft_ddaiterator_set_image.argtypes = [ctypes.POINTER(RAFT_DDA), RAFT_IMAGE]
@@ -116,6 +124,28 @@ def radon_transpose_bresenham(sino, shape, img_corners=_o.IMG_CORNERS,
     sino = np.ascontiguousarray(sino, dtype=np.float64)
     out = np.zeros(tuple(shape))
     _call2("raft_radon_transpose_bresenham", sino, sino_corners, out, img_corners, threads)
+    return out
+
+
+def backprojection_bresenham(sino, shape, img_corners=_o.IMG_CORNERS,
+                             sino_corners=_o.SINO_CORNERS, threads=4):
+    sino = np.ascontiguousarray(sino, dtype=np.float64)
+    out = np.zeros(tuple(shape))
+    _call2("raft_backprojection_bresenham", sino, sino_corners, out, img_corners, threads)
+    return out
+
+
+def radon_slantstack_withmesh(img, t, theta, img_corners=_o.IMG_CORNERS, threads=1):
+    """The reference drops the last (nrays*nviews mod nthreads) outputs; with
+    threads=1 every output is computed."""
+    img = np.ascontiguousarray(img, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    theta = np.ascontiguousarray(theta, dtype=np.float64)
+    out = np.zeros((len(t), len(theta)))
+    vt = RAFT_VECTOR(t.ctypes.data_as(_dp), len(t), 1)
+    vth = RAFT_VECTOR(theta.ctypes.data_as(_dp), len(theta), 1)
+    lib().raft_radon_slantstack_withmesh(_image(img, img_corners), _image(out, _o.SINO_CORNERS),
+                                         vt, vth, ctypes.c_int(threads))
     return out
 
 

@@ -75,6 +75,13 @@ _SIGS = {
     "rg_radon_bresenham": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
     "rg_radon_transpose_bresenham_workspace": ([_IMG, _IMG], _size_t),
     "rg_radon_transpose_bresenham": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
+    "rg_backprojection_bresenham_workspace": ([_IMG, _IMG], _size_t),
+    "rg_backprojection_bresenham": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
+    "rg_radon_slantstack_withmesh_workspace": ([_IMG, _IMG, _c_int], _size_t),
+    "rg_radon_slantstack_withmesh": ([_IMG, _ll, _IMG, _ll, _c_int, ctypes.POINTER(_c_double),
+                                      ctypes.POINTER(_c_double), _vp, _size_t, _vp], _c_int),
+    "rg_em_transmission_workspace": ([_IMG, _IMG], _size_t),
+    "rg_em_transmission": ([_IMG, _IMG, _IMG, _IMG, _c_int, _vp, _size_t, _vp], _c_int),
     "rg_dda_trace": ([_c_int, _c_int, ctypes.POINTER(_c_double), ctypes.POINTER(_c_double),
                       ctypes.POINTER(_c_double), _c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
                      _c_int),

@@ -6,6 +6,9 @@
 * ``radon_transpose(sino, shape, method)``: BRESENHAM is the exact transpose
   of the DDA Radon (raft_radon_transpose_bresenham); SLANTSTACK (new) is the
   exact transpose of the slant-stack Radon, i.e. the matched adjoint.
+* ``backprojection(sino, plan)`` with a BRESENHAM plan: the normalised DDA
+  backprojection (raft_backprojection_bresenham), sum(s sigma) / sum(sigma)
+  per pixel, 0 where no ray passes.
 * ``backprojection_gpu(sino, shape)``: host arrays in and out, default
   geometry, slant-stack backprojection.
 The Fourier-domain families (BST, ANDERSSON, ANDERSSONPB) are not part of
@@ -54,6 +57,9 @@ def backprojection(sino, plan, **kwargs):
     L = _native.load()
     if method_id(method) == method_id(radon_method.SLANTSTACK):
         return _gather(L.rg_backprojection_slantstack, L.rg_backprojection_slantstack_workspace,
+                       sino, shape, kwargs)
+    if method_id(method) == method_id(radon_method.BRESENHAM):
+        return _gather(L.rg_backprojection_bresenham, L.rg_backprojection_bresenham_workspace,
                        sino, shape, kwargs)
     raise TypeError('Unsupported method for Backprojection!')
 

@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libraftgb.so")
-UNITS = ("api", "slantstack", "aux", "filter", "bresenham", "em", "batch", "noalloc", "f64")
+UNITS = ("api", "slantstack", "aux", "filter", "bresenham", "em", "batch", "noalloc", "f64", "mesh")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -51,7 +51,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with tempfile.TemporaryDirectory() as tmp:
         def one(src):
             obj = os.path.join(tmp, os.path.basename(src)[:-3] + ".o")
-            cmd = [cc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+            # RG_NVCC_EXTRA: extra compile flags (development experiments)
+            extra = os.environ.get("RG_NVCC_EXTRA", "").split()
+            cmd = [cc, *ARCH, *FLAGS, *extra, "-c", src, "-o", obj]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")

@@ -684,6 +684,7 @@ static int check_dda(const rg_image &img, const rg_image &sino)
     if (img.lines < 2 || img.columns < 2 || sino.lines < 2 || sino.columns < 2)
         return set_error(RG_EINVAL, "DDA projector needs >= 2 lines and columns in image and "
                                     "sinogram (the sampling distances divide by n - 1)");
+    if (sino.columns > 65535) return set_error(RG_EINVAL, "DDA projector: at most 65535 views");
     return RG_OK;
 }
 
@@ -779,6 +780,41 @@ int rg_radon_transpose_bresenham(rg_image sino, rg_image image, void *ws, size_t
         !(rc = launch_bres_transpose(g, (const double *)cs->p, am, img, 0, 1, st)))
         rc = launch_copy2d(img, g.columns, 1, image.data, image.column_stride, image.line_stride,
                            g.lines, g.columns, st);
+    scratch_end(s);
+    return rc;
+}
+
+size_t rg_backprojection_bresenham_workspace(rg_image sino, rg_image image)
+{
+    return ws_total({(size_t)sino.lines * sino.columns * sizeof(float),
+                     (size_t)image.lines * image.columns * sizeof(double),
+                     (size_t)image.lines * image.columns * sizeof(double)});
+}
+
+int rg_backprojection_bresenham(rg_image sino, rg_image image, void *ws, size_t wsb, void *stream)
+{
+    int rc = check_dda(image, sino);
+    if (!rc) rc = check_ws(ws);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const DDAGeom g = dda_geom(image, sino);
+    std::shared_ptr<DevTable> cs;
+    if ((rc = dda_views(g, cs))) return rc;
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, rg_backprojection_bresenham_workspace(sino, image), st)))
+        return rc;
+    const size_t npix = (size_t)g.lines * g.columns;
+    float *am = (float *)s.take((size_t)g.R * g.A * sizeof(float));
+    double *num = (double *)s.take(npix * sizeof(double));
+    double *den = (double *)s.take(npix * sizeof(double));
+    if (!(rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, g.R, g.A, am, st))) {
+        cudaError_t e = cudaMemsetAsync(num, 0, npix * sizeof(double), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(den, 0, npix * sizeof(double), st);
+        if (e != cudaSuccess) rc = cuda_error(e, "normalised backprojection zeroing");
+    }
+    if (!rc)
+        rc = launch_bres_normalised(g, (const double *)cs->p, am, num, den, image.data,
+                                    image.column_stride, image.line_stride, st);
     scratch_end(s);
     return rc;
 }

@@ -210,6 +210,23 @@ __global__ void k_invert(const float *__restrict__ s, float *__restrict__ inv, s
         inv[e] = (s[e] > 0.f) ? 1.f / s[e] : 0.f;
 }
 
+__global__ void k_sub_clamp(const float *__restrict__ a, const float *__restrict__ b,
+                            float *__restrict__ o, size_t n)
+{
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
+         e += (size_t)gridDim.x * blockDim.x)
+        o[e] = fmaxf(a[e] - (b ? b[e] : 0.f), 0.f);
+}
+
+int launch_sub_clamp(const float *a, const float *b, float *out, size_t n, cudaStream_t st)
+{
+    if (n == 0) return RG_OK;
+    int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+    k_sub_clamp<<<blocks, 256, 0, st>>>(a, b, out, n);
+    RG_CK_LAUNCH("k_sub_clamp");
+    return RG_OK;
+}
+
 int launch_em_update(float *x, const float *bp, const float *inv, size_t n, cudaStream_t st)
 {
     if (n == 0) return RG_OK;

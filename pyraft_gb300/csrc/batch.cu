@@ -92,17 +92,17 @@ __global__ __launch_bounds__(128) void k_batch_radon(const BatchSlice *__restric
         const BatchSlice &b = d[find_slice(d, n, item, kRadon)];
         const int local = item - b.begin[kRadon], rb = (b.R + 31) / 32;
         if (VPT == 2)
-            radon_tile2<true>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
+            radon_tile2<kEpiRatio>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
                               b.R, local % rb, local / rb);
         else
-            radon_tile<true>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
+            radon_tile<kEpiRatio>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
                              b.R, local % rb, local / rb);
     }
 }
 
 // MODE 1: adjoint with the EM update; MODE 2: FP64 sensitivity -> inv_sens.
 // Tiles are 32 columns x 8*kBatchRows rows.
-constexpr int kBatchRows = 4;
+constexpr int kBatchRows = 8;
 
 template <int MODE, int WMAX>
 __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restrict__ d, int n,

@@ -233,16 +233,17 @@ int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, lo
 }
 
 // s(i, j) = s_am[j * R + i]; img_c: contiguous lines x columns, pre-zeroed.
+// den != nullptr: also accumulate the intersection lengths.
 __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double *__restrict__ cs_tab,
                                                         const float *__restrict__ s_am,
                                                         float *__restrict__ img_c, int first,
-                                                        int stride)
+                                                        int stride, float *__restrict__ den)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = first + blockIdx.y * stride;
     if (i >= g.R) return;
     const float sv = s_am[(size_t)j * g.R + i];
-    if (sv == 0.f) return;
+    if (sv == 0.f && !den) return;
     DDA it;
     dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
     dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
@@ -250,9 +251,61 @@ __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double 
     dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
     for (int step = 0; step < cap && !dda_end(it); ++step) {
-        atomicAdd(img_c + (size_t)it.i * g.columns + it.j, sv * (float)it.sigma);
+        const size_t e = (size_t)it.i * g.columns + it.j;
+        if (sv != 0.f) atomicAdd(img_c + e, sv * (float)it.sigma);
+        if (den) atomicAdd(den + e, (float)it.sigma);
         dda_update(it);
     }
+}
+
+// Normalised backprojection in FP64: sum(s sigma) and sum(sigma) per pixel.
+// A pixel grazed by a single short intersection has a tiny weight sum, and
+// the quotient inherits the relative error of that sum, so both sums stay in
+// FP64 (sigma is FP64 already).
+__global__ __launch_bounds__(128) void k_bres_norm_sums(DDAGeom g, const double *__restrict__ cs_tab,
+                                                        const float *__restrict__ s_am,
+                                                        double *__restrict__ num,
+                                                        double *__restrict__ den)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= g.R) return;
+    const double sv = s_am[(size_t)j * g.R + i];
+    DDA it;
+    dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
+    dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
+    const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
+    dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    const int cap = 2 * (g.lines + g.columns) + 8;
+    for (int step = 0; step < cap && !dda_end(it); ++step) {
+        const size_t e = (size_t)it.i * g.columns + it.j;
+        if (sv != 0.0) atomicAdd(num + e, sv * it.sigma);
+        atomicAdd(den + e, it.sigma);
+        dda_update(it);
+    }
+}
+
+// out(strided) = num / den, 0 where den == 0.
+__global__ void k_bres_normalise(const double *__restrict__ num, const double *__restrict__ den,
+                                 int lines, int cols, float *__restrict__ out, long long cs,
+                                 long long ls)
+{
+    const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
+    if (c >= cols) return;
+    const size_t e = (size_t)r * cols + c;
+    out[(long long)r * cs + (long long)c * ls] = den[e] != 0.0 ? (float)(num[e] / den[e]) : 0.f;
+}
+
+int launch_bres_normalised(const DDAGeom &g, const double *d_cs, const float *s_am, double *num,
+                           double *den, float *out, long long cs, long long ls, cudaStream_t st)
+{
+    dim3 grid((g.R + 127) / 128, g.A);
+    k_bres_norm_sums<<<grid, 128, 0, st>>>(g, d_cs, s_am, num, den);
+    RG_CK_LAUNCH("k_bres_norm_sums");
+    dim3 g2((g.columns + 127) / 128, g.lines);
+    k_bres_normalise<<<g2, 128, 0, st>>>(num, den, g.lines, g.columns, out, cs, ls);
+    RG_CK_LAUNCH("k_bres_normalise");
+    return RG_OK;
 }
 
 int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_am, float *img_c,
@@ -261,7 +314,7 @@ int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_a
     const int nv = (g.A - first + stride - 1) / stride;
     if (nv <= 0) return RG_OK;
     dim3 grid((g.R + 127) / 128, nv);
-    k_bres_transpose<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride);
+    k_bres_transpose<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride, nullptr);
     RG_CK_LAUNCH("k_bres_transpose");
     return RG_OK;
 }

@@ -129,11 +129,81 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
     return rc;
 }
 
+// Transmission EM (the update of raft/raft_transmission_em.cu:53-60 applied
+// once per iteration; the reference multiplies twice, :57,59):
+//   x <- x * A^T(b exp(-A x)) / A^T y,  y = max(raw - dark, 0),
+//   b = max(flat - dark, 0),
+// whose fixed point A^T(b exp(-A x)) = A^T y is the stationarity condition
+// of the Poisson transmission likelihood.  exp is fused into the Radon
+// epilogue and the update into the adjoint epilogue; 1 / A^T y is formed
+// once in FP64 (0 where A^T y == 0).
+static int tr_em_ss(const rg_image &raw, const rg_image &flat, const rg_image &dark,
+                    const rg_image &image, int niter, void *ws, size_t wsb, cudaStream_t st)
+{
+    SSGeom g = make_ss_geom(image, raw);
+    const int N = g.N, R = g.R, A = g.A;
+    const SSPlan *p = nullptr;
+    void *h = nullptr;
+    int rc = get_ss_plan(g, 1, 0, &p, &h);
+    if (rc) return rc;
+    Holders hold;
+    hold.h.push_back(h);
+    if (!p->adj_ok)
+        return set_error(RG_EUNSUPPORTED, "EM needs ray spacing >= pixel spacing (nrays <= size)");
+    const size_t sb = (size_t)R * A * sizeof(float), ib = (size_t)N * N * sizeof(float);
+    Scratch s;
+    if ((rc = scratch_begin(s, ws, wsb, ws_sum({sb, sb, sb, sb, radon_pairs_bytes(N),
+                                                radon_pairs_bytes(N), ib, ib}), st)))
+        return rc;
+    float *y = (float *)s.take(sb), *b = (float *)s.take(sb), *q = (float *)s.take(sb);
+    float *d = (float *)s.take(sb);
+    float2 *prow = (float2 *)s.take(radon_pairs_bytes(N));
+    float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N));
+    float *x = (float *)s.take(ib), *inv = (float *)s.take(ib);
+    rc = launch_to_am(raw.data, raw.column_stride, raw.line_stride, R, A, y, st);
+    if (!rc) rc = launch_to_am(flat.data, flat.column_stride, flat.line_stride, R, A, b, st);
+    if (!rc && dark.data) rc = launch_to_am(dark.data, dark.column_stride, dark.line_stride, R, A, d, st);
+    if (!rc) rc = launch_sub_clamp(y, dark.data ? d : nullptr, y, (size_t)R * A, st);
+    if (!rc) rc = launch_sub_clamp(b, dark.data ? d : nullptr, b, (size_t)R * A, st);
+    if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, N, 1, N, N, st);
+    if (!rc) rc = launch_gather(*p, 2, y, R, inv, N, 1, nullptr, nullptr, nullptr, st);
+    for (int it = 0; it < niter && !rc; ++it) {
+        if ((rc = launch_line_pairs(x, N, 1, N, prow, pcol, st))) break;
+        if ((rc = launch_radon(*p, prow, pcol, q, R, b, R, st, 1, 0, 0, kEpiTransmissionId))) break;
+        rc = launch_gather(*p, 1, q, R, nullptr, 0, 0, x, inv, nullptr, st);
+    }
+    if (!rc) rc = launch_copy2d(x, N, 1, image.data, image.column_stride, image.line_stride, N, N, st);
+    scratch_end(s);
+    return rc;
+}
+
 }  // namespace rg
 
 using namespace rg;
 
 extern "C" {
+
+size_t rg_em_transmission_workspace(rg_image rawsino, rg_image image)
+{
+    const size_t sb = (size_t)rawsino.lines * rawsino.columns * sizeof(float);
+    const size_t ib = (size_t)image.lines * image.columns * sizeof(float);
+    return ws_sum({sb, sb, sb, sb, radon_pairs_bytes(image.lines), radon_pairs_bytes(image.lines),
+                   ib, ib});
+}
+
+int rg_em_transmission(rg_image rawsino, rg_image flat, rg_image dark, rg_image image, int niter,
+                       void *ws, size_t wsb, void *stream)
+{
+    if (!rawsino.data || !flat.data || !image.data)
+        return set_error(RG_EINVAL, "rg_em_transmission: null data pointer");
+    if (niter < 0) return set_error(RG_EINVAL, "rg_em_transmission: niter < 0");
+    if (int rc0 = check_ws(ws)) return rc0;
+    if (int rc0 = validate_ss(image, rawsino)) return rc0;
+    if (flat.lines != rawsino.lines || flat.columns != rawsino.columns ||
+        (dark.data && (dark.lines != rawsino.lines || dark.columns != rawsino.columns)))
+        return set_error(RG_EINVAL, "rg_em_transmission: flat/dark shapes differ from the sinogram");
+    return tr_em_ss(rawsino, flat, dark, image, niter, ws, wsb, (cudaStream_t)stream);
+}
 
 size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets)
 {

@@ -125,9 +125,12 @@ int launch_line_pairs(const float *img, long long cs, long long ls, int N,
                       int nz = 1, long long zi = 0, long long zp = 0);
 // Radon over the plan's views; out row v.view (angle-major, ld = out_ld)
 // gets the ray sums, or the EM ratio y/Ax when y_am != nullptr.
+// epi: -1 = ray sums (y_am == nullptr) or EM ratio (y_am != nullptr);
+// kEpiTransmissionId = transmission, out = y_am * exp(-sum).
+constexpr int kEpiTransmissionId = 2;
 int launch_radon(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
                  float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,
-                 int nz = 1, long long zp = 0, long long zo = 0);
+                 int nz = 1, long long zp = 0, long long zo = 0, int epi = -1);
 // Views per thread of the Radon for this plan: 2 when its views are
 // consecutive (the two share L1 lines), else 1.  RG_RADON_VIEWS=1|2 overrides.
 int radon_views_per_thread(const SSPlan &p);
@@ -190,6 +193,8 @@ int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, lo
                       const float *y_am, int first, int stride, cudaStream_t st);
 int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_am,
                           float *img_c, int first, int stride, cudaStream_t st);
+// elementwise on view-major sinograms: out = max(a - b, 0) (b may be null)
+int launch_sub_clamp(const float *a, const float *b, float *out, size_t n, cudaStream_t st);
 int launch_em_update(float *x, const float *bp, const float *inv_sens, size_t n, cudaStream_t st);
 int launch_invert(const float *sens, float *inv, size_t n, cudaStream_t st);
 
@@ -198,6 +203,9 @@ int get_ss_plan(const SSGeom &g, int stride, int first, const SSPlan **out, void
 void release_holder(void *holder);
 int get_dda_views(const DDAGeom &g, const double **d_cs, void **holder);
 size_t ws_sum(std::initializer_list<size_t> pieces);
+// num, den: contiguous lines x columns FP64, pre-zeroed; out strided.
+int launch_bres_normalised(const DDAGeom &g, const double *d_cs, const float *s_am, double *num,
+                           double *den, float *out, long long cs, long long ls, cudaStream_t st);
 int launch_dda_trace(int lines, int columns, const double *corners, const double *d_cst, int n,
                      int cap, int *oi, int *oj, double *os, int *ocount, cudaStream_t st);
 

@@ -180,7 +180,7 @@ int launch_line_pairs(const float *img, long long cs, long long ls, int N, float
     return RG_OK;
 }
 
-template <bool RATIO>
+template <int EPI>
 __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                const float2 *__restrict__ pcol, int N,
                                                const View *__restrict__ views, int nv, int R,
@@ -188,11 +188,11 @@ __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                const float *__restrict__ y_am, int y_ld,
                                                long long zp, long long zo)
 {
-    radon_tile<RATIO>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
+    radon_tile<EPI>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
                       out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x, blockIdx.y);
 }
 
-template <bool RATIO>
+template <int EPI>
 __global__ __launch_bounds__(128) void k_radon2(const float2 *__restrict__ prow,
                                                 const float2 *__restrict__ pcol, int N,
                                                 const View *__restrict__ views, int nv, int R,
@@ -200,7 +200,7 @@ __global__ __launch_bounds__(128) void k_radon2(const float2 *__restrict__ prow,
                                                 const float *__restrict__ y_am, int y_ld,
                                                 long long zp, long long zo)
 {
-    radon_tile2<RATIO>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
+    radon_tile2<EPI>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
                        out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x, blockIdx.y);
 }
 
@@ -213,27 +213,35 @@ int radon_views_per_thread(const SSPlan &p)
 
 int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float *out_am,
                  int out_ld, const float *y_am, int y_ld, cudaStream_t st, int nz, long long zp,
-                 long long zo)
+                 long long zo, int epi)
 {
     if (p.nv == 0) return RG_OK;
+    if (epi < 0) epi = y_am ? kEpiRatio : kEpiSum;
+    const int N = p.g.N, R = p.g.R;
     if (radon_views_per_thread(p) == 2) {
-        dim3 grid((p.g.R + 31) / 32, (p.nv + 7) / 8, nz);
-        if (y_am)
-            k_radon2<true><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R,
-                                                 out_am, out_ld, y_am, y_ld, zp, zo);
+        dim3 grid((R + 31) / 32, (p.nv + 7) / 8, nz);
+        if (epi == kEpiRatio)
+            k_radon2<kEpiRatio><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
+                                                      out_ld, y_am, y_ld, zp, zo);
+        else if (epi == kEpiTransmission)
+            k_radon2<kEpiTransmission><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R,
+                                                             out_am, out_ld, y_am, y_ld, zp, zo);
         else
-            k_radon2<false><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R,
-                                                  out_am, out_ld, nullptr, 0, zp, zo);
+            k_radon2<kEpiSum><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
+                                                    out_ld, nullptr, 0, zp, zo);
         RG_CK_LAUNCH("k_radon2");
         return RG_OK;
     }
-    dim3 grid((p.g.R + 31) / 32, (p.nv + 3) / 4, nz);
-    if (y_am)
-        k_radon<true><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R, out_am,
-                                            out_ld, y_am, y_ld, zp, zo);
+    dim3 grid((R + 31) / 32, (p.nv + 3) / 4, nz);
+    if (epi == kEpiRatio)
+        k_radon<kEpiRatio><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
+                                                 out_ld, y_am, y_ld, zp, zo);
+    else if (epi == kEpiTransmission)
+        k_radon<kEpiTransmission><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
+                                                        out_ld, y_am, y_ld, zp, zo);
     else
-        k_radon<false><<<grid, 128, 0, st>>>(prow, pcol, p.g.N, p.d_views, p.nv, p.g.R, out_am,
-                                             out_ld, nullptr, 0, zp, zo);
+        k_radon<kEpiSum><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am, out_ld,
+                                               nullptr, 0, zp, zo);
     RG_CK_LAUNCH("k_radon");
     return RG_OK;
 }

@@ -90,8 +90,23 @@ __device__ __forceinline__ void radon_line_range(long long u0, long long q, int 
 
 }
 
+// Radon epilogues: kEpiSum writes the ray sum; kEpiRatio the EM ratio
+// y / (A x) (0 where A x == 0); kEpiTransmission b exp(-(A x)), with b read
+// from the y argument.
+enum { kEpiSum = 0, kEpiRatio = 1, kEpiTransmission = 2 };
+
+__device__ __forceinline__ float radon_epilogue(int epi, float val, const float *y, size_t idx)
+{
+    if (epi == kEpiRatio) {
+        const float yv = y[idx];
+        return (val != 0.f) ? yv / val : 0.f;
+    }
+    if (epi == kEpiTransmission) return y[idx] * expf(-val);
+    return val;
+}
+
 // One CTA (128 threads) = rays [32 bx, 32 bx + 32) of views [4 by, 4 by + 4).
-template <bool RATIO>
+template <int EPI>
 __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
                                            const float2 *__restrict__ pcol, int N,
                                            const View *__restrict__ views, int nv, int R,
@@ -131,12 +146,8 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
             kahan_add(acc, comp, part);
         }
     }
-    float val = (acc - comp) * v.delta;
-    if (RATIO) {
-        const float y = y_am[(size_t)v.view * y_ld + k];
-        val = (val != 0.f) ? y / val : 0.f;
-    }
-    out_am[(size_t)v.view * out_ld + k] = val;
+    const float val = (acc - comp) * v.delta;
+    out_am[(size_t)v.view * out_ld + k] = radon_epilogue(EPI, val, y_am, (size_t)v.view * y_ld + k);
 }
 
 // Two views per thread: a CTA (128 threads) covers rays [32 bx, 32 bx + 32) of
@@ -147,7 +158,7 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
 // of both views' line ranges; a sample index outside a view's own range is
 // clamped (one unsigned min) onto the line's zero pad at N+1, so it adds 0
 // and never leaves the padded line.
-template <bool RATIO>
+template <int EPI>
 __device__ __forceinline__ void radon_tile2(const float2 *__restrict__ prow,
                                             const float2 *__restrict__ pcol, int N,
                                             const View *__restrict__ views, int nv, int R,
@@ -194,17 +205,12 @@ __device__ __forceinline__ void radon_tile2(const float2 *__restrict__ prow,
             kahan_add(accb, compb, pb);
         }
     }
-    float vala = (acca - compa) * va.delta, valb = (accb - compb) * vb.delta;
-    if (RATIO) {
-        const float ya = y_am[(size_t)va.view * y_ld + k];
-        vala = (vala != 0.f) ? ya / vala : 0.f;
-        if (two) {
-            const float yb = y_am[(size_t)vb.view * y_ld + k];
-            valb = (valb != 0.f) ? yb / valb : 0.f;
-        }
-    }
-    out_am[(size_t)va.view * out_ld + k] = vala;
-    if (two) out_am[(size_t)vb.view * out_ld + k] = valb;
+    const float vala = (acca - compa) * va.delta, valb = (accb - compb) * vb.delta;
+    out_am[(size_t)va.view * out_ld + k] =
+        radon_epilogue(EPI, vala, y_am, (size_t)va.view * y_ld + k);
+    if (two)
+        out_am[(size_t)vb.view * out_ld + k] =
+            radon_epilogue(EPI, valb, y_am, (size_t)vb.view * y_ld + k);
 }
 
 // ============================================================================
@@ -251,11 +257,20 @@ __device__ __forceinline__ float fma_sat(float a, float b, float c)
 // pair_bytes (== 8) arrives as a kernel argument, so the address is an
 // integer multiply-add on the FMA pipe rather than a shift + LEA on the
 // integer ALU pipe, which the inner loops keep busy with the weight bits.
+// RG_LDS_ADDR_IMAD=0 at compile time selects plain indexing instead.
+#ifndef RG_LDS_ADDR_IMAD
+#define RG_LDS_ADDR_IMAD 1
+#endif
 __device__ __forceinline__ float2 lds_pair(unsigned base, unsigned idx, unsigned pair_bytes)
 {
     float2 v;
+#if RG_LDS_ADDR_IMAD
     asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
                  : "=f"(v.x), "=f"(v.y) : "r"(idx * pair_bytes + base));
+#else
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                 : "=f"(v.x), "=f"(v.y) : "r"((idx << 3) + base));
+#endif
     return v;
 }
 

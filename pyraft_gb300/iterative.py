@@ -154,3 +154,32 @@ def em_plain(sino, size=None, niter=5, nsubsets=1):
     _native.check(_native.load().rg_em_plain_host(
         out.ctypes.data, s.ctypes.data, n, s.shape[0], s.shape[1], int(niter), int(nsubsets)))
     return out
+
+
+def em_transmission_gpu(*args):
+    """pyraft's em_transmission_gpu(s, f, d, img_size=rays, niter=20):
+    transmission EM from raw counts s, flat field f and dark field d (host
+    (rays, views) arrays on the default geometry) -> (img_size, img_size)
+    float64 array.  The update is applied once per iteration (the reference
+    applies it twice, raft/raft_transmission_em.cu:57,59)."""
+    if len(args) < 3:
+        raise TypeError('Not enough arguments!')
+    s, f, d = args[0], args[1], args[2]
+    n = args[3] if len(args) > 3 else s.shape[0]
+    niter = args[4] if len(args) > 4 else 20
+    corners = ((0.0, 1.0), (numpy.pi, -1.0))
+    gs, _ = to_gpu(image(numpy.asarray(s, numpy.float64), top_left=corners[0],
+                         bottom_right=corners[1]))
+    gf, _ = to_gpu(image(numpy.asarray(f, numpy.float64), top_left=corners[0],
+                         bottom_right=corners[1]))
+    gd = None if d is None else to_gpu(image(numpy.asarray(d, numpy.float64),
+                                             top_left=corners[0], bottom_right=corners[1]))[0]
+    x = new_gpu((n, n), (-1.0, 1.0), (1.0, -1.0))
+    x.data.fill_(1.0)
+    L = _native.load()
+    S, F, X = rg_image(gs), rg_image(gf), rg_image(x)
+    D = rg_image(gd) if gd is not None else _native.RG_IMAGE(None, 0, 0, 0, 0, 0., 0., 0., 0.)
+    ws_t, ws = workspace(L.rg_em_transmission_workspace(S, X))
+    _native.check(L.rg_em_transmission(S, F, D, X, int(niter), ws,
+                                       ws_t.numel() if ws_t is not None else 0, stream_ptr()))
+    return numpy.asarray(x.cpu(), dtype=numpy.float64)

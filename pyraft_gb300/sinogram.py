@@ -98,3 +98,84 @@ def _is_tensor(x):
         return isinstance(x, torch.Tensor)
     except ImportError:
         return False
+
+
+def _mesh(vol, theta, t, nstack, img_stride, sino_shape):
+    """Mesh Radon of nstack slices of a device volume `vol` laid out as
+    rg_image views (first slice `vol`, consecutive slices img_stride apart).
+    Returns the (nstack, len(t), len(theta)) float32 device tensor."""
+    import torch
+    L = _native.load()
+    t = numpy.ascontiguousarray(t, dtype=numpy.float64)
+    theta = numpy.ascontiguousarray(theta, dtype=numpy.float64)
+    out = torch.zeros((nstack,) + tuple(sino_shape), dtype=torch.float32, device='cuda')
+    S = _native.RG_IMAGE(out.data_ptr(), sino_shape[0], 1, sino_shape[1], sino_shape[1],
+                         -1.0, 1.0, 1.0, -1.0)
+    dp = ctypes.POINTER(ctypes.c_double)
+    ws_t, ws = workspace(L.rg_radon_slantstack_withmesh_workspace(vol, S, nstack))
+    _native.check(L.rg_radon_slantstack_withmesh(
+        vol, img_stride, S, sino_shape[0] * sino_shape[1], nstack, t.ctypes.data_as(dp),
+        theta.ctypes.data_as(dp), ws, ws_t.numel() if ws_t is not None else 0, stream_ptr()))
+    return out
+
+
+def radon_withmesh(*args):
+    """pyraft's radon_withmesh(f, theta, t=linspace over f's x extent):
+    slant-stack Radon on the given t and theta vectors -> (len(t),
+    len(theta)) host image (default corners, as pyraft)."""
+    if len(args) == 0:
+        raise TypeError('Not enough arguments!')
+    f, theta = args[0], numpy.atleast_1d(numpy.asarray(args[1], dtype=numpy.float64))
+    t = args[2] if len(args) > 2 else numpy.linspace(f.top_left[0], f.bottom_right[0], f.shape[1])
+    g, _ = to_gpu(f)
+    out = _mesh(rg_image(g), theta, t, 1, 0, (len(t), len(theta)))
+    return image(out[0].double().cpu().numpy())
+
+
+def radon_view(*args):
+    """pyraft's radon_view(f, theta, t): one view on the mesh t -> 1-D array."""
+    if len(args) < 2:
+        raise TypeError('Not enough arguments!')
+    f = args[0]
+    t = args[2] if len(args) > 2 else numpy.linspace(f.top_left[0], f.bottom_right[0], f.shape[1])
+    return numpy.asarray(radon_withmesh(f, [float(args[1])], t))[:, 0]
+
+
+def _volume_slices(f):
+    """Device copy of a (N, M, K) volume and the rg_image of slice f[:, 0, :]
+    (slices f[:, i, :] are K floats apart), as pyraft's radon_3d_stack reads
+    them (pyraft/sinogram/sino.py:307-310)."""
+    import torch
+    v = torch.from_numpy(numpy.ascontiguousarray(f, dtype=numpy.float32)).cuda()
+    n0, n1, n2 = v.shape
+    img = _native.RG_IMAGE(v.data_ptr(), n0, 1, n2, n1 * n2, -1.0, 1.0, 1.0, -1.0)
+    return v, img, n2
+
+
+def radon_3d_stack(*args):
+    """pyraft's radon_3d_stack(f, theta, t): mesh Radon of every slice
+    f[:, i, :] (i < f.shape[0]) of a cubic volume, in one launch ->
+    S (len(theta), N, len(t)) with S[:, i, :] = Radon(slice i)^T."""
+    if len(args) == 0:
+        raise TypeError('Not enough arguments!')
+    f = numpy.asarray(args[0])
+    theta = numpy.asarray(args[1], numpy.float64) if len(args) > 1 else numpy.linspace(0, numpy.pi, 180)
+    t = numpy.asarray(args[2], numpy.float64) if len(args) > 2 else numpy.linspace(-1, 1, f.shape[1])
+    n = f.shape[0]
+    v, img, step = _volume_slices(f)
+    out = _mesh(img, theta, t, n, step, (len(t), len(theta)))
+    return numpy.transpose(out.double().cpu().numpy(), (2, 0, 1))
+
+
+def snapshot(*args):
+    """pyraft's snapshot(f, theta=0, t): one view of every slice f[:, k, :]
+    -> (N, len(t))."""
+    if len(args) == 0:
+        raise TypeError('Not enough arguments!')
+    f = numpy.asarray(args[0])
+    theta = float(args[1]) if len(args) > 1 else 0.0
+    t = numpy.asarray(args[2], numpy.float64) if len(args) > 2 else numpy.linspace(-1.0, 1.0, f.shape[1])
+    n = f.shape[0]
+    v, img, step = _volume_slices(f)
+    out = _mesh(img, [theta], t, n, step, (len(t), 1))
+    return out[:, :, 0].double().cpu().numpy()

@@ -76,6 +76,24 @@ def main() -> None:
         img_corners=np.array(ODD_IMG), sino_corners=np.array(ODD_SINO),
     )
 
+    # Normalised DDA backprojection (views start at 0.1: no theta == 0 ray,
+    # whose first sigma the reference leaves unset, enters the weights).
+    s_bn = rng.random((40, 33))
+    out["bres_norm"] = dict(
+        sino_in=s_bn, sino_corners=np.array(ODD_SINO),
+        bp=R.backprojection_bresenham(s_bn, (48, 48), sino_corners=ODD_SINO, threads=3),
+        bp_odd=R.backprojection_bresenham(s_bn, (31, 37), ODD_IMG, ODD_SINO, threads=2),
+        img_corners=np.array(ODD_IMG))
+
+    # Mesh Radon: non-uniform t and theta.
+    img_m = rng.random((45, 45))
+    t_m = np.sort(rng.uniform(-1.2, 1.2, 37))
+    th_m = np.sort(rng.uniform(0.0, np.pi, 29))
+    out["mesh"] = dict(img=img_m, t=t_m, theta=th_m,
+                       radon=R.radon_slantstack_withmesh(img_m, t_m, th_m, threads=1),
+                       radon_odd=R.radon_slantstack_withmesh(img_m, t_m, th_m, ODD_IMG, threads=1),
+                       img_corners=np.array(ODD_IMG))
+
     # Rectangular image for the DDA path (the slant-stack path is square-only).
     rect = rng.random((40, 48))
     out["rect"] = dict(img=rect,

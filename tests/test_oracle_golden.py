@@ -127,3 +127,30 @@ def test_live_against_compiled_reference(orc):
                               R.backprojection_slantstack(s, n, threads=1))
         rb = orc.radon_bresenham(img, r, a)
         assert np.array_equal(rb[:, 1:], R.radon_bresenham(img, r, a, threads=2)[:, 1:])
+
+
+def test_normalised_bresenham_backprojection(orc, golden):
+    g = golden("bres_norm")
+    sc = tuple(g["sino_corners"])
+    ic = tuple(g["img_corners"])
+    for key, shape, corners in (("bp", (48, 48), orc.IMG_CORNERS), ("bp_odd", (31, 37), ic)):
+        ours = orc.backprojection_bresenham(g["sino_in"], shape, corners, sc)
+        ref = g[key]
+        hole = ~np.isfinite(ref)            # 0/0 in the reference: no ray passes
+        assert np.all(ours[hole] == 0.0)
+        np.testing.assert_allclose(ours[~hole], ref[~hole], rtol=1e-10, atol=1e-12)
+
+
+def test_mesh_radon(orc, golden):
+    g = golden("mesh")
+    assert np.array_equal(orc.radon_slantstack_withmesh(g["img"], g["t"], g["theta"]), g["radon"])
+    ic = tuple(g["img_corners"])
+    assert np.array_equal(orc.radon_slantstack_withmesh(g["img"], g["t"], g["theta"], ic),
+                          g["radon_odd"])
+    # on the uniform mesh it is the plain slant-stack
+    img = g["img"]
+    A, R = 21, 30
+    th = np.arange(A) * (math.pi / A)
+    t = -1.0 + np.arange(R) * (2.0 / (R - 1))
+    np.testing.assert_allclose(orc.radon_slantstack_withmesh(img, t, th),
+                               orc.radon_slantstack(img, R, A), rtol=1e-12, atol=1e-12)
