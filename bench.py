@@ -40,7 +40,7 @@ UNIT = "GUPS"
 UPDATES = N * N * A
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) of one backprojection
 # launch at this size (profiles/bp_2048x1800_ncu.md).
-BP_TRAFFIC_BYTES = 14957312
+BP_TRAFFIC_BYTES = 14961152
 
 
 def env_rank():
@@ -84,27 +84,40 @@ class Clocks:
         for line in self.proc.stdout:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) >= 7:
-                self.samples.append(parts)
+                self.samples.append((time.perf_counter(), parts))
 
-    def stop(self):
+    def wait_first(self, timeout=5.0):
+        """Block until nvidia-smi has produced its first sample (its start-up
+        takes a few hundred ms), so that the sampling covers the timed steps."""
+        t0 = time.perf_counter()
+        while self.proc and not self.samples and time.perf_counter() - t0 < timeout:
+            time.sleep(0.02)
+
+    def stop(self, t_from=None, t_to=None):
+        """Median SM clock and the throttle reasons over the samples taken in
+        [t_from, t_to] (all samples when no window is given)."""
         if self.proc:
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
             except subprocess.TimeoutExpired:
                 self.proc.kill()
+            self.proc = None
         if self.t:
             self.t.join(timeout=2)
-        if not self.samples:
+            self.t = None
+        got = [p for t, p in self.samples
+               if (t_from is None or t >= t_from) and (t_to is None or t <= t_to)]
+        if not got:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        sm = [float(s[0]) for s in got if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in got if s[1].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for s in self.samples for k in range(4)
+        reasons = sorted({names[k] for s in got for k in range(4)
                           if s[3 + k].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
-                "samples": len(self.samples)}
+                "samples": len(got)}
 
 
 # ----------------------------------------------------------------------------
@@ -366,18 +379,19 @@ def main():
     def step():
         _native.check(L.rg_fbp(S, I, _native.RG_FILTER_RAMLAK, ws.data_ptr(), ws_bytes, sp))
 
+    clocks = Clocks(local)
+    clocks.start()
     for _ in range(warm):
         step()
     torch.cuda.synchronize()
+    clocks.wait_first()
 
     # ---- device-resident steps
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    clocks = Clocks(local)
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    clocks.start()
     wall0 = time.perf_counter()
     for k in range(args.steps):
         flush.zero_()
@@ -385,10 +399,10 @@ def main():
         step()
         ev[k][1].record(stream)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
+    wall1 = time.perf_counter()
+    wall = wall1 - wall0
     if dist:
         dist.barrier()
-    clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
     if dist:
         t = torch.tensor([ms], device="cuda")
@@ -475,6 +489,15 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e_ms = float(t)
     ok = bool(torch.isfinite(h_out).all())
+    wall_end = time.perf_counter()
+    # nvidia-smi samples every 50 ms: a short timed region may hold none, in
+    # which case the window widens to every GPU phase after it (the same
+    # kernels under the same load: kernel-only and end-to-end steps).
+    clk = clocks.stop(wall0, wall1)
+    clk["window"] = "timed steps"
+    if clk["sm_mhz"] is None:
+        clk = clocks.stop(wall0, wall_end)
+        clk["window"] = "timed steps + kernel-only + end-to-end steps"
 
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world,
