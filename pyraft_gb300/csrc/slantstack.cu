@@ -38,6 +38,9 @@
 #include <stdlib.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "ss_tiles.cuh"
@@ -254,12 +257,96 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
                                                 float *__restrict__ em_x,
                                                 const float *__restrict__ inv_sens,
                                                 int *__restrict__ err, long long zs,
-                                                long long zo, unsigned pair_bytes)
+                                                long long zo, unsigned pair_bytes, int split)
 {
     extern __shared__ float2 pairs[];          // [kSlots][WMAX]
     gather_tile<MODE, WMAX, ROWS, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, scale,
                                       out + blockIdx.z * zo, cs, ls, em_x, inv_sens, err,
-                                      blockIdx.x, blockIdx.y, pairs, pair_bytes);
+                                      blockIdx.x / split, blockIdx.y, pairs, pair_bytes, split,
+                                      blockIdx.x % split);
+}
+
+// Cluster size for the view split of a gather launch of `tiles` CTAs: the
+// split in {1, 2, 4} (ROWS divisible by it, >= 64 views per rank) whose
+// last wave is fullest, from the occupancy of the kernel (clusters counted
+// by cudaOccupancyMaxActiveClusters).  Occupancies are cached per kernel, so
+// launches inside a stream capture make no queries once the plain call has
+// run; an uncached query during a capture gives split 1.
+// RG_GATHER_SPLIT=1|2|4 forces a choice.
+struct SplitOcc {
+    int slots[3] = {0, 0, 0};      // concurrent CTAs at split 1, 2, 4
+};
+static std::mutex g_occ_mu;
+static std::map<std::pair<const void *, int>, SplitOcc> g_occ;
+
+static int env_split()
+{
+    const char *e = getenv("RG_GATHER_SPLIT");
+    if (!e) return 0;
+    const int v = atoi(e);
+    return (v == 1 || v == 2 || v == 4) ? v : 0;
+}
+
+template <typename K>
+static int pick_split(K k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st)
+{
+    const int forced = env_split();
+    if (forced) return (rows % forced == 0 && nv >= forced) ? forced : 1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    const auto key = std::make_pair((const void *)k, dev * 4096 + (int)(smem >> 10));
+    SplitOcc occ;
+    bool have = false;
+    {
+        std::lock_guard<std::mutex> lock(g_occ_mu);
+        auto it = g_occ.find(key);
+        if (it != g_occ.end()) { occ = it->second; have = true; }
+    }
+    if (!have) {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+            return 1;
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 1;
+        occ.slots[0] = per_sm * sms;
+        for (int t = 1; t < 3; ++t) {
+            const int S = 1 << t;
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = S;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(grid.x * S, grid.y, grid.z);
+            cfg.blockDim = dim3(256);
+            cfg.dynamicSmemBytes = smem;
+            cfg.stream = st;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int ncl = 0;
+            if (cudaOccupancyMaxActiveClusters(&ncl, k, &cfg) != cudaSuccess) {
+                cudaGetLastError();
+                ncl = 0;
+            }
+            occ.slots[t] = ncl * S;
+        }
+        std::lock_guard<std::mutex> lock(g_occ_mu);
+        g_occ[key] = occ;
+    }
+    const double tiles = (double)grid.x * grid.y * grid.z;
+    int best = 1;
+    double best_e = 0.0;
+    for (int t = 0; t < 3; ++t) {
+        const int S = 1 << t;
+        if (rows % S || nv < 64 * S || occ.slots[t] <= 0) continue;
+        const double w = tiles * S / occ.slots[t];
+        // fullness of the last wave, less a small cost per extra CTA
+        const double e = w / ceil(w) - 0.01 * (S - 1);
+        if (e > best_e + 1e-9) { best_e = e; best = S; }
+    }
+    return best;
 }
 
 template <int MODE, int WMAX, int ROWS, bool EM>
@@ -272,9 +359,29 @@ static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
     const float scale = (MODE == 0) ? p.dth : 1.f;
     auto k = k_gather<MODE, WMAX, ROWS, EM>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, p.g.N, scale, out, cs, ls,
-                               em_x, inv_sens, d_err, z.in, z.out, (unsigned)sizeof(float2));
-    RG_CK_LAUNCH("k_gather");
+    const int split = (MODE == 2) ? 1 : pick_split(k, smem, ROWS, p.nv, grid, st);
+    const unsigned pb = (unsigned)sizeof(float2);
+    if (split == 1) {
+        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, p.g.N, scale, out, cs, ls,
+                                   em_x, inv_sens, d_err, z.in, z.out, pb, 1);
+        RG_CK_LAUNCH("k_gather");
+        return RG_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, p.nv, p.g.N,
+                             scale, out, cs, ls, em_x, inv_sens, d_err, z.in, z.out, pb, split));
+    RG_CK_LAUNCH("k_gather (cluster)");
     return RG_OK;
 }
 

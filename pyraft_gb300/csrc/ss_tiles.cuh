@@ -4,6 +4,8 @@
 // described at the top of slantstack.cu.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include <climits>
 #include <type_traits>
 
@@ -324,9 +326,33 @@ __device__ __forceinline__ void accumulate(float (&part)[ROWS], const float2 *__
     }
 }
 
+// Final value of pixel (row, col) of a gather: stored, or (EM) folded into
+// the multiplicative update x <- x * val * inv_sens.
+template <int MODE, bool EM>
+__device__ __forceinline__ void gather_store(float val, int row, int col, int N,
+                                             float *__restrict__ out, long long cs, long long ls,
+                                             float *__restrict__ em_x,
+                                             const float *__restrict__ inv_sens)
+{
+    if (EM) {
+        const size_t idx = (size_t)row * N + col;
+        em_x[idx] = em_x[idx] * val * inv_sens[idx];
+    } else {
+        out[(long long)row * cs + (long long)col * ls] = val;
+    }
+}
+
 // MODE 0: backprojection; 1: adjoint (FP32 accumulate); 2: adjoint, FP64.
 // One CTA (256 threads) = the tile of 32 columns x 8*ROWS rows at tile
 // coordinates (tx, ty); `pairs` is kSlots * WMAX float2 of shared memory.
+//
+// split > 1 (MODE 0 and 1; the CTA is rank `rank` of a thread-block cluster
+// of `split` CTAs along x that share the tile): this CTA sums views
+// [rank nv / split, (rank + 1) nv / split) only.  The partial sums meet in
+// distributed shared memory and each rank finishes ROWS / split of the rows,
+// adding the partials in rank order (deterministic).  Splitting the views
+// of every tile over a cluster multiplies the CTA count, so the last wave of
+// a grid of few large tiles no longer leaves most SMs idle.
 template <int MODE, int WMAX, int ROWS, bool EM>
 __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int s_ld, int R,
                                             const View *__restrict__ views, int nv, int N,
@@ -334,7 +360,8 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
                                             long long ls, float *__restrict__ em_x,
                                             const float *__restrict__ inv_sens,
                                             int *__restrict__ err, int tx, int ty,
-                                            float2 *__restrict__ pairs, unsigned pair_bytes)
+                                            float2 *__restrict__ pairs, unsigned pair_bytes,
+                                            int split = 1, int rank = 0)
 {
     constexpr int TH = kWarps * ROWS;          // tile height
     __shared__ SlotInfo slot[kSlots];
@@ -355,8 +382,10 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
 #pragma unroll
     for (int r = 0; r < ROWS; ++r) { acc[r] = 0; comp[r] = 0; }
 
-    for (int chunk = 0; chunk < nv; chunk += kSlots) {
-        const int nslot = min(kSlots, nv - chunk);
+    const int vbeg = (int)((long long)nv * rank / split);
+    const int vend = (int)((long long)nv * (rank + 1) / split);
+    for (int chunk = vbeg; chunk < vend; chunk += kSlots) {
+        const int nslot = min(kSlots, vend - chunk);
         if (warp == 0) {
             SlotInfo si = {0u, 0, 0, INT_MIN};
             int W = 0, view = 0, flags = 0;
@@ -434,13 +463,35 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
                 acc[r] += (double)part[r];
             } else {
                 float a = acc[r], c = comp[r];
-                kahan_add(a, c, (float)part[r]);
+                kahan_add(a, c, part[r]);
                 acc[r] = a; comp[r] = c;
             }
         }
         __syncthreads();
     }
 
+    if (MODE != 2 && split > 1) {
+        // The last chunk ended with a barrier: the staging area is free.
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        float *red = reinterpret_cast<float *>(pairs);    // [ROWS][256]
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r)
+            red[r * 256 + threadIdx.x] = (float)acc[r] - (float)comp[r];
+        cl.sync();
+        const int per = ROWS / split;
+        for (int q = 0; q < per; ++q) {
+            const int r = rank * per + q;
+            float sum = 0.f;
+            for (int src = 0; src < split; ++src)
+                sum += cl.map_shared_rank(red, src)[r * 256 + threadIdx.x];
+            const int row = myrow + r;
+            if (row < N && col < N) gather_store<MODE, EM>(sum * scale, row, col, N, out, cs, ls,
+                                                           em_x, inv_sens);
+        }
+        cl.sync();    // no CTA leaves while a peer still reads its partials
+        return;
+    }
 #pragma unroll
     for (int r = 0; r < ROWS; ++r) {
         const int row = myrow + r;
@@ -449,13 +500,8 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
             const double sv = (double)acc[r];
             out[(long long)row * cs + (long long)col * ls] = (sv > 0.0) ? (float)(1.0 / sv) : 0.f;
         } else {
-            const float val = ((float)acc[r] - (float)comp[r]) * scale;
-            if (EM) {
-                const size_t idx = (size_t)row * N + col;
-                em_x[idx] = em_x[idx] * val * inv_sens[idx];
-            } else {
-                out[(long long)row * cs + (long long)col * ls] = val;
-            }
+            gather_store<MODE, EM>(((float)acc[r] - (float)comp[r]) * scale, row, col, N, out, cs,
+                                   ls, em_x, inv_sens);
         }
     }
 }
