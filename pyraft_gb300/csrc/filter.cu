@@ -90,34 +90,39 @@ namespace rg {
 
 // ----------------------------------------------------------------------------
 // Ram-Lak specialisation.  Its taps vanish at even offsets except 0, so
-// out[n] = h0 in[n] + sum_{n-k odd} h[n-k] in[k].  A thread owns the output
-// pair (n_e, n_o) = (n0 + 2t, n0 + 2t + 1): the even output meets only odd
-// inputs and the odd output only even inputs, both through odd taps.  With
-// g[q] = h[2q + 1 - ...] stored compactly (odd taps only), input pair j
-// (k_e = k0 + 2j, k_o = k_e + 1) contributes
-//     out_e += g[c + t - j] * x[k_o],   out_o += g[c + t - j + 1] * x[k_e],
-// so one new tap is loaded per step and the other is the previous step's.
-// CTA = 512 outputs x 8 views; inputs walked in tiles of 256 (128 pairs).
-constexpr int kRN = 512, kRK = 256, kRA = 8;
+// out[n] = h0 in[n] + sum_{n-k odd} h[n-k] in[k]: an even output meets only
+// odd inputs and an odd output only even inputs, both through odd taps
+// g[q] = h[2q - 2R + 1] (q in [0, 2R); dt included; zero beyond |m| = R-1).
+//
+// Output pair t' (outputs n0 + 2t', n0 + 2t' + 1) and input pair j (inputs
+// k0 + 2j, k0 + 2j + 1) meet through the taps Q = (n0 - k0)/2 + R - 1 + t' - j
+// (even output x odd input) and Q + 1 (odd output x even input).
+//
+// CTA = 1024 outputs x 4 views; thread t owns output pairs 2t and 2t + 1, so
+// at input pair j it needs the three taps G0 = g[Q(2t, j)], G1 = G0's
+// successor and G2 the next one; stepping j by one shifts the three by one
+// place, so each step loads one new tap from shared memory and reuses two.
+// Per step: one LDS.32 (the new tap) + two broadcast LDS.128 (the even and
+// odd inputs of four views) feed 16 FFMAs.  The taps are staged split by
+// index parity so the lanes (which read every other tap) hit distinct banks.
+// Inputs are walked in tiles of 512; per-tile partial sums are added with
+// Kahan compensation.
+constexpr int kRN = 1024, kRK = 512, kRA = 4;
+constexpr int kRT = kRN / 2 + kRK / 2 + 2;      // staged taps per tile (even count)
 
-// godd[q] = h[2q - 2R + 1] (dt included) for q in [0, 2R): every odd offset
-// of [-(2R-1), 2R-1], zero where |m| > R-1.  For the tile (n0, k0) the even
-// output's tap has q1 = (n0 - k0)/2 + R - 1 + t - j and the odd output's
-// q1 + 1; t - j spans [-(kRK/2 - 1), kRN/2 - 1], so the staged taps start at
-// qbase = (n0 - k0)/2 + R - kRK/2 and sg[t - j + kRK/2 - 1] is g1.
 __global__ __launch_bounds__(256) void k_ramlak_rows(const float *__restrict__ in,
                                                      float *__restrict__ out, int R, int A,
                                                      const float *__restrict__ godd, float h0)
 {
-    __shared__ float4 sxe[kRK / 2][kRA / 4];   // even inputs  [pair][view]
-    __shared__ float4 sxo[kRK / 2][kRA / 4];   // odd inputs
-    __shared__ float sg[kRN / 2 + kRK / 2 + 1];
+    __shared__ float4 sxe[kRK / 2];             // even inputs of the tile, 4 views
+    __shared__ float4 sxo[kRK / 2];             // odd inputs
+    __shared__ float sg0[kRT / 2], sg1[kRT / 2];  // staged taps: index 2i -> sg0[i], 2i+1 -> sg1[i]
     const int t = threadIdx.x;
     const int n0 = blockIdx.x * kRN, a0 = blockIdx.y * kRA;
-    const int ne = n0 + 2 * t;
-    float acc_e[kRA], acc_o[kRA], ce[kRA], co[kRA];
+    // accumulator index: 8 * pair + 4 * (odd output) + view
+    float acc[16], comp[16];
 #pragma unroll
-    for (int a = 0; a < kRA; ++a) { acc_e[a] = acc_o[a] = ce[a] = co[a] = 0.f; }
+    for (int i = 0; i < 16; ++i) { acc[i] = 0.f; comp[i] = 0.f; }
 
     for (int k0 = 0; k0 < R; k0 += kRK) {
         float *xe = reinterpret_cast<float *>(sxe), *xo = reinterpret_cast<float *>(sxo);
@@ -127,57 +132,64 @@ __global__ __launch_bounds__(256) void k_ramlak_rows(const float *__restrict__ i
             const float v = (k < R && av < A) ? __ldg(in + (size_t)av * R + k) : 0.f;
             if (kk & 1) xo[(kk >> 1) * kRA + a] = v; else xe[(kk >> 1) * kRA + a] = v;
         }
+        // sg[e] = g[qbase + e]; Q(t', j) - qbase = t' - j + kRK/2 - 1
         const int qbase = (n0 - k0) / 2 + R - kRK / 2;
-        for (int e = t; e < kRN / 2 + kRK / 2 + 1; e += 256) {
+        for (int e = t; e < kRT; e += 256) {
             const int q = qbase + e;
-            sg[e] = (q >= 0 && q < 2 * R) ? __ldg(godd + q) : 0.f;
+            const float g = (q >= 0 && q < 2 * R) ? __ldg(godd + q) : 0.f;
+            if (e & 1) sg1[e >> 1] = g; else sg0[e >> 1] = g;
         }
         __syncthreads();
-        float pe[kRA], po[kRA];
+        float part[16];
 #pragma unroll
-        for (int a = 0; a < kRA; ++a) { pe[a] = po[a] = 0.f; }
-        const int jend = min(kRK / 2, (R - k0 + 1) / 2);
-        // tap for (n_e, k_o = k0 + 2j + 1): m = ne - k0 - 2j - 1 (odd);
-        // its q - qbase = t - j + (kRK / 2 - 1); for (n_o, k_e) it is one more
-        float gnext = sg[t + (kRK / 2 - 1) + 1];
-#pragma unroll 2
-        for (int j = 0; j < jend; ++j) {
-            const float g1 = sg[t - j + (kRK / 2 - 1)];
-            const float g2 = gnext;
-            gnext = g1;
+        for (int i = 0; i < 16; ++i) part[i] = 0.f;
+        // input pairs of this tile that hold data, rounded up to even (the
+        // staged inputs past R are zeros)
+        const int jend = min(kRK / 2, ((R - k0 + 1) / 2 + 1) & ~1);
+        // at step j: G0 = sg[2t + kRK/2 - 1 - j], G1 = sg[.. + 1], G2 = sg[.. + 2]
+        float G1 = sg0[t + kRK / 4], G2 = sg1[t + kRK / 4];
+        for (int j = 0; j < jend; j += 2) {
 #pragma unroll
-            for (int q = 0; q < kRA / 4; ++q) {
-                const float4 xo4 = sxo[j][q];
-                const float4 xe4 = sxe[j][q];
-                pe[4 * q + 0] = fmaf(g1, xo4.x, pe[4 * q + 0]);
-                pe[4 * q + 1] = fmaf(g1, xo4.y, pe[4 * q + 1]);
-                pe[4 * q + 2] = fmaf(g1, xo4.z, pe[4 * q + 2]);
-                pe[4 * q + 3] = fmaf(g1, xo4.w, pe[4 * q + 3]);
-                po[4 * q + 0] = fmaf(g2, xe4.x, po[4 * q + 0]);
-                po[4 * q + 1] = fmaf(g2, xe4.y, po[4 * q + 1]);
-                po[4 * q + 2] = fmaf(g2, xe4.z, po[4 * q + 2]);
-                po[4 * q + 3] = fmaf(g2, xe4.w, po[4 * q + 3]);
+            for (int h = 0; h < 2; ++h) {
+                // 2t + kRK/2 - 1 - (j + h): odd for h = 0, even for h = 1
+                const float G0 = h == 0 ? sg1[t + kRK / 4 - 1 - j / 2]
+                                        : sg0[t + kRK / 4 - 1 - j / 2];
+                const float4 xo4 = sxo[j + h];
+                const float4 xe4 = sxe[j + h];
+                const float o[4] = {xo4.x, xo4.y, xo4.z, xo4.w};
+                const float ev[4] = {xe4.x, xe4.y, xe4.z, xe4.w};
+#pragma unroll
+                for (int v = 0; v < 4; ++v) {
+                    part[v] = fmaf(G0, o[v], part[v]);              // pair 2t, even output
+                    part[4 + v] = fmaf(G1, ev[v], part[4 + v]);     // pair 2t, odd output
+                    part[8 + v] = fmaf(G1, o[v], part[8 + v]);      // pair 2t+1, even output
+                    part[12 + v] = fmaf(G2, ev[v], part[12 + v]);   // pair 2t+1, odd output
+                }
+                G2 = G1;
+                G1 = G0;
             }
         }
 #pragma unroll
-        for (int a = 0; a < kRA; ++a) {
-            float y = pe[a] - ce[a], s = acc_e[a] + y;
-            ce[a] = (s - acc_e[a]) - y;
-            acc_e[a] = s;
-            y = po[a] - co[a];
-            s = acc_o[a] + y;
-            co[a] = (s - acc_o[a]) - y;
-            acc_o[a] = s;
+        for (int i = 0; i < 16; ++i) {
+            const float y = part[i] - comp[i], s = acc[i] + y;
+            comp[i] = (s - acc[i]) - y;
+            acc[i] = s;
         }
         __syncthreads();
     }
+    const int nb = n0 + 4 * t;
 #pragma unroll
-    for (int a = 0; a < kRA; ++a) {
-        const int av = a0 + a;
+    for (int v = 0; v < kRA; ++v) {
+        const int av = a0 + v;
         if (av >= A) break;
         const float *row = in + (size_t)av * R;
-        if (ne < R) out[(size_t)av * R + ne] = fmaf(h0, __ldg(row + ne), acc_e[a] - ce[a]);
-        if (ne + 1 < R) out[(size_t)av * R + ne + 1] = fmaf(h0, __ldg(row + ne + 1), acc_o[a] - co[a]);
+        float *orow = out + (size_t)av * R;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int n = nb + u;
+            const int i = 8 * (u >> 1) + 4 * (u & 1) + v;
+            if (n < R) orow[n] = fmaf(h0, __ldg(row + n), acc[i] - comp[i]);
+        }
     }
 }
 
