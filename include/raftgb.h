@@ -68,6 +68,13 @@ typedef struct {
 const char *rg_last_error(void);
 /* ABI version (major * 100 + minor). */
 int rg_version(void);
+/* Error bits that kernels with in-kernel checks recorded on the current
+ * device since the last call, then cleared (synchronises the device):
+ * 1 = a staged Radon window check failed and its strip was skipped,
+ * 2 = a bounded wait for an asynchronous copy ran out.  0 = none; a
+ * negative RG_E* code if the query itself failed.  No counterpart in the
+ * reference, whose kernels have no such checks. */
+int rg_device_status(void);
 
 /* ----------------------------------------------------------------------
  * Slant-stack projector family (square images).

@@ -57,6 +57,7 @@ _PI = ctypes.POINTER(RG_IMAGE)
 _SIGS = {
     "rg_last_error": ([], ctypes.c_char_p),
     "rg_version": ([], _c_int),
+    "rg_device_status": ([], _c_int),
     "rg_radon_slantstack_workspace": ([_IMG, _IMG], _size_t),
     "rg_radon_slantstack": ([_IMG, _IMG, _vp, _size_t, _vp], _c_int),
     "rg_radon_slantstack_noalloc": ([_IMG, _IMG, _vp], _c_int),

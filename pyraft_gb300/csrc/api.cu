@@ -132,6 +132,33 @@ static int current_device()
     return d;
 }
 
+// One device int per GPU that kernels with bounded waits or in-kernel
+// checks OR their error bits into (1: a window check failed and a strip was
+// skipped; 2: an mbarrier wait ran out).  Allocated with the first plan on
+// the device, so no allocation happens inside a stream capture.
+static std::mutex g_errw_mu;
+static std::map<int, int *> g_errw;
+
+int *device_error_word()
+{
+    const int d = current_device();
+    std::lock_guard<std::mutex> lock(g_errw_mu);
+    auto it = g_errw.find(d);
+    return it == g_errw.end() ? nullptr : it->second;
+}
+
+int ensure_device_error_word()
+{
+    const int d = current_device();
+    std::lock_guard<std::mutex> lock(g_errw_mu);
+    if (g_errw.count(d)) return RG_OK;
+    int *w = nullptr;
+    RG_CK(cudaMalloc(&w, sizeof(int)));
+    RG_CK(cudaMemset(w, 0, sizeof(int)));
+    g_errw[d] = w;
+    return RG_OK;
+}
+
 struct PlanHolder {
     SSPlan p;
     ~PlanHolder() { ss_plan_free(p); }
@@ -344,6 +371,18 @@ extern "C" {
 const char *rg_last_error(void) { return g_err.c_str(); }
 int rg_version(void) { return 100; }
 
+int rg_device_status(void)
+{
+    int *w = device_error_word();
+    if (!w) return 0;
+    int v = 0;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&v, w, sizeof v, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemset(w, 0, sizeof(int));
+    if (e != cudaSuccess) return cuda_error(e, "rg_device_status");
+    return v;
+}
+
 // ---------------------------------------------------------------- Radon
 size_t rg_radon_slantstack_workspace(rg_image phantom, rg_image radon)
 {
@@ -400,7 +439,7 @@ int rg_radon_slantstack_stack(rg_image phantom, long long phantom_stride, rg_ima
     Scratch s;
     if ((rc = scratch_begin(s, ws, wsb, rg_radon_slantstack_stack_workspace(phantom, radon, nstack), st)))
         return rc;
-    const long long zp = (long long)N * (N + 2);
+    const long long zp = (long long)N * pairs_pitch(N);
     float2 *prow = (float2 *)s.take(radon_pairs_bytes(N) * (size_t)nstack);
     float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N) * (size_t)nstack);
     const bool direct = is_view_major(radon);

@@ -40,7 +40,7 @@ __global__ __launch_bounds__(128) void k_radon_mesh(const float2 *__restrict__ p
     const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (k >= R) return;
     const MeshView v = mv[j];
-    const int pitch = N + 2;
+    const int pitch = pairs_pitch(N);
     const float2 *__restrict__ base =
         ((v.flags & kLinesAreRows) ? prow : pcol) + blockIdx.z * zp;
     const double u0d = __dadd_rn(__dmul_rn(t[k], v.c1), v.r0);
@@ -131,7 +131,7 @@ int rg_radon_slantstack_withmesh(rg_image phantom, long long phantom_stride, rg_
     if ((rc = scratch_begin(sc, ws, wsb, rg_radon_slantstack_withmesh_workspace(phantom, radon, nstack),
                             st)))
         return rc;
-    const long long zp = (long long)N * (N + 2);
+    const long long zp = (long long)N * pairs_pitch(N);
     float2 *prow = (float2 *)sc.take(radon_pairs_bytes(N) * (size_t)nstack);
     float2 *pcol = (float2 *)sc.take(radon_pairs_bytes(N) * (size_t)nstack);
     MeshView *dv = (MeshView *)sc.take(sizeof(MeshView) * A);

@@ -1,0 +1,476 @@
+// radon_tma.cu -- slant-stack Radon with TMA-staged line windows.
+//
+// Same operator as radon_tile (raft/raft_radon_slantstack.c:122-214; see
+// slantstack.cu): ray k of view j sums, over the lines i of the image, the
+// linear interpolation at u = r0 + k rk + i ri (Q32.32), read as one pair
+// (s - d, d) of the padded line-pair arrays.
+//
+// GB300 design.  A CTA owns 64 consecutive rays of a block of up to 16
+// adjacent views of one orientation (lines = image rows, or columns).  On
+// every image line those 64 x 16 sample positions fall inside one window of
+// at most BW consecutive entries: the rays of a view are ~1 entry apart and
+// adjacent views move the positions by a few entries.  The CTA walks the
+// lines in strips of 16; for each strip one elected thread issues a single
+// 3-D TMA load (cp.async.bulk.tensor) of the BW x 16 window box into shared
+// memory, double-buffered on two mbarriers, so the next strip streams in
+// while the current one is summed.  Entries outside the line-pair array
+// (left of entry 0, right of the pitch, past line N-1) are zero-filled by the
+// TMA unit, so the box needs no clamping.  Every (ray, view) then reads its
+// samples with LDS.64 at a Q9.23 local position (index = bits 23..31, weight
+// 1 + w from the low 23 bits); a thread carries one ray of four views.
+//
+// The host partitions the plan's views into blocks whose window provably
+// fits: positions are affine in (ray, line), so the window width over all
+// ray tiles and strips is largest at the corner tiles and strips, which are
+// checked exactly in integer arithmetic.  The kernel re-derives each strip's
+// window start from the same corner positions and checks the width again;
+// a strip that would not fit is skipped with an error flag, never read out
+// of bounds.  Every mbarrier wait is bounded; a CTA whose wait runs out sets
+// the error flag, waits (bounded) for its own copies and leaves.
+#include <cuda.h>
+#include <string.h>
+
+#include <climits>
+#include <mutex>
+#include <vector>
+
+#include "ss_tiles.cuh"
+
+namespace rg {
+
+constexpr int kTmRays = 64;     // rays per CTA (two warps of 32)
+constexpr int kTmViews = 16;    // views per block (max)
+constexpr int kTmVpt = 4;       // views per thread
+constexpr int kTmLines = 16;    // lines per strip
+constexpr int kTmWaitLimit = 1 << 24;                    // polls (backstop)
+constexpr unsigned long long kTmWaitNs = 200000000ull;    // 0.2 s per wait
+
+__device__ __forceinline__ unsigned smem_addr(const void *p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait on phase `parity` of an mbarrier for at most kTmWaitNs (strips
+// normally arrive within microseconds); false if the time ran out.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (int it = 0; it < kTmWaitLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 63) == 63 && global_ns() - t0 > kTmWaitNs) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *tm, int x, int y,
+                                            int z, unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+template <int OFF>
+__device__ __forceinline__ float2 lds_pair_at(unsigned addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];"
+                 : "=f"(v.x), "=f"(v.y)
+                 : "r"(addr), "n"(OFF));
+    return v;
+}
+
+// One full strip of a (ray, view): 16 lines, line r of the strip buffer at
+// byte offset r * BW * 8 (an immediate of the load).
+template <int BW, int R0>
+__device__ __forceinline__ void strip16(unsigned sb, unsigned &L, unsigned dq, float &part)
+{
+    if constexpr (R0 < kTmLines) {
+        const float2 pr = lds_pair_at<R0 * BW * 8>(sb + ((L >> 23) << 3));
+        part += fmaf(frac_plus_one(L), pr.y, pr.x);
+        L += dq;
+        strip16<BW, R0 + 1>(sb, L, dq, part);
+    }
+}
+
+template <int EPI, int BW>
+__global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CUtensorMap tm_rows,
+                                                   const __grid_constant__ CUtensorMap tm_cols,
+                                                   int N, const View *__restrict__ views,
+                                                   const StBlock *__restrict__ blocks, int R,
+                                                   float *__restrict__ out_am, int out_ld,
+                                                   const float *__restrict__ y_am, int y_ld,
+                                                   long long zo, int *__restrict__ err)
+{
+    extern __shared__ __align__(128) float2 sbuf[];   // [2][kTmLines][BW]
+    __shared__ __align__(8) unsigned long long full[2];
+    __shared__ int xs[2];                             // window start entry per buffer
+    __shared__ int bad[2];                            // window did not fit
+    __shared__ long long cr0[kTmViews], crk[kTmViews], cri[kTmViews];
+    __shared__ int s_lo, s_hi;
+
+    const StBlock blk = blocks[blockIdx.y];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int k0 = blockIdx.x * kTmRays;
+    const int k = k0 + (warp & 1) * 32 + lane;
+    const int vg = (warp >> 1) * kTmVpt;
+    const int z = blockIdx.z;
+    const CUtensorMap *tm = (blk.flags & kLinesAreRows) ? &tm_rows : &tm_cols;
+    out_am += (long long)z * zo;
+
+    long long u0[kTmVpt], q[kTmVpt];
+    int lo[kTmVpt], hi[kTmVpt];
+    int mylo = INT_MAX, myhi = INT_MIN;
+#pragma unroll
+    for (int v = 0; v < kTmVpt; ++v) {
+        lo[v] = 1;
+        hi[v] = 0;
+        u0[v] = 0;
+        q[v] = 0;
+        if (vg + v < blk.count && k < R) {
+            const View &V = views[blk.first + vg + v];
+            u0[v] = V.r0 + (long long)k * V.rk;
+            q[v] = V.ri;
+            radon_line_range(u0[v], q[v], N, lo[v], hi[v]);
+            if (lo[v] <= hi[v]) {
+                mylo = min(mylo, lo[v]);
+                myhi = max(myhi, hi[v]);
+            }
+        }
+    }
+    if (threadIdx.x < kTmViews && threadIdx.x < blk.count) {
+        const View &V = views[blk.first + threadIdx.x];
+        cr0[threadIdx.x] = V.r0;
+        crk[threadIdx.x] = V.rk;
+        cri[threadIdx.x] = V.ri;
+    }
+    if (threadIdx.x == 0) {
+        s_lo = INT_MAX;
+        s_hi = INT_MIN;
+        mbar_init(smem_addr(&full[0]), 1);
+        mbar_init(smem_addr(&full[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    mylo = __reduce_min_sync(0xffffffffu, mylo);
+    myhi = __reduce_max_sync(0xffffffffu, myhi);
+    if (lane == 0) {
+        atomicMin(&s_lo, mylo);
+        atomicMax(&s_hi, myhi);
+    }
+    __syncthreads();
+    const int Lo = s_lo, Hi = s_hi;
+
+    float acc[kTmVpt], comp[kTmVpt];
+#pragma unroll
+    for (int v = 0; v < kTmVpt; ++v) acc[v] = comp[v] = 0.f;
+
+    if (Lo <= Hi) {
+        const int sfirst = Lo / kTmLines;
+        const int nstrips = Hi / kTmLines - sfirst + 1;
+        const unsigned sbase = smem_addr(sbuf);
+        constexpr unsigned kBufBytes = kTmLines * BW * 8;
+
+        // Warp 0: window of strip n from the block's corner positions, then
+        // lane 0 arms the buffer's barrier and issues the TMA load.
+        auto issue = [&](int n) {
+            const int i0 = (sfirst + n) * kTmLines;
+            const int i1 = min(i0 + kTmLines - 1, N - 1);
+            const int c = lane >> 1;
+            int emin = INT_MAX, emax = INT_MIN;
+            if (c < blk.count) {
+                const int kk = (lane & 1) ? min(k0 + kTmRays - 1, R - 1) : k0;
+                const long long ua = cr0[c] + (long long)kk * crk[c] + (long long)i0 * cri[c];
+                const long long ub = ua + (long long)(i1 - i0) * cri[c];
+                const int ea = (int)(ua >> 32) + 1, eb = (int)(ub >> 32) + 1;
+                emin = min(ea, eb);
+                emax = max(ea, eb);
+            }
+            emin = __reduce_min_sync(0xffffffffu, emin);
+            emax = __reduce_max_sync(0xffffffffu, emax);
+            // one entry of slack on both sides for the Q9.23 stepping
+            const int x0 = (emin - 1) & ~1;
+            if (lane == 0) {
+                const int b = n & 1;
+                xs[b] = x0;
+                bad[b] = (emax + 1 - x0 >= BW) ? 1 : 0;
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_expect_tx(smem_addr(&full[b]), kBufBytes);
+                tma_load_3d(sbase + b * kBufBytes, tm, x0, i0, z, smem_addr(&full[b]));
+            }
+        };
+
+        if (warp == 0) issue(0);
+        int n = 0;
+        bool failed = false;
+        for (; n < nstrips; ++n) {
+            const int b = n & 1;
+            // buffer b ^ 1 was last read in strip n - 1, which every thread
+            // finished before the barrier that closed it
+            if (warp == 0 && n + 1 < nstrips) issue(n + 1);
+            const bool ok = mbar_wait(smem_addr(&full[b]), (n >> 1) & 1);
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            const int i0 = (sfirst + n) * kTmLines;
+            if (!bad[b]) {
+                const int x0 = xs[b];
+                const unsigned sb = sbase + b * kBufBytes;
+#pragma unroll
+                for (int v = 0; v < kTmVpt; ++v) {
+                    const int a = max(lo[v], i0), e = min(hi[v], i0 + kTmLines - 1);
+                    if (a > e) continue;
+                    const long long ua = u0[v] + (long long)a * q[v];
+                    unsigned L = (unsigned)((ua - ((long long)(x0 - 1) << 32)) >> 9);
+                    const unsigned dq = (unsigned)((q[v] + 256) >> 9);
+                    float part = 0.f;
+                    if (a == i0 && e == i0 + kTmLines - 1) {
+                        strip16<BW, 0>(sb, L, dq, part);
+                    } else {
+                        unsigned lb = sb + (unsigned)(a - i0) * (BW * 8);
+                        for (int i = a; i <= e; ++i) {
+                            const float2 pr = lds_pair_at<0>(lb + ((L >> 23) << 3));
+                            part += fmaf(frac_plus_one(L), pr.y, pr.x);
+                            L += dq;
+                            lb += BW * 8;
+                        }
+                    }
+                    kahan_add(acc[v], comp[v], part);
+                }
+            } else if (threadIdx.x == 0 && err) {
+                atomicOr(err, 1);
+            }
+            __syncthreads();
+        }
+        if (failed && threadIdx.x == 0) {
+            if (err) atomicOr(err, 2);
+            // copies still in flight: strip n (buffer n & 1) and, if issued,
+            // strip n + 1; wait for them (bounded) before leaving
+            mbar_wait(smem_addr(&full[n & 1]), (n >> 1) & 1);
+            if (n + 1 < nstrips) mbar_wait(smem_addr(&full[(n + 1) & 1]), ((n + 1) >> 1) & 1);
+        }
+    }
+
+#pragma unroll
+    for (int v = 0; v < kTmVpt; ++v) {
+        if (vg + v >= blk.count || k >= R) continue;
+        const View &V = views[blk.first + vg + v];
+        const float val = (acc[v] - comp[v]) * V.delta;
+        out_am[(size_t)V.view * out_ld + k] =
+            radon_epilogue(EPI, val, y_am, (size_t)V.view * y_ld + k);
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Host side.
+
+// Window width (entries, with the kernel's slack) of a growing block of
+// views, over the corner ray tiles and strips (positions are affine in
+// (ray, line), so the width over every tile and strip is largest there).
+struct BlockSpan {
+    long long emin[4], emax[4];
+    int k0[2], i0[2];
+    BlockSpan(int N, int R)
+    {
+        k0[0] = 0;
+        k0[1] = ((R - 1) / kTmRays) * kTmRays;
+        i0[0] = 0;
+        i0[1] = ((N - 1) / kTmLines) * kTmLines;
+        for (int c = 0; c < 4; ++c) { emin[c] = LLONG_MAX; emax[c] = LLONG_MIN; }
+    }
+    void add(const View &v, long long *mn, long long *mx) const
+    {
+        for (int c = 0; c < 4; ++c) {
+            mn[c] = emin[c];
+            mx[c] = emax[c];
+            const int ka = k0[c & 1], ia = i0[c >> 1];
+            for (int kk : {ka, ka + kTmRays - 1})
+                for (int ii : {ia, ia + kTmLines - 1}) {
+                    const long long u = v.r0 + (long long)kk * v.rk + (long long)ii * v.ri;
+                    const long long en = (u >> 32) + 1;
+                    mn[c] = std::min(mn[c], en);
+                    mx[c] = std::max(mx[c], en);
+                }
+        }
+    }
+    static long long width(const long long *mn, const long long *mx)
+    {
+        long long w = 0;
+        for (int c = 0; c < 4; ++c) w = std::max(w, mx[c] + 2 - ((mn[c] - 1) & ~1LL));
+        return w;
+    }
+};
+
+static bool radon_kernel_direct()
+{
+    const char *e = getenv("RG_RADON_KERNEL");
+    return e && !strcmp(e, "direct");
+}
+
+int st_blocks_build(SSPlan &p, const View *hv)
+{
+    p.nblocks = 0;
+    p.st_bw = 0;
+    const int N = p.g.N, R = p.g.R, nv = p.nv;
+    if (nv < 1) return RG_OK;
+    for (int bw : {128, 256}) {
+        std::vector<StBlock> bl;
+        bool fits = true;
+        for (int e = 0; e < nv && fits;) {
+            BlockSpan sp(N, R);
+            long long mn[4], mx[4];
+            sp.add(hv[e], mn, mx);
+            if (BlockSpan::width(mn, mx) > bw) { fits = false; break; }
+            memcpy(sp.emin, mn, sizeof mn);
+            memcpy(sp.emax, mx, sizeof mx);
+            int c = 1;
+            while (c < kTmViews && e + c < nv &&
+                   (hv[e + c].flags & kLinesAreRows) == (hv[e].flags & kLinesAreRows)) {
+                sp.add(hv[e + c], mn, mx);
+                if (BlockSpan::width(mn, mx) > bw) break;
+                memcpy(sp.emin, mn, sizeof mn);
+                memcpy(sp.emax, mx, sizeof mx);
+                ++c;
+            }
+            bl.push_back(StBlock{e, c, hv[e].flags & kLinesAreRows, 0});
+            e += c;
+        }
+        // worth it only when blocks share their windows among several views
+        if (!fits || (int)bl.size() > 65535 || nv < 6 * (int)bl.size()) continue;
+        if (bw == 128 && nv < 12 * (int)bl.size()) continue;   // 256 packs more views
+        RG_CK(cudaMalloc(&p.d_blocks, sizeof(StBlock) * bl.size()));
+        RG_CK(cudaMemcpy(p.d_blocks, bl.data(), sizeof(StBlock) * bl.size(),
+                         cudaMemcpyHostToDevice));
+        p.nblocks = (int)bl.size();
+        p.st_bw = bw;
+        return RG_OK;
+    }
+    return RG_OK;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)f;
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// 3-D map over nz stacked line-pair arrays: (entry, line, image), 8-byte
+// elements, box BW x kTmLines x 1, zero fill outside.
+static int encode_pairs_map(CUtensorMap *tm, const float2 *pairs, int N, int nz, long long zp,
+                            int bw)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return set_error(RG_ECUDA, "cuTensorMapEncodeTiled is not available");
+    const int pitch = pairs_pitch(N);
+    cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)N, (cuuint64_t)nz};
+    cuuint64_t strides[2] = {(cuuint64_t)pitch * 8,
+                             (cuuint64_t)(nz > 1 ? zp : (long long)N * pitch) * 8};
+    cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)kTmLines, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, (void *)pairs, dims, strides, box,
+                    estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+        return set_error(RG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return RG_OK;
+}
+
+bool radon_tma_usable(const SSPlan &p)
+{
+    return p.nblocks > 0 && p.d_blocks && !radon_kernel_direct();
+}
+
+template <int EPI, int BW>
+static int launch_tma_bw(const SSPlan &p, const CUtensorMap &tr, const CUtensorMap &tc,
+                         float *out_am, int out_ld, const float *y_am, int y_ld, int nz,
+                         long long zo, int *d_err, cudaStream_t st)
+{
+    const size_t smem = (size_t)2 * kTmLines * BW * 8;
+    auto k = k_radon_tma<EPI, BW>;
+    RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((p.g.R + kTmRays - 1) / kTmRays, p.nblocks, nz);
+    k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
+                               out_am, out_ld, y_am, y_ld, zo, d_err);
+    RG_CK_LAUNCH("k_radon_tma");
+    return RG_OK;
+}
+
+template <int EPI>
+static int launch_tma_epi(const SSPlan &p, const CUtensorMap &tr, const CUtensorMap &tc,
+                          float *out_am, int out_ld, const float *y_am, int y_ld, int nz,
+                          long long zo, int *d_err, cudaStream_t st)
+{
+    if (p.st_bw == 128)
+        return launch_tma_bw<EPI, 128>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo, d_err, st);
+    return launch_tma_bw<EPI, 256>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo, d_err, st);
+}
+
+int launch_radon_tma(const SSPlan &p, const float2 *prow, const float2 *pcol, float *out_am,
+                     int out_ld, const float *y_am, int y_ld, cudaStream_t st, int nz,
+                     long long zp, long long zo, int epi)
+{
+    CUtensorMap tr, tc;
+    int rc = encode_pairs_map(&tr, prow, p.g.N, nz, zp, p.st_bw);
+    if (!rc) rc = encode_pairs_map(&tc, pcol, p.g.N, nz, zp, p.st_bw);
+    if (rc) return rc;
+    int *d_err = device_error_word();
+    if (epi == kEpiRatio)
+        return launch_tma_epi<kEpiRatio>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo, d_err, st);
+    if (epi == kEpiTransmission)
+        return launch_tma_epi<kEpiTransmission>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo,
+                                                d_err, st);
+    return launch_tma_epi<kEpiSum>(p, tr, tc, out_am, out_ld, nullptr, 0, nz, zo, d_err, st);
+}
+
+}  // namespace rg

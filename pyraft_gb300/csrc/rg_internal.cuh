@@ -106,6 +106,16 @@ struct SSPlan {
     bool adj_ok = true;            // every |rk| >= 1 (two-tap adjoint)
     bool contiguous = true;        // views are consecutive (not an OSEM subset)
     int device = -1;
+    // TMA-staged Radon (radon_tma.cu): blocks of adjacent views whose line
+    // windows fit st_bw entries (nblocks == 0: the direct kernels are used)
+    void *d_blocks = nullptr;      // StBlock[nblocks], device
+    int nblocks = 0, st_bw = 0;
+};
+
+// A block of the TMA-staged Radon: views [first, first + count) of a plan,
+// all with the same line orientation.
+struct StBlock {
+    int first, count, flags, pad;
 };
 
 int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv);
@@ -117,6 +127,10 @@ void ss_plan_free(SSPlan &p);
 
 // Kernel launchers (slantstack.cu).  Images handed to the kernels are
 // strided views: element (row, col) at ptr[row*cs + col*ls].
+// Line pairs: N lines of pairs_pitch(N) float2 entries; entry 1 + n holds
+// the pair of sample n, entries 0, N and above N are zeros.  The pitch is
+// even, so every line starts on a 16-byte boundary (TMA rows).
+__host__ __device__ __forceinline__ int pairs_pitch(int N) { return (N + 3) & ~1; }
 size_t radon_pairs_bytes(int N);
 // nz > 1: a stack of nz images, consecutive ones zi floats apart, their
 // line pairs zp pairs apart.
@@ -131,6 +145,17 @@ constexpr int kEpiTransmissionId = 2;
 int launch_radon(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
                  float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,
                  int nz = 1, long long zp = 0, long long zo = 0, int epi = -1);
+// radon_tma.cu: view blocks of a plan (after its views are computed), and
+// the staged Radon over them (same arguments as launch_radon).
+int st_blocks_build(SSPlan &p, const View *hv);
+bool radon_tma_usable(const SSPlan &p);
+int launch_radon_tma(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
+                     float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,
+                     int nz, long long zp, long long zo, int epi);
+// Per-device error word of kernels with bounded waits (api.cu): nullptr
+// until ensure_device_error_word ran on the current device.
+int *device_error_word();
+int ensure_device_error_word();
 // Views per thread of the Radon for this plan: 2 when its views are
 // consecutive (the two share L1 lines), else 1.  RG_RADON_VIEWS=1|2 overrides.
 int radon_views_per_thread(const SSPlan &p);

@@ -147,6 +147,8 @@ int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
     if (nv > 0) {
         RG_CK(cudaMalloc(&p.d_views, sizeof(View) * nv));
         RG_CK(cudaMemcpy(p.d_views, hv.data(), sizeof(View) * nv, cudaMemcpyHostToDevice));
+        if ((rc = ensure_device_error_word())) return rc;
+        if ((rc = st_blocks_build(p, hv.data()))) return rc;
     }
     return RG_OK;
 }
@@ -155,13 +157,17 @@ void ss_plan_free(SSPlan &p)
 {
     if (p.d_views) cudaFree(p.d_views);
     p.d_views = nullptr;
+    if (p.d_blocks) cudaFree(p.d_blocks);
+    p.d_blocks = nullptr;
+    p.nblocks = 0;
 }
 
 // ============================================================================
-// Line pairs for the Radon.  pitch = N + 2: entry 0 and N+1 are zero pads,
-// entry 1 + n holds the pair of sample n.
+// Line pairs for the Radon.  pitch = pairs_pitch(N) (N + 2 rounded up to
+// even): entry 1 + n holds the pair of sample n, entry 0 and every entry
+// from N + 1 on are zero pads.
 
-size_t radon_pairs_bytes(int N) { return (size_t)N * (N + 2) * sizeof(float2); }
+size_t radon_pairs_bytes(int N) { return (size_t)N * pairs_pitch(N) * sizeof(float2); }
 
 // blockIdx.z selects one image of a stack (strides zi in floats, zp in pairs).
 __global__ __launch_bounds__(256) void k_line_pairs(const float *__restrict__ img, long long cs,
@@ -220,6 +226,8 @@ int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float 
 {
     if (p.nv == 0) return RG_OK;
     if (epi < 0) epi = y_am ? kEpiRatio : kEpiSum;
+    if (radon_tma_usable(p))
+        return launch_radon_tma(p, prow, pcol, out_am, out_ld, y_am, y_ld, st, nz, zp, zo, epi);
     const int N = p.g.N, R = p.g.R;
     if (radon_views_per_thread(p) == 2) {
         dim3 grid((R + 31) / 32, (p.nv + 7) / 8, nz);

@@ -27,7 +27,7 @@ __device__ __forceinline__ void line_pairs_tile(const float *__restrict__ img, l
 {
     __shared__ float t[33][33];
     const int r0 = by * 32, c0 = bx * 32;
-    const int pitch = N + 2;
+    const int pitch = pairs_pitch(N);
     for (int e = threadIdx.x; e < 33 * 33; e += 256) {
         int y = e / 33, x = e % 33;
         int r = r0 + y, c = c0 + x;
@@ -45,14 +45,17 @@ __device__ __forceinline__ void line_pairs_tile(const float *__restrict__ img, l
         if (r < N && c < N)
             pcol[(size_t)c * pitch + 1 + r] = make_pair(t[lane][x], t[lane + 1][x], r <= N - 2);
     }
-    // zero pads of the lines this tile starts / ends
+    // zero pads of the lines this tile starts / ends (entry 0 and entries
+    // N + 1 .. pitch - 1)
     if (c0 == 0 && threadIdx.x < 32 && r0 + lane < N) {
         prow[(size_t)(r0 + lane) * pitch] = make_float2(0.f, 0.f);
-        prow[(size_t)(r0 + lane) * pitch + N + 1] = make_float2(0.f, 0.f);
+        for (int e = N + 1; e < pitch; ++e)
+            prow[(size_t)(r0 + lane) * pitch + e] = make_float2(0.f, 0.f);
     }
     if (r0 == 0 && threadIdx.x < 32 && c0 + lane < N) {
         pcol[(size_t)(c0 + lane) * pitch] = make_float2(0.f, 0.f);
-        pcol[(size_t)(c0 + lane) * pitch + N + 1] = make_float2(0.f, 0.f);
+        for (int e = N + 1; e < pitch; ++e)
+            pcol[(size_t)(c0 + lane) * pitch + e] = make_float2(0.f, 0.f);
     }
     __syncthreads();   // t is reused by the next tile of a persistent CTA
 }
@@ -120,7 +123,7 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
     const int e = by * 4 + (threadIdx.x >> 5);
     if (e >= nv || k >= R) return;   // no barrier below: early exit is safe
     const View v = views[e];
-    const int pitch = N + 2;
+    const int pitch = pairs_pitch(N);
     const float2 *__restrict__ base = (v.flags & kLinesAreRows) ? prow : pcol;
 
     // Position on line 0 and per-line step, Q32.32.
@@ -174,7 +177,7 @@ __device__ __forceinline__ void radon_tile2(const float2 *__restrict__ prow,
     const bool two = e0 + 1 < nv;
     const View va = views[e0];
     const View vb = two ? views[e0 + 1] : va;
-    const unsigned pitch = (unsigned)(N + 2);
+    const unsigned pitch = (unsigned)pairs_pitch(N);
     const float2 *__restrict__ ba = (va.flags & kLinesAreRows) ? prow : pcol;
     const float2 *__restrict__ bb = (vb.flags & kLinesAreRows) ? prow : pcol;
     const long long ua0 = va.r0 + (long long)k * va.rk, ub0 = vb.r0 + (long long)k * vb.rk;
