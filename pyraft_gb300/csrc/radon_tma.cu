@@ -127,7 +127,14 @@ __device__ __forceinline__ void strip16(unsigned sb, unsigned &L, unsigned dq, f
     }
 }
 
-template <int EPI, int BW>
+// Lane layout: each shared load of a warp covers RPL consecutive rays of
+// 32 / RPL adjacent views.  Rays are >= 1 entry apart on a line while
+// adjacent views sit a few entries apart, so fewer rays per load (more
+// views) packs the 32 lanes' 8-byte reads into fewer shared-memory
+// wavefronts.  A thread carries 4 (ray, view) pairs m: the warp's 32 rays x
+// 4 views are covered as ray group m % (32 / RPL) and view group
+// m / (32 / RPL).
+template <int EPI, int BW, int RPL>
 __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CUtensorMap tm_rows,
                                                    const __grid_constant__ CUtensorMap tm_cols,
                                                    int N, const View *__restrict__ views,
@@ -146,8 +153,16 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
     const StBlock blk = blocks[blockIdx.y];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int k0 = blockIdx.x * kTmRays;
-    const int k = k0 + (warp & 1) * 32 + lane;
-    const int vg = (warp >> 1) * kTmVpt;
+    constexpr int kRG = 32 / RPL;
+    static_assert(RPL == 32 || RPL == 16 || RPL == 8, "rays per load");
+    // pair m: ray k0 + 32 (warp & 1) + RPL (m % kRG) + lane % RPL,
+    //         view (warp >> 1) * 4 + lane / RPL + (32 / RPL) (m / kRG)
+    int kk_[kTmVpt], vv_[kTmVpt];
+#pragma unroll
+    for (int m = 0; m < kTmVpt; ++m) {
+        kk_[m] = k0 + (warp & 1) * 32 + RPL * (m % kRG) + lane % RPL;
+        vv_[m] = (warp >> 1) * kTmVpt + lane / RPL + (32 / RPL) * (m / kRG);
+    }
     const int z = blockIdx.z;
     const CUtensorMap *tm = (blk.flags & kLinesAreRows) ? &tm_rows : &tm_cols;
     out_am += (long long)z * zo;
@@ -161,9 +176,9 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
         hi[v] = 0;
         u0[v] = 0;
         q[v] = 0;
-        if (vg + v < blk.count && k < R) {
-            const View &V = views[blk.first + vg + v];
-            u0[v] = V.r0 + (long long)k * V.rk;
+        if (vv_[v] < blk.count && kk_[v] < R) {
+            const View &V = views[blk.first + vv_[v]];
+            u0[v] = V.r0 + (long long)kk_[v] * V.rk;
             q[v] = V.ri;
             radon_line_range(u0[v], q[v], N, lo[v], hi[v]);
             if (lo[v] <= hi[v]) {
@@ -288,11 +303,11 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
 
 #pragma unroll
     for (int v = 0; v < kTmVpt; ++v) {
-        if (vg + v >= blk.count || k >= R) continue;
-        const View &V = views[blk.first + vg + v];
+        if (vv_[v] >= blk.count || kk_[v] >= R) continue;
+        const View &V = views[blk.first + vv_[v]];
         const float val = (acc[v] - comp[v]) * V.delta;
-        out_am[(size_t)V.view * out_ld + k] =
-            radon_epilogue(EPI, val, y_am, (size_t)V.view * y_ld + k);
+        out_am[(size_t)V.view * out_ld + kk_[v]] =
+            radon_epilogue(EPI, val, y_am, (size_t)V.view * y_ld + kk_[v]);
     }
 }
 
@@ -431,19 +446,39 @@ bool radon_tma_usable(const SSPlan &p)
     return p.nblocks > 0 && p.d_blocks && !radon_kernel_direct();
 }
 
-template <int EPI, int BW>
-static int launch_tma_bw(const SSPlan &p, const CUtensorMap &tr, const CUtensorMap &tc,
-                         float *out_am, int out_ld, const float *y_am, int y_ld, int nz,
-                         long long zo, int *d_err, cudaStream_t st)
+// Rays per shared load (lane layout); RG_RADON_RPL=32|16|8 overrides.
+static int radon_rpl()
+{
+    const char *e = getenv("RG_RADON_RPL");
+    const int v = e ? atoi(e) : 0;
+    return (v == 32 || v == 16 || v == 8) ? v : 8;
+}
+
+template <int EPI, int BW, int RPL>
+static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensorMap &tc,
+                          float *out_am, int out_ld, const float *y_am, int y_ld, int nz,
+                          long long zo, int *d_err, cudaStream_t st)
 {
     const size_t smem = (size_t)2 * kTmLines * BW * 8;
-    auto k = k_radon_tma<EPI, BW>;
+    auto k = k_radon_tma<EPI, BW, RPL>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((p.g.R + kTmRays - 1) / kTmRays, p.nblocks, nz);
     k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
                                out_am, out_ld, y_am, y_ld, zo, d_err);
     RG_CK_LAUNCH("k_radon_tma");
     return RG_OK;
+}
+
+template <int EPI, int BW>
+static int launch_tma_bw(const SSPlan &p, const CUtensorMap &tr, const CUtensorMap &tc,
+                         float *out_am, int out_ld, const float *y_am, int y_ld, int nz,
+                         long long zo, int *d_err, cudaStream_t st)
+{
+    switch (radon_rpl()) {
+    case 32: return launch_tma_rpl<EPI, BW, 32>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo, d_err, st);
+    case 16: return launch_tma_rpl<EPI, BW, 16>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo, d_err, st);
+    default: return launch_tma_rpl<EPI, BW, 8>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo, d_err, st);
+    }
 }
 
 template <int EPI>
