@@ -208,12 +208,15 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7):
         _native.check(L.rg_osem_batch(S, I, nslices, it, nsubsets, 1, ws.data_ptr(), wsb, sp))
     run_batch(1)                                     # warm-up (plans, graph path)
     torch.cuda.synchronize()
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    run_batch(niter)
-    b.record()
-    b.synchronize()
-    t_batch = a.elapsed_time(b) * 1e-3
+    times = []
+    for _ in range(3):                               # median of three full runs
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        run_batch(niter)
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b) * 1e-3)
+    t_batch = statistics.median(times)
     upd = sum(2.0 * n * n * v for n, v in sizes) * niter
     m = nslices if plain_slices is None else min(plain_slices, nslices)
     host = [s.cpu().numpy() for s in sinos[:m]]
@@ -267,14 +270,18 @@ def em_run(torch, rg, n=1024, nviews=720, seed=5):
         ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
         x.fill_(1.0)
         _native.check(L.rg_em(S, X, _native.RG_SLANTSTACK, 1, subsets, ws.data_ptr(), wsb, sp))
-        x.fill_(1.0)
-        torch.cuda.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record()
-        _native.check(L.rg_em(S, X, _native.RG_SLANTSTACK, it, subsets, ws.data_ptr(), wsb, sp))
-        b.record()
-        b.synchronize()
-        t = a.elapsed_time(b) * 1e-3
+        ts = []
+        for _ in range(3):                           # median of three full runs
+            x.fill_(1.0)
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            _native.check(L.rg_em(S, X, _native.RG_SLANTSTACK, it, subsets, ws.data_ptr(), wsb,
+                                  sp))
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b) * 1e-3)
+        t = statistics.median(ts)
         upd = 2.0 * n * n * nviews * it
         out[name] = {"seconds": round(t, 4), "slices_per_s": round(1.0 / t, 3),
                      "gups": round(upd / t / 1e9, 1)}

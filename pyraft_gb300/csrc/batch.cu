@@ -92,7 +92,7 @@ __global__ __launch_bounds__(128) void k_batch_radon(const BatchSlice *__restric
         const BatchSlice &b = d[find_slice(d, n, item, kRadon)];
         const int local = item - b.begin[kRadon], rb = (b.R + 31) / 32;
         if (VPT == 2)
-            radon_tile2<kEpiRatio>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
+            radon_tile2<kEpiRatio, 16>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
                               b.R, local % rb, local / rb);
         else
             radon_tile<kEpiRatio>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
@@ -413,7 +413,10 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
     BatchRun br;
     br.n = nslices;
     br.S = S;
-    br.vpt = radon_views_per_thread(*plans[0]);
+    // two views per thread with a 16-deep unroll: the batch has parallelism
+    // to spare, so more loads in flight per thread beat occupancy
+    // (RG_RADON_VIEWS=1|2 overrides)
+    br.vpt = getenv("RG_RADON_VIEWS") ? radon_views_per_thread(*plans[0]) : 2;
     const int vpb = br.vpt == 2 ? 8 : 4;   // views per Radon item
     br.wmax = wneed <= 64 ? 64 : wneed <= 128 ? 128 : wneed <= 256 ? 256 : 512;
     if (wneed > 512) return set_error(RG_EUNSUPPORTED, "gather window of %d exceeds 512", wneed);

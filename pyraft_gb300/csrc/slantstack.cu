@@ -195,10 +195,85 @@ __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                const View *__restrict__ views, int nv, int R,
                                                float *__restrict__ out_am, int out_ld,
                                                const float *__restrict__ y_am, int y_ld,
-                                               long long zp, long long zo)
+                                               long long zp, long long zo, int split)
 {
     radon_tile<EPI>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
-                      out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x, blockIdx.y);
+                    out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x / split, blockIdx.y,
+                    split, blockIdx.x % split);
+}
+
+// Line split of the direct Radon (clusters of `split` CTAs, see radon_tile):
+// the largest of 1, 2, 4 that keeps the grid within two waves of resident
+// CTAs, so launches smaller than the GPU get more CTAs in flight.  The
+// per-SM occupancy is cached per kernel and device (queried outside stream
+// captures; an uncached query during a capture gives 1).
+// RG_RADON_SPLIT=1|2|4 forces a choice.
+static std::mutex g_rocc_mu;
+static std::map<std::pair<const void *, int>, int> g_rocc;
+
+template <typename K>
+static int radon_split(K k, long long ctas, cudaStream_t st)
+{
+    if (const char *e = getenv("RG_RADON_SPLIT")) {
+        const int v = atoi(e);
+        if (v == 1 || v == 2 || v == 4) return v;
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    const auto key = std::make_pair((const void *)k, dev);
+    int cap = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_rocc_mu);
+        auto it = g_rocc.find(key);
+        if (it != g_rocc.end()) cap = it->second;
+    }
+    if (!cap) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+            return 1;
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, 0) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 1;
+        cap = per_sm * sms;
+        std::lock_guard<std::mutex> lock(g_rocc_mu);
+        g_rocc[key] = cap;
+    }
+    int s = 1;
+    while (s < 4 && ctas * 2 * s <= 2 * cap) s *= 2;   // up to two waves
+    return s;
+}
+
+template <int EPI>
+static int launch_radon_direct1(const SSPlan &p, const float2 *prow, const float2 *pcol,
+                                float *out_am, int out_ld, const float *y_am, int y_ld,
+                                cudaStream_t st, int nz, long long zp, long long zo)
+{
+    const int N = p.g.N, R = p.g.R;
+    dim3 grid((R + 31) / 32, (p.nv + 3) / 4, nz);
+    auto k = k_radon<EPI>;
+    const int split = radon_split(k, (long long)grid.x * grid.y * grid.z, st);
+    if (split == 1) {
+        k<<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am, out_ld, y_am, y_ld,
+                                zp, zo, 1);
+        RG_CK_LAUNCH("k_radon");
+        return RG_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
+    cfg.blockDim = dim3(128);
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RG_CK(cudaLaunchKernelEx(&cfg, k, prow, pcol, N, (const View *)p.d_views, p.nv, R, out_am,
+                             out_ld, y_am, y_ld, zp, zo, split));
+    RG_CK_LAUNCH("k_radon (cluster)");
+    return RG_OK;
 }
 
 template <int EPI>
@@ -243,18 +318,14 @@ int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float 
         RG_CK_LAUNCH("k_radon2");
         return RG_OK;
     }
-    dim3 grid((R + 31) / 32, (p.nv + 3) / 4, nz);
     if (epi == kEpiRatio)
-        k_radon<kEpiRatio><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
-                                                 out_ld, y_am, y_ld, zp, zo);
-    else if (epi == kEpiTransmission)
-        k_radon<kEpiTransmission><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
-                                                        out_ld, y_am, y_ld, zp, zo);
-    else
-        k_radon<kEpiSum><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am, out_ld,
-                                               nullptr, 0, zp, zo);
-    RG_CK_LAUNCH("k_radon");
-    return RG_OK;
+        return launch_radon_direct1<kEpiRatio>(p, prow, pcol, out_am, out_ld, y_am, y_ld, st, nz,
+                                               zp, zo);
+    if (epi == kEpiTransmission)
+        return launch_radon_direct1<kEpiTransmission>(p, prow, pcol, out_am, out_ld, y_am, y_ld,
+                                                      st, nz, zp, zo);
+    return launch_radon_direct1<kEpiSum>(p, prow, pcol, out_am, out_ld, nullptr, 0, st, nz, zp,
+                                         zo);
 }
 
 template <int MODE, int WMAX, int ROWS, bool EM>

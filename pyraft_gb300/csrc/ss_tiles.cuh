@@ -110,19 +110,33 @@ __device__ __forceinline__ float radon_epilogue(int epi, float val, const float 
     return val;
 }
 
+// UNROLL of the direct Radon walks: the walks are bound by load latency
+// (line pairs from L1, L2 or, for batches larger than L2, DRAM), and a
+// deeper unroll keeps more independent loads in flight per thread at the
+// cost of registers.  Measured on GB300: 8 for one-view walks over few
+// CTAs (OSEM subsets of one slice), 16 for two-view walks of the batched
+// OSEM.
 // One CTA (128 threads) = rays [32 bx, 32 bx + 32) of views [4 by, 4 by + 4).
-template <int EPI>
+//
+// split > 1: the CTA is rank `rank` of a thread-block cluster of `split`
+// CTAs along x that share the rays and views; it walks lines
+// [rank N / split, (rank + 1) N / split) only, and rank 0 adds the partial
+// sums (in rank order, from distributed shared memory) and writes the
+// epilogue.  Splitting the lines multiplies the CTA count of launches too
+// small to fill the GPU (one slice's OSEM subset).
+template <int EPI, int UNROLL = 8>
 __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
                                            const float2 *__restrict__ pcol, int N,
                                            const View *__restrict__ views, int nv, int R,
                                            float *__restrict__ out_am, int out_ld,
                                            const float *__restrict__ y_am, int y_ld, int bx,
-                                           int by)
+                                           int by, int split = 1, int rank = 0)
 {
     const int k = bx * 32 + (threadIdx.x & 31);
     const int e = by * 4 + (threadIdx.x >> 5);
-    if (e >= nv || k >= R) return;   // no barrier below: early exit is safe
-    const View v = views[e];
+    const bool active = e < nv && k < R;
+    if (!active && split == 1) return;   // no barrier below: early exit is safe
+    const View v = views[active ? e : 0];
     const int pitch = pairs_pitch(N);
     const float2 *__restrict__ base = (v.flags & kLinesAreRows) ? prow : pcol;
 
@@ -131,6 +145,11 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
     const long long q = v.ri;
     int lo, hi;
     radon_line_range(u0, q, N, lo, hi);
+    if (split > 1) {
+        lo = max(lo, (int)((long long)N * rank / split));
+        hi = min(hi, (int)((long long)N * (rank + 1) / split) - 1);
+        if (!active) { lo = 1; hi = 0; }
+    }
     float acc = 0.f, comp = 0.f;
     if (lo <= hi) {
         long long u = u0 + (long long)lo * q;
@@ -139,7 +158,7 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
         while (i <= hi) {
             const int iend = min(hi, i + 31);
             float part = 0.f;
-#pragma unroll 4
+#pragma unroll UNROLL
             for (; i <= iend; ++i) {
                 const int n = (int)(u >> 32);
                 const float w1 = __uint_as_float(((unsigned)u >> 9) | 0x3F800000u);
@@ -150,6 +169,22 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
             }
             kahan_add(acc, comp, part);
         }
+    }
+    if (split > 1) {
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        __shared__ float red[128];
+        red[threadIdx.x] = acc - comp;
+        cl.sync();
+        if (rank == 0 && active) {
+            float sum = 0.f;
+            for (int src = 0; src < split; ++src)
+                sum += cl.map_shared_rank(red, src)[threadIdx.x];
+            out_am[(size_t)v.view * out_ld + k] =
+                radon_epilogue(EPI, sum * v.delta, y_am, (size_t)v.view * y_ld + k);
+        }
+        cl.sync();    // no CTA leaves while rank 0 still reads its partials
+        return;
     }
     const float val = (acc - comp) * v.delta;
     out_am[(size_t)v.view * out_ld + k] = radon_epilogue(EPI, val, y_am, (size_t)v.view * y_ld + k);
@@ -163,7 +198,7 @@ __device__ __forceinline__ void radon_tile(const float2 *__restrict__ prow,
 // of both views' line ranges; a sample index outside a view's own range is
 // clamped (one unsigned min) onto the line's zero pad at N+1, so it adds 0
 // and never leaves the padded line.
-template <int EPI>
+template <int EPI, int UNROLL = 4>
 __device__ __forceinline__ void radon_tile2(const float2 *__restrict__ prow,
                                             const float2 *__restrict__ pcol, int N,
                                             const View *__restrict__ views, int nv, int R,
@@ -194,7 +229,7 @@ __device__ __forceinline__ void radon_tile2(const float2 *__restrict__ prow,
         while (i <= hi) {
             const int iend = min(hi, i + 31);
             float pa = 0.f, pb = 0.f;
-#pragma unroll 4
+#pragma unroll UNROLL
             for (; i <= iend; ++i) {
                 const unsigned ia = min((unsigned)((int)(ua >> 32) + 1), pad);
                 const unsigned ib = min((unsigned)((int)(ub >> 32) + 1), pad);

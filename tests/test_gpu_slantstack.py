@@ -278,3 +278,24 @@ def test_radon_tma_odd_corners_stack_and_em(orc, golden):
         ref = orc.radon_slantstack(xs[i].double().cpu().numpy(), 96, 120)
         assert rel(ys[i].double().cpu().numpy(), ref) <= 1e-5
     assert _native.load().rg_device_status() == 0
+
+
+@pytest.mark.parametrize("split", [2, 4])
+def test_direct_radon_cluster_line_split(orc, monkeypatch, split):
+    """The direct Radon with its lines split over a thread-block cluster
+    (partials added in distributed shared memory by rank 0), forced on a
+    plain geometry and inside OSEM (ratio epilogue, interleaved subsets)."""
+    monkeypatch.setenv("RG_RADON_KERNEL", "direct")
+    monkeypatch.setenv("RG_RADON_VIEWS", "1")
+    monkeypatch.setenv("RG_RADON_SPLIT", str(split))
+    rng = np.random.default_rng(70 + split)
+    n, r, a = 150, 150, 70
+    x = interior_image(rng, n)
+    out = np.asarray(rg.radon(rg.image(x), (r, a), SLANT))
+    assert rel(out, orc.radon_slantstack(x, r, a)) <= 1e-5
+    y = orc.radon_slantstack(x + 0.1, r, a)
+    got = np.asarray(rg.osem(sino_img(y), (n, n), 3, 5))
+    monkeypatch.setenv("RG_RADON_SPLIT", "1")
+    one = np.asarray(rg.osem(sino_img(y), (n, n), 3, 5))
+    assert rel(got, one) <= 1e-5
+    assert _native.load().rg_device_status() == 0
