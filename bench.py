@@ -134,14 +134,16 @@ def cpu_fbp_sample(sino_np, kind_ref):
     dt = 2.0 / (R - 1)
     t0 = time.perf_counter()
     O.ramlak_views(np.ascontiguousarray(sino_np.T), dt, views, threads=cores)
-    t_filter = (time.perf_counter() - t0) * (A / views)
+    s_filter = time.perf_counter() - t0
     t0 = time.perf_counter()
     O.backprojection_rows(sino_np, N, N // 2 - rows // 2, N // 2 + rows // 2, threads=cores)
-    t_bp = (time.perf_counter() - t0) * (N / rows)
+    s_bp = time.perf_counter() - t0
+    cpu_fbp_sample.last_sample_s = s_filter + s_bp
     sample = (f"FP64 oracle port of raft_backprojection_slantstack on {rows} of {N} image "
               f"rows and the Ram-Lak convolution on {views} of {A} views, each scaled to the "
-              f"full 2048^2 x 1800 step")
-    return t_filter + t_bp, sample, cores, "port"
+              f"full 2048^2 x 1800 step (the sample itself runs "
+              f"{1e3 * (s_filter + s_bp):.0f} ms; ms_per_step is the scaled full step)")
+    return s_filter * (A / views) + s_bp * (N / rows), sample, cores, "port"
 
 
 # ----------------------------------------------------------------------------
@@ -557,11 +559,12 @@ def reference_arm(args, rank, world, warm):
     from oracle import oracle as O
     rng = np.random.default_rng(1234)
     sino = rng.random((R, A))
-    steps = []
+    steps, samples = [], []
     for k in range(warm + args.steps):
         t, sample, cores, kind = cpu_fbp_sample(sino, True)
         if k >= warm:
             steps.append(t)
+            samples.append(cpu_fbp_sample.last_sample_s)
     t = statistics.mean(steps)
     v = UPDATES / t / 1e9
     print(json.dumps({
@@ -572,7 +575,8 @@ def reference_arm(args, rank, world, warm):
         "config": {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
                                "slant-stack backprojection", "image": N, "views": A, "rays": R},
         "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": sample},
+                         "sample": sample,
+                         "measured_sample_ms_per_step": round(1e3 * statistics.mean(samples), 1)},
         "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }), flush=True)

@@ -18,21 +18,26 @@
 //    hat(x) = max(0, 1-|x|) and the same [0, N-2] floor validity.
 //
 // GB300 design:
-//  * Radon is ray-driven: a warp owns 32 consecutive rays of one view and a
-//    CTA four adjacent views, so at every line the four warps read
-//    overlapping windows of the same image line (L1 reuse).  The image is
-//    pre-packed once per call into "line pairs" (s - d, d) with
-//    d = s[n+1] - s[n] and (0, 0) at n = N-1 and in one pad entry at each
-//    end, for both orientations (rows and columns).  One 8-byte load then
-//    yields a sample: value = (s - d) + (1 + w) d, and invalid samples read
-//    zeros, so the loop has no validity branch.  Ray sums accumulate in FP32
-//    in blocks of 32 samples, compensated (Kahan) across blocks.
-//  * Backprojection and adjoint are pixel-driven gathers over a 32 x 32
-//    pixel tile per CTA (256 threads, 4 rows each).  Views are processed in
-//    chunks of 32: for each view the tile needs a window of < W consecutive
-//    sinogram samples, which is staged into shared memory as 8-byte pairs;
-//    the inner loop is then one LDS.64 + two FP32 ops per (pixel, view) for
-//    the backprojection, plus the two hat weights for the adjoint.
+//  * Radon is ray-driven over "line pairs": the image is pre-packed once per
+//    call into (s - d, d) with d = s[n+1] - s[n], (0, 0) at n = N-1 and in
+//    the pad entries, for both orientations (rows and columns).  One 8-byte
+//    load then yields a sample, value = (s - d) + (1 + w) d, and invalid
+//    samples read zeros, so the walks have no validity branch.  Ray sums
+//    accumulate in FP32 in blocks of samples, compensated (Kahan) across
+//    blocks.  Plans whose views come in runs of adjacent views use the
+//    TMA-staged kernel of radon_tma.cu; the direct kernels here walk the
+//    line pairs from L1/L2: a warp owns 32 consecutive rays of one view (a
+//    CTA four views, or eight with two views per thread), and launches too
+//    small for the GPU split their lines over a thread-block cluster.
+//  * Backprojection and adjoint are pixel-driven gathers over tiles of 32
+//    columns x 8 ROWS rows per CTA (256 threads, ROWS rows per thread, ROWS
+//    autotuned over 4, 8 and 16).  Views are processed in chunks of 32: for
+//    each view the tile needs a window of < W consecutive sinogram samples,
+//    which is staged into shared memory as 8-byte pairs; the inner loop is
+//    then one LDS.64 + two FP32 ops per (pixel, view) for the
+//    backprojection, plus the two hat weights for the adjoint.  Grids of
+//    few tiles split each tile's views over a thread-block cluster and add
+//    the partials in distributed shared memory.
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
