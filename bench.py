@@ -164,63 +164,86 @@ def make_sinogram(torch, rg, seed):
     return s.contiguous()
 
 
-def make_osem_batch(torch, rg, nslices, seed):
-    """Config-5 style batch: N uniform over {256, 512, 1024, 2048}, views
-    uniform in [180, 1800], rays = N, random-ellipse emission phantoms,
-    Poisson counts with mean 50 per bin.  Returns (sinos, sizes) on the GPU
-    (sinograms as (rays, views) tensors)."""
+def osem_batch_sizes(nslices, seed):
+    """(N, views) of every slice of the config-5 batch: N uniform over
+    {256, 512, 1024, 2048}, views uniform in [180, 1800], rays = N."""
     import numpy as np
     rng = np.random.default_rng(seed)
-    sinos, sizes = [], []
-    gen = torch.Generator(device="cuda")
-    gen.manual_seed(seed)
-    for k in range(nslices):
-        n = int(rng.choice([256, 512, 1024, 2048]))
-        a = int(rng.integers(180, 1801))
+    return [(int(rng.choice([256, 512, 1024, 2048])), int(rng.integers(180, 1801)))
+            for _ in range(nslices)]
+
+
+def make_osem_batch(torch, rg, idx, sizes, seed):
+    """Sinograms of slices `idx` of the config-5 batch: random-ellipse
+    emission phantoms, Poisson counts with mean 50 per bin.  Each slice draws
+    from its own seeded generators, so a slice is the same whichever rank
+    builds it.  Returns (rays, views) GPU tensors."""
+    import numpy as np
+    sinos = []
+    for i in idx:
+        n, a = sizes[i]
+        rng = np.random.default_rng([seed, i])
         desc = rg.random_ellipses(12, rng)
         ph = rg.phantom_fromdesc((n, n), desc, device=True)
         ph = rg.gpu_image(torch.flip(ph.data, dims=[0]).abs().contiguous())
         p = rg.radon(ph, (n, a), rg.radon_method.SLANTSTACK).data
         lam = p.clamp(min=0) * (50.0 / max(float(p.mean()), 1e-9))
+        gen = torch.Generator(device="cuda")
+        gen.manual_seed(seed * 1000003 + i)
         sinos.append(torch.poisson(lam, generator=gen).contiguous())
-        sizes.append((n, a))
-    return sinos, sizes
+    return sinos
 
 
-def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7):
+def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7, rank=0, world=1):
     """Batched graph-captured OSEM vs the plain one-slice-per-call form on
-    the same slices.  The plain form is timed on the first `plain_slices`
-    slices (all, if None) and reported per slice."""
+    the same slices.  With several ranks (one per GPU) the slices are
+    partitioned by cost (pyraft_gb300.shard) and the batched time is the max
+    over ranks; the plain form runs on rank 0 only, on its first
+    `plain_slices` slices (all, if None), and is reported per slice."""
     import numpy as np
-    from pyraft_gb300 import _native
-    from pyraft_gb300.raftypes import rg_image, workspace
+    from pyraft_gb300 import _native, shard
+    from pyraft_gb300.raftypes import rg_image
     L = _native.load()
-    sinos, sizes = make_osem_batch(torch, rg, nslices, seed)
-    S = (_native.RG_IMAGE * nslices)(*[rg_image(rg.gpu_image(s, (0.0, 1.0), (math.pi, -1.0)))
-                                        for s in sinos])
+    sizes_all = osem_batch_sizes(nslices, seed)
+    mine = shard.rank_slices([n * n * a for n, a in sizes_all], rank, world)
+    sizes = [sizes_all[i] for i in mine]
+    sinos = make_osem_batch(torch, rg, mine, sizes_all, seed)
+    ns = len(mine)
+    S = (_native.RG_IMAGE * ns)(*[rg_image(rg.gpu_image(s, (0.0, 1.0), (math.pi, -1.0)))
+                                  for s in sinos])
     xs = [torch.ones((n, n), dtype=torch.float32, device="cuda") for n, _ in sizes]
-    I = (_native.RG_IMAGE * nslices)(*[rg_image(rg.gpu_image(x)) for x in xs])
-    wsb = L.rg_osem_batch_workspace(S, I, nslices, nsubsets)
+    I = (_native.RG_IMAGE * ns)(*[rg_image(rg.gpu_image(x)) for x in xs])
+    wsb = L.rg_osem_batch_workspace(S, I, ns, nsubsets)
     ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
     sp = torch.cuda.current_stream().cuda_stream
 
     def run_batch(it):
         for x in xs:
             x.fill_(1.0)
-        _native.check(L.rg_osem_batch(S, I, nslices, it, nsubsets, 1, ws.data_ptr(), wsb, sp))
+        _native.check(L.rg_osem_batch(S, I, ns, it, nsubsets, 1, ws.data_ptr(), wsb, sp))
     run_batch(1)                                     # warm-up (plans, graph path)
     torch.cuda.synchronize()
     times = []
     for _ in range(3):                               # median of three full runs
+        if world > 1:
+            torch.distributed.barrier()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record()
         run_batch(niter)
         b.record()
         b.synchronize()
-        times.append(a.elapsed_time(b) * 1e-3)
+        times.append(shard.max_over_ranks(a.elapsed_time(b) * 1e-3, device="cuda"))
     t_batch = statistics.median(times)
-    upd = sum(2.0 * n * n * v for n, v in sizes) * niter
-    m = nslices if plain_slices is None else min(plain_slices, nslices)
+    upd = sum(2.0 * n * n * v for n, v in sizes_all) * niter
+    res = {
+        "slices": nslices, "iterations": niter, "subsets": nsubsets, "n_gpus": world,
+        "batched_slices_per_s": round(nslices / t_batch, 3),
+        "batched_s": round(t_batch, 3),
+        "batched_gups": round(upd / t_batch / 1e9, 1),
+    }
+    if rank != 0:
+        return res
+    m = ns if plain_slices is None else min(plain_slices, ns)
     host = [s.cpu().numpy() for s in sinos[:m]]
     out = np.zeros((2048, 2048), dtype=np.float32)
     t0 = time.perf_counter()
@@ -230,20 +253,17 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7):
                                          nsubsets))
     t_plain = time.perf_counter() - t0
     frac = sum(sizes[k][0] ** 2 * sizes[k][1] for k in range(m)) / \
-        sum(n * n * v for n, v in sizes)
-    t_plain_all = t_plain / frac if m < nslices else t_plain
-    return {
-        "slices": nslices, "iterations": niter, "subsets": nsubsets,
-        "batched_slices_per_s": round(nslices / t_batch, 3),
-        "batched_s": round(t_batch, 3),
-        "batched_gups": round(upd / t_batch / 1e9, 1),
+        sum(n * n * v for n, v in sizes_all)
+    t_plain_all = t_plain / frac
+    res.update({
         "plain_slices_per_s": round(nslices / t_plain_all, 3),
         "plain_s": round(t_plain_all, 3),
         "plain_timed_slices": m,
-        "plain_note": ("all slices timed" if m == nslices else
-                       f"first {m} slices timed, scaled by their share of N^2*views"),
-        "speedup": round(t_plain_all / t_batch, 2),
-    }
+        "plain_note": (f"one GPU, first {m} slices of rank 0 timed, scaled by their share of "
+                       f"N^2*views of the whole batch"),
+        "speedup_per_gpu": round(t_plain_all / t_batch / world, 2),
+    })
+    return res
 
 
 def em_run(torch, rg, n=1024, nviews=720, seed=5):
@@ -358,8 +378,16 @@ def main():
         import torch
         import pyraft_gb300 as rg
         torch.cuda.set_device(local)
-        res = osem_compare(torch, rg, args.slices, args.iters, 10, args.plain_slices)
-        print(json.dumps({"workload": "batched uneven OSEM vs plain per-call form", **res}))
+        if world > 1:
+            torch.distributed.init_process_group("nccl")
+        res = osem_compare(torch, rg, args.slices, args.iters, 10, args.plain_slices,
+                           rank=rank, world=world)
+        if rank == 0:
+            print(json.dumps({"workload": "batched uneven OSEM vs plain per-call form",
+                              "scaling": "strong (slices partitioned over GPUs by cost)",
+                              **res}))
+        if world > 1:
+            torch.distributed.destroy_process_group()
         return
 
     import numpy as np
