@@ -63,6 +63,10 @@ typedef struct {
 /* Method ids, as raft/raft_enums.h:4-9 and pyraft/sinogram/sino.py:159-167. */
 #define RG_BRESENHAM  1
 #define RG_SLANTSTACK 2
+/* EM only: slant-stack Radon with the slant-stack BACKPROJECTION as the EM
+ * backprojector (x <- x * B(y / Ax) / B1), the operator pair of
+ * raft_em_gpu (raft/raft_em_gpu.cu:20-87); not a transpose pair. */
+#define RG_SLANTSTACK_BP 3
 
 /* Text of the last error on this thread ("" if none). */
 const char *rg_last_error(void);
@@ -224,7 +228,9 @@ int rg_fbp(rg_image sino, rg_image image, int kind,
  * pyraft/raftypes.py:211) and pyraft's make_em/em
  * (pyraft/iterative/em.py:109-169).  image holds x0 on entry and the
  * iterate on return.  method RG_SLANTSTACK uses the slant-stack Radon with
- * its matched adjoint; RG_BRESENHAM the DDA pair, as pyraft's em().
+ * its matched adjoint (true MLEM); RG_SLANTSTACK_BP the slant-stack Radon
+ * with the slant-stack backprojection, as raft_em_gpu pairs them;
+ * RG_BRESENHAM the DDA pair, as pyraft's em().
  * nsubsets == 1 is plain EM; > 1 is OSEM over interleaved view subsets
  * (subset s = views s, s+S, s+2S, ...).  Guards: y/0 -> 0, and pixels with
  * zero sensitivity are set to 0 (the reference divides by zero).
@@ -288,7 +294,9 @@ int rg_radon_fromdesc(rg_image sino, const double *desc, int n, void *stream);
  * on [0, pi) and rays on [-1, 1]; allocate, copy, run, copy back, free.
  * Unlike the reference they return a status and do not reset the device.
  * The backprojection wrapper computes the C slant-stack backprojection
- * (not the reference GPU kernel's nearest-sample, x-flipped variant).       */
+ * (not the reference GPU kernel's nearest-sample, x-flipped variant); the
+ * EM wrapper pairs the slant-stack Radon with it (RG_SLANTSTACK_BP), as
+ * raft_em_gpu pairs its Radon with its backprojection.                     */
 int rg_radon_slantstack_host(float *h_output, const float *h_input,
                              int size_image, int nrays, int nangles);
 int rg_backprojection_slantstack_host(float *h_image, const float *h_sino,

@@ -17,6 +17,7 @@ HEADER = os.path.join(os.path.dirname(HERE), "include", "raftgb.h")
 RG_OK = 0
 RG_BRESENHAM = 1
 RG_SLANTSTACK = 2
+RG_SLANTSTACK_BP = 3
 RG_FILTER_RAMLAK = 1
 RG_FILTER_LOWPASS = 2
 

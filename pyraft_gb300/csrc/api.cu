@@ -987,7 +987,7 @@ static int host_call(int op, float *h_out, const float *h_in, int size, int nray
         if (!rc && op == 1) rc = rg_backprojection_slantstack(sino, img, nullptr, 0, nullptr);
         if (!rc && op == 2) {
             rc = launch_fill(di, (size_t)size * size, 1.f, nullptr);
-            if (!rc) rc = rg_em(sino, img, RG_SLANTSTACK, niter, 1, nullptr, 0, nullptr);
+            if (!rc) rc = rg_em(sino, img, RG_SLANTSTACK_BP, niter, 1, nullptr, 0, nullptr);
         }
         if (!rc && (e = cudaMemcpy(h_out, di, ni, cudaMemcpyDeviceToHost)) != cudaSuccess)
             rc = cuda_error(e, "download");

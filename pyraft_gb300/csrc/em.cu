@@ -52,8 +52,12 @@ size_t em_dda_ws(int L, int C, int R, int A, int S)
 // Runs EM on one slice whose buffers are already laid out internally:
 // y_am (A x R view-major), x (N x N contiguous).  Scratch `s` must have room
 // for ratio, pairs and sensitivities (em_ss_ws minus y and x).
+// bp: the slant-stack backprojection is the backprojector (RG_SLANTSTACK_BP,
+// raft_em_gpu's pairing) instead of the matched adjoint; its sensitivity
+// B 1 is the FP32-compensated backprojection of ones (the dth scale of B
+// cancels between B r and B 1).
 static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, float *x,
-                      Scratch &s, cudaStream_t st)
+                      Scratch &s, cudaStream_t st, bool bp = false)
 {
     const int N = g.N, R = g.R, A = g.A;
     Holders hold;
@@ -63,7 +67,7 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
         int rc = get_ss_plan(g, S, k, &plans[k], &h);
         if (rc) return rc;
         hold.h.push_back(h);
-        if (!plans[k]->adj_ok)
+        if (!bp && !plans[k]->adj_ok)
             return set_error(RG_EUNSUPPORTED, "EM needs ray spacing >= pixel spacing (nrays <= size)");
     }
     float *ratio = (float *)s.take((size_t)R * A * sizeof(float));
@@ -71,15 +75,21 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
     float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N));
     float *inv = (float *)s.take((size_t)N * N * sizeof(float) * S);
     int rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
-    for (int k = 0; k < S && !rc; ++k)
-        rc = launch_gather(*plans[k], 2, ratio, R, inv + (size_t)k * N * N, N, 1, nullptr, nullptr,
-                           nullptr, st);
+    for (int k = 0; k < S && !rc; ++k) {
+        float *ik = inv + (size_t)k * N * N;
+        if (bp) {
+            rc = launch_gather(*plans[k], 0, ratio, R, ik, N, 1, nullptr, nullptr, nullptr, st);
+            if (!rc) rc = launch_invert(ik, ik, (size_t)N * N, st);
+        } else {
+            rc = launch_gather(*plans[k], 2, ratio, R, ik, N, 1, nullptr, nullptr, nullptr, st);
+        }
+    }
     for (int it = 0; it < niter && !rc; ++it)
         for (int k = 0; k < S && !rc; ++k) {
             if ((rc = launch_line_pairs(x, N, 1, N, prow, pcol, st))) break;
             if ((rc = launch_radon(*plans[k], prow, pcol, ratio, R, y_am, R, st))) break;
-            rc = launch_gather(*plans[k], 1, ratio, R, nullptr, 0, 0, x, inv + (size_t)k * N * N,
-                               nullptr, st);
+            rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, nullptr, 0, 0, x,
+                               inv + (size_t)k * N * N, nullptr, st);
         }
     return rc;
 }
@@ -223,7 +233,8 @@ int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, vo
         return set_error(RG_EINVAL, "rg_em: nsubsets must be in [1, nviews]");
     cudaStream_t st = (cudaStream_t)stream;
     if (method == RG_BRESENHAM) return em_dda(sino, image, niter, nsubsets, ws, wsb, st);
-    if (method != RG_SLANTSTACK) return set_error(RG_EINVAL, "rg_em: unknown method %d", method);
+    if (method != RG_SLANTSTACK && method != RG_SLANTSTACK_BP)
+        return set_error(RG_EINVAL, "rg_em: unknown method %d", method);
     if (image.lines != image.columns || image.lines < 2 || sino.lines < 2)
         return set_error(RG_EINVAL, "slant-stack EM needs a square image, size >= 2, nrays >= 2");
     SSGeom g;
@@ -239,7 +250,7 @@ int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, vo
     float *x = (float *)s.take((size_t)N * N * sizeof(float));
     rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, y, st);
     if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, N, 1, N, N, st);
-    if (!rc) rc = em_ss_core(g, niter, nsubsets, y, x, s, st);
+    if (!rc) rc = em_ss_core(g, niter, nsubsets, y, x, s, st, method == RG_SLANTSTACK_BP);
     if (!rc) rc = launch_copy2d(x, N, 1, image.data, image.column_stride, image.line_stride, N, N, st);
     scratch_end(s);
     return rc;

@@ -161,7 +161,7 @@ int ensure_device_error_word();
 int radon_views_per_thread(const SSPlan &p);
 // Gathers.  mode 0: backprojection (scaled by dth); 1: matched adjoint;
 // 2: matched adjoint accumulated in FP64, epilogue writes 1/x (0 where 0).
-// em_x != nullptr (mode 1): x <- x * adj * inv_sens, with x, inv_sens
+// em_x != nullptr (modes 0, 1): x <- x * gather * inv_sens, with x, inv_sens
 // contiguous N x N.
 // A stack of n equal-geometry problems in one launch (grid z): consecutive
 // inputs `in` floats apart, outputs `out` floats apart.

@@ -502,8 +502,11 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                   cudaStream_t st, int rows, Stack z)
 {
     if (rows == 0) rows = tuned_rows(p, mode);
-    if (mode == 0)
+    if (mode == 0) {
+        if (em_x)
+            return gather_rows<0, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
         return gather_rows<0, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
+    }
     if (!p.adj_ok)
         return set_error(RG_EUNSUPPORTED,
                          "matched adjoint needs ray spacing >= pixel spacing along each line "

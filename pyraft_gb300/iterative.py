@@ -31,15 +31,20 @@ def _run_em(sino, x0, method, niter, nsubsets):
                           ws_t.numel() if ws_t is not None else 0, stream_ptr()))
 
 
-def _method(projection_method, backprojection_method):
+def _method(projection_method, backprojection_method, reference=False):
+    """Native EM method id.  reference=True (slant-stack only) backprojects
+    with the slant-stack backprojection instead of the matched adjoint, the
+    pairing of the reference's GPU EM (raft/raft_em_gpu.cu:20-87)."""
     p, b = method_id(projection_method), method_id(backprojection_method)
     if p != b:
         raise TypeError('projection and backprojection methods must form a transpose pair '
                         '(both BRESENHAM or both SLANTSTACK)')
     if p == method_id(radon_method.BRESENHAM):
+        if reference:
+            raise TypeError('reference=True applies to the SLANTSTACK method')
         return _native.RG_BRESENHAM
     if p == method_id(radon_method.SLANTSTACK):
-        return _native.RG_SLANTSTACK
+        return _native.RG_SLANTSTACK_BP if reference else _native.RG_SLANTSTACK
     raise TypeError('Unsupported method for EM!')
 
 
@@ -63,12 +68,14 @@ def _finish_em(x, shape_host, sino_host):
 
 
 def make_em(sino, shape, projection_method=radon_method.BRESENHAM,
-            backprojection_method=radon_method.BRESENHAM, weight=None, **kwargs):
-    """One-iteration EM map x -> x * A^T(y / A x) / A^T 1."""
+            backprojection_method=radon_method.BRESENHAM, weight=None, reference=False,
+            **kwargs):
+    """One-iteration EM map x -> x * A^T(y / A x) / A^T 1 (reference=True:
+    the slant-stack backprojection B in place of A^T)."""
     if weight is not None:
         raise TypeError('a precomputed weight is not supported; the sensitivity is computed '
                         'on the device in FP64')
-    m = _method(projection_method, backprojection_method)
+    m = _method(projection_method, backprojection_method, reference)
     gs, _ = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
 
     def em_step(x):
@@ -79,27 +86,33 @@ def make_em(sino, shape, projection_method=radon_method.BRESENHAM,
     return em_step
 
 
-def em(sino, shape=None, niter=5, method=radon_method.BRESENHAM, **kwargs):
+def em(sino, shape=None, niter=5, method=radon_method.BRESENHAM, reference=False, **kwargs):
+    """EM (pyraft/iterative/em.py:151-169).  reference=True with SLANTSTACK:
+    backproject with the slant-stack backprojection, as the reference's GPU
+    EM does, instead of the matched adjoint."""
     if shape is None:
         shape = [sino.shape[1], sino.shape[1]]
     x, host = _start(shape, kwargs)
     gs, shost = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
-    _run_em(gs, x, _method(method, method), niter, 1)
+    _run_em(gs, x, _method(method, method, reference), niter, 1)
     return _finish_em(x, host, shost)
 
 
-def osem(sino, shape=None, niter=5, nblocks=4, method=radon_method.SLANTSTACK, **kwargs):
+def osem(sino, shape=None, niter=5, nblocks=4, method=radon_method.SLANTSTACK, reference=False,
+         **kwargs):
     if shape is None:
         shape = [sino.shape[0], sino.shape[0]]
     x, host = _start(shape, kwargs)
     gs, shost = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
-    _run_em(gs, x, _method(method, method), niter, nblocks)
+    _run_em(gs, x, _method(method, method, reference), niter, nblocks)
     return _finish_em(x, host, shost)
 
 
 def em_gpu(*args):
     """pyraft's em_gpu(s, img_size=rays, niter=20): host sinogram on the
-    default geometry -> (img_size, img_size) float32 array."""
+    default geometry -> (img_size, img_size) float32 array, with the
+    reference GPU EM's operator pair (slant-stack Radon, slant-stack
+    backprojection; raft/raft_em_gpu.cu:20-87)."""
     if len(args) == 0:
         raise TypeError('Not enough arguments!')
     s = args[0]
@@ -107,7 +120,7 @@ def em_gpu(*args):
     niter = args[2] if len(args) > 2 else 20
     src = image(numpy.asarray(s, dtype=numpy.float64), top_left=(0.0, 1.0),
                 bottom_right=(numpy.pi, -1.0))
-    out = em(src, (n, n), niter, method=radon_method.SLANTSTACK)
+    out = em(src, (n, n), niter, method=radon_method.SLANTSTACK, reference=True)
     return numpy.asarray(out, dtype=numpy.float32)
 
 

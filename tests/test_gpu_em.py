@@ -77,11 +77,14 @@ def test_em_dda_pair_vs_oracle(orc):
 def test_em_gpu_wrapper_and_make_em(orc):
     n, r, a = 32, 32, 30
     y = _emission(orc, n, r, a, 4)
-    out = rg.em_gpu(y, n, 7)
     fwd = lambda x: orc.radon_slantstack(x, r, a)
     adj = lambda s: orc.radon_slantstack_transpose(s, n)
+    bp = lambda s: orc.backprojection_slantstack(s, n)
+    # em_gpu pairs the Radon with the backprojection, as raft_em_gpu does
+    out = rg.em_gpu(y, n, 7)
+    ref_bp = orc.em_guarded(y, np.ones((n, n)), fwd, bp, 7)
+    assert out.dtype == np.float32 and rel(out, ref_bp) <= 1e-4
     ref = orc.em_guarded(y, np.ones((n, n)), fwd, adj, 7)
-    assert out.dtype == np.float32 and rel(out, ref) <= 1e-4
     s = rg.image(y, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
     step = rg.make_em(s, (n, n), SLANT, SLANT)
     x = rg.image(np.ones((n, n)))
@@ -94,3 +97,29 @@ def test_em_zero_data_is_guarded():
     s = rg.image(np.zeros((32, 30)), top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
     out = rg.em(s, (32, 32), 3, method=SLANT)
     assert np.isfinite(np.asarray(out)).all() and np.abs(np.asarray(out)).max() == 0.0
+
+
+def test_em_reference_backprojector_vs_oracle(orc):
+    """reference=True: EM and OSEM with the slant-stack backprojection as the
+    backprojector (the reference GPU EM's pairing), 30 iterations."""
+    n, r, a = 64, 64, 60
+    y = _emission(orc, n, r, a, 6)
+    fwd = lambda x: orc.radon_slantstack(x, r, a)
+    bp = lambda s: orc.backprojection_slantstack(s, n)
+    ref = orc.em_guarded(y, np.ones((n, n)), fwd, bp, 30)
+    s = rg.image(y, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
+    out = rg.em(s, (n, n), 30, method=SLANT, reference=True)
+    assert rel(out, ref) <= 1e-4
+
+    def fsub(x, idx):
+        return orc.radon_slantstack(x, r, a)[:, idx]
+
+    def bsub(t, idx):
+        full = np.zeros((r, a))
+        full[:, idx] = t
+        return orc.backprojection_slantstack(full, n)
+    ref_os = orc.osem_interleaved(y, np.ones((n, n)), fsub, bsub, 4, 5)
+    out_os = rg.osem(s, (n, n), 5, 4, reference=True)
+    assert rel(out_os, ref_os) <= 1e-4
+    with pytest.raises(TypeError):
+        rg.em(s, (n, n), 1, method=rg.radon_method.BRESENHAM, reference=True)
