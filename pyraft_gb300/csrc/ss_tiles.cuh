@@ -399,7 +399,7 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
                                             const float *__restrict__ inv_sens,
                                             int *__restrict__ err, int tx, int ty,
                                             float2 *__restrict__ pairs, unsigned pair_bytes,
-                                            int split = 1, int rank = 0)
+                                            int split = 1, int rank = 0, bool edge_fixup = false)
 {
     constexpr int TH = kWarps * ROWS;          // tile height
     __shared__ SlotInfo slot[kSlots];
@@ -414,7 +414,13 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
     const int row0 = ty * TH, col0 = tx * kTile;
     const int col = col0 + lane;
     const int myrow = row0 + warp * ROWS;
-    const bool border = row0 == 0 || col0 == 0 || row0 + TH >= N || col0 + kTile >= N;
+    // edge_fixup (adjoint modes): every tile takes the interior path and the
+    // image's edge pixels (row or column 0 or N-1, the only pixels where the
+    // position-0 / N-1 validity rules apply) are left to k_adjoint_edges,
+    // which recomputes them with the rules; otherwise border tiles apply the
+    // rules inline.
+    const bool border = !edge_fixup &&
+                        (row0 == 0 || col0 == 0 || row0 + TH >= N || col0 + kTile >= N);
 
     Acc acc[ROWS], comp[ROWS];
 #pragma unroll
@@ -524,8 +530,9 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
             for (int src = 0; src < split; ++src)
                 sum += cl.map_shared_rank(red, src)[r * 256 + threadIdx.x];
             const int row = myrow + r;
-            if (row < N && col < N) gather_store<MODE, EM>(sum * scale, row, col, N, out, cs, ls,
-                                                           em_x, inv_sens);
+            const bool edge = edge_fixup && (row == 0 || col == 0 || row == N - 1 || col == N - 1);
+            if (row < N && col < N && !edge)
+                gather_store<MODE, EM>(sum * scale, row, col, N, out, cs, ls, em_x, inv_sens);
         }
         cl.sync();    // no CTA leaves while a peer still reads its partials
         return;
@@ -534,6 +541,7 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
     for (int r = 0; r < ROWS; ++r) {
         const int row = myrow + r;
         if (row >= N || col >= N) break;
+        if (edge_fixup && (row == 0 || col == 0 || row == N - 1 || col == N - 1)) continue;
         if (MODE == 2) {
             const double sv = (double)acc[r];
             out[(long long)row * cs + (long long)col * ls] = (sv > 0.0) ? (float)(1.0 / sv) : 0.f;
