@@ -43,10 +43,10 @@ struct BatchSlice {
     float2 *prow, *pcol;   // line pairs of the iterate
     float *x;              // iterate, N x N contiguous
     float *inv_sens;       // 1 / A_s^T 1 of this subset, N x N
-    int begin[3];          // first item of this slice in each work list
+    int begin[4];          // first item of this slice in each work list
 };
 
-enum { kLP = 0, kRadon = 1, kGather = 2 };
+enum { kLP = 0, kRadon = 1, kGather = 2, kEdges = 3 };
 
 __device__ __forceinline__ int find_slice(const BatchSlice *__restrict__ d, int n, int item, int w)
 {
@@ -119,13 +119,31 @@ __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restri
             gather_tile<1, WMAX, kBatchRows, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
                                                    nullptr, 0, 0, b.x, b.inv_sens, nullptr,
                                                    local % tiles, local / tiles, pairs,
-                                                   pair_bytes);
+                                                   pair_bytes, 1, 0, true);
         else
             gather_tile<2, WMAX, kBatchRows, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
                                                     b.inv_sens, b.N, 1, nullptr, nullptr, nullptr,
                                                     local % tiles, local / tiles, pairs,
-                                                    pair_bytes);
+                                                    pair_bytes, 1, 0, true);
     }
+}
+
+// Edge pixels left out by k_batch_gather (adjoint_edge_pixel): one warp per
+// edge pixel of every slice (items: slice x (4N - 4)).
+template <int MODE>
+__global__ __launch_bounds__(128) void k_batch_edges(const BatchSlice *__restrict__ d, int n,
+                                                     int total)
+{
+    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (item >= total) return;        // warp-uniform
+    const BatchSlice &b = d[find_slice(d, n, item, kEdges)];
+    const int e = item - b.begin[kEdges];
+    if (MODE == 1)
+        adjoint_edge_pixel<1, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, e, nullptr, 0, 0,
+                                    b.x, b.inv_sens);
+    else
+        adjoint_edge_pixel<2, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, e, b.inv_sens, b.N,
+                                     1, nullptr, nullptr);
 }
 
 // Grid of a persistent launch: resident capacity, capped by the item count.
@@ -142,7 +160,7 @@ int persistent_grid(K kernel, int threads, size_t smem, int items, int *out)
 
 struct BatchRun {
     int n = 0, S = 0, wmax = 64, vpt = 2;
-    int total[3][64] = {};            // [kind][subset] item counts (subset 0 for pairs)
+    int total[4][64] = {};            // [kind][subset] item counts (subset 0 for pairs)
     int grid[4][64] = {};             // persistent grids: pairs, radon[s], gather1, gather2
     BatchSlice *d_desc = nullptr;     // S x n descriptors (device, in scratch)
     int *counter = nullptr;
@@ -187,6 +205,9 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
                                                                   br.counter,
                                                                   (unsigned)sizeof(float2));
         RG_CK_LAUNCH("k_batch_gather<1>");
+        k_batch_edges<1><<<(br.total[kEdges][0] + 3) / 4, 128, 0, st>>>(d, br.n,
+                                                                       br.total[kEdges][0]);
+        RG_CK_LAUNCH("k_batch_edges<1>");
     }
     return RG_OK;
 }
@@ -202,6 +223,9 @@ int enqueue_sensitivity(const BatchRun &br, cudaStream_t st)
                                                                   br.counter,
                                                                   (unsigned)sizeof(float2));
         RG_CK_LAUNCH("k_batch_gather<2>");
+        k_batch_edges<2><<<(br.total[kEdges][0] + 3) / 4, 128, 0, st>>>(d, br.n,
+                                                                       br.total[kEdges][0]);
+        RG_CK_LAUNCH("k_batch_edges<2>");
     }
     return RG_OK;
 }
@@ -428,7 +452,7 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
     br.counter = (int *)sc.take(sizeof(int));
     br.d_desc = (BatchSlice *)sc.take(sizeof(BatchSlice) * S * nslices);
     std::vector<BatchSlice> hd((size_t)S * nslices);
-    int items_lp = 0, items_g = 0;
+    int items_lp = 0, items_g = 0, items_e = 0;
     std::vector<int> items_r(S, 0);
     std::vector<float *> xs(nslices);
     for (int q = 0; q < nslices && !rc; ++q) {
@@ -464,13 +488,16 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
             d.begin[kLP] = items_lp;
             d.begin[kRadon] = items_r[s];
             d.begin[kGather] = items_g;
+            d.begin[kEdges] = items_e;
             items_r[s] += ((R + 31) / 32) * ((p->nv + vpb - 1) / vpb);
         }
         items_lp += tiles * tiles;
         items_g += tiles * tiles_y;
+        items_e += 4 * N - 4;
     }
     br.total[kLP][0] = items_lp;
     br.total[kGather][0] = items_g;
+    br.total[kEdges][0] = items_e;
     for (int s = 0; s < S; ++s) br.total[kRadon][s] = items_r[s];
     if (!rc) {
         cudaError_t e = cudaMemcpyAsync(br.d_desc, hd.data(), sizeof(BatchSlice) * hd.size(),

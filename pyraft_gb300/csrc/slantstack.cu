@@ -350,14 +350,9 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
                                       blockIdx.x % split, MODE != 0);
 }
 
-// Edge pixels of the matched adjoint (MODE 1, optionally with the EM update)
-// and of its FP64-accumulated sensitivity (MODE 2): the image's first and
-// last rows and columns are the only pixels where the Radon's validity
-// rules at line positions 0 and N-1 apply.  One warp per edge pixel; lane l
-// sums views l, l + 32, ... straight from the view-major sinogram, with the
-// same hat weights and rules as the gather's border tiles, and the lanes'
-// sums meet in a fixed butterfly order.  The gathers themselves then run the
-// rule-free interior path on every tile.
+// Edge pixels of the matched adjoint and of its FP64 sensitivity
+// (adjoint_edge_pixel, ss_tiles.cuh): one warp per pixel of the image's
+// first and last rows and columns.
 template <int MODE, bool EM>
 __global__ __launch_bounds__(128) void k_adjoint_edges(const float *__restrict__ s_am, int s_ld,
                                                        int R, const View *__restrict__ views,
@@ -367,57 +362,10 @@ __global__ __launch_bounds__(128) void k_adjoint_edges(const float *__restrict__
                                                        const float *__restrict__ inv_sens,
                                                        long long zs, long long zo)
 {
-    const int e = blockIdx.x * 4 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (e >= 4 * N - 4) return;       // warp-uniform
-    int row, col;                     // rows 0 and N-1, then columns 0 and N-1
-    if (e < N) { row = 0; col = e; }
-    else if (e < 2 * N) { row = N - 1; col = e - N; }
-    else if (e < 3 * N - 2) { row = e - 2 * N + 1; col = 0; }
-    else { row = e - (3 * N - 2) + 1; col = N - 1; }
-    s_am += blockIdx.z * zs;
-    out += blockIdx.z * zo;
-    float acc = 0.f, comp = 0.f;
-    double acc64 = 0.0;
-    for (int j = lane; j < nv; j += 32) {
-        const View &v = views[j];
-        const long long kap = v.k0 + (long long)row * v.krow + (long long)col * v.kcol;
-        const int k = (int)(kap >> 32);
-        const float w1 = frac_plus_one((unsigned)kap >> 9);
-        const float P = v.P;
-        float wa = fma_sat(-P, w1, 1.f + P);
-        float wb = fma_sat(P, w1, 1.f - 2.f * P);
-        const bool pneg = (v.flags & kRkNegative) != 0;
-        const int m = (v.flags & kLinesAreRows) ? col : row;
-        const bool f0 = (w1 == 1.0f);
-        if (m == 0) {                       // drop u < 0
-            if (!pneg && !f0) wa = 0.f;
-            if (pneg) wb = 0.f;
-        } else if (m == N - 1) {            // drop u >= N-1
-            if (pneg || f0) wa = 0.f;
-            if (!pneg) wb = 0.f;
-        }
-        const float *__restrict__ srow = s_am + (size_t)v.view * s_ld;
-        const float s0 = (k >= 0 && k < R) ? __ldg(srow + k) * v.delta : 0.f;
-        const float s1 = (k + 1 >= 0 && k + 1 < R) ? __ldg(srow + k + 1) * v.delta : 0.f;
-        const float term = fmaf(s1, wb, s0 * wa);
-        if (MODE == 2) acc64 += (double)term;
-        else kahan_add(acc, comp, term);
-    }
-    float sum = acc - comp;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        if (MODE == 2) acc64 += __shfl_xor_sync(0xffffffffu, acc64, o);
-        else sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    }
-    if (lane != 0) return;
-    if (MODE == 2) {
-        out[(long long)row * cs + (long long)col * ls] = (acc64 > 0.0) ? (float)(1.0 / acc64) : 0.f;
-    } else if (EM) {
-        const size_t idx = (size_t)row * N + col;
-        em_x[idx] = em_x[idx] * sum * inv_sens[idx];
-    } else {
-        out[(long long)row * cs + (long long)col * ls] = sum;
-    }
+    adjoint_edge_pixel<MODE, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, e,
+                                 out + blockIdx.z * zo, cs, ls, em_x, inv_sens);
 }
 
 template <int MODE, bool EM>

@@ -364,6 +364,72 @@ __device__ __forceinline__ void accumulate(float (&part)[ROWS], const float2 *__
     }
 }
 
+// Edge pixel e (of 4N - 4: rows 0 and N-1, then columns 0 and N-1) of the
+// matched adjoint (MODE 1, optionally with the EM update) or of its
+// FP64-accumulated sensitivity (MODE 2), computed by one warp.  The image's
+// first and last rows and columns are the only pixels where the Radon's
+// validity rules at line positions 0 and N-1 apply; the gathers leave them
+// out (edge_fixup) and run the rule-free interior path on every tile.  Lane
+// l sums views l, l + 32, ... straight from the view-major sinogram, with
+// the hat weights and rules of the border path of `accumulate`, and the
+// lanes' sums meet in a fixed butterfly order.
+template <int MODE, bool EM>
+__device__ __forceinline__ void adjoint_edge_pixel(const float *__restrict__ s_am, int s_ld, int R,
+                                                   const View *__restrict__ views, int nv, int N,
+                                                   int e, float *__restrict__ out, long long cs,
+                                                   long long ls, float *__restrict__ em_x,
+                                                   const float *__restrict__ inv_sens)
+{
+    const int lane = threadIdx.x & 31;
+    int row, col;
+    if (e < N) { row = 0; col = e; }
+    else if (e < 2 * N) { row = N - 1; col = e - N; }
+    else if (e < 3 * N - 2) { row = e - 2 * N + 1; col = 0; }
+    else { row = e - (3 * N - 2) + 1; col = N - 1; }
+    float acc = 0.f, comp = 0.f;
+    double acc64 = 0.0;
+    for (int j = lane; j < nv; j += 32) {
+        const View &v = views[j];
+        const long long kap = v.k0 + (long long)row * v.krow + (long long)col * v.kcol;
+        const int k = (int)(kap >> 32);
+        const float w1 = frac_plus_one((unsigned)kap >> 9);
+        const float P = v.P;
+        float wa = fma_sat(-P, w1, 1.f + P);
+        float wb = fma_sat(P, w1, 1.f - 2.f * P);
+        const bool pneg = (v.flags & kRkNegative) != 0;
+        const int m = (v.flags & kLinesAreRows) ? col : row;
+        const bool f0 = (w1 == 1.0f);
+        if (m == 0) {                       // drop u < 0
+            if (!pneg && !f0) wa = 0.f;
+            if (pneg) wb = 0.f;
+        } else if (m == N - 1) {            // drop u >= N-1
+            if (pneg || f0) wa = 0.f;
+            if (!pneg) wb = 0.f;
+        }
+        const float *__restrict__ srow = s_am + (size_t)v.view * s_ld;
+        const float s0 = (k >= 0 && k < R) ? __ldg(srow + k) * v.delta : 0.f;
+        const float s1 = (k + 1 >= 0 && k + 1 < R) ? __ldg(srow + k + 1) * v.delta : 0.f;
+        const float term = fmaf(s1, wb, s0 * wa);
+        if (MODE == 2) acc64 += (double)term;
+        else kahan_add(acc, comp, term);
+    }
+    float sum = acc - comp;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        if (MODE == 2) acc64 += __shfl_xor_sync(0xffffffffu, acc64, o);
+        else sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    }
+    if (lane != 0) return;
+    if (MODE == 2) {
+        out[(long long)row * cs + (long long)col * ls] = (acc64 > 0.0) ? (float)(1.0 / acc64) : 0.f;
+    } else if (EM) {
+        const size_t idx = (size_t)row * N + col;
+        em_x[idx] = em_x[idx] * sum * inv_sens[idx];
+    } else {
+        out[(long long)row * cs + (long long)col * ls] = sum;
+    }
+}
+
 // Final value of pixel (row, col) of a gather: stored, or (EM) folded into
 // the multiplicative update x <- x * val * inv_sens.
 template <int MODE, bool EM>
