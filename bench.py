@@ -8,8 +8,8 @@ U(0, 1)); transmission sinogram = slant-stack Radon scaled to a maximum
 attenuation of 3, Poisson counts at I0 = 1e4 per ray, -log(counts / I0) with
 counts >= 1.  One step = one rg_fbp call (filter + backprojection) on a
 resident sinogram.  The sinogram (14.7 MB) fits in L2, so L2 is flushed
-(256 MiB write) before every timed step and the step time is the sum of
-per-step CUDA-event intervals.
+(160 MiB write, above the 129 MB L2) before every timed step and the step
+time is the sum of per-step CUDA-event intervals.
 
 Also reported: the backprojection kernel alone against the HBM roofline of
 the gather-byte model (8 B per interpolated update + compulsory image and
@@ -411,7 +411,7 @@ def main():
     I = rg_image(rg.gpu_image(img))
     ws_bytes = L.rg_fbp_workspace(S, I, _native.RG_FILTER_RAMLAK)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(160 << 20, dtype=torch.uint8, device="cuda")   # > 129 MB L2
 
     def step():
         _native.check(L.rg_fbp(S, I, _native.RG_FILTER_RAMLAK, ws.data_ptr(), ws_bytes, sp))
@@ -596,7 +596,7 @@ def main():
         "config": {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
                                "slant-stack backprojection, one slice per GPU",
                    "image": N, "views": A, "rays": R, "filter": "ramlak",
-                   "l2": "flushed (256 MiB write) before every timed step; step time = sum "
+                   "l2": "flushed (160 MiB write) before every timed step; step time = sum "
                          "of per-step CUDA-event intervals",
                    "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
         "e2e": {"value": round(world * UPDATES / (p_ms * 1e-3) / 1e9, 3), "unit": UNIT,
