@@ -421,9 +421,9 @@ static EncodeTiledFn encode_fn()
 }
 
 // 3-D map over nz stacked line-pair arrays: (entry, line, image), 8-byte
-// elements, box BW x kTmLines x 1, zero fill outside.
+// elements, box bw x box_lines x 1, zero fill outside.
 static int encode_pairs_map(CUtensorMap *tm, const float2 *pairs, int N, int nz, long long zp,
-                            int bw)
+                            int bw, int box_lines = kTmLines)
 {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return set_error(RG_ECUDA, "cuTensorMapEncodeTiled is not available");
@@ -431,7 +431,7 @@ static int encode_pairs_map(CUtensorMap *tm, const float2 *pairs, int N, int nz,
     cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)N, (cuuint64_t)nz};
     cuuint64_t strides[2] = {(cuuint64_t)pitch * 8,
                              (cuuint64_t)(nz > 1 ? zp : (long long)N * pitch) * 8};
-    cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)kTmLines, 1};
+    cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)box_lines, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, (void *)pairs, dims, strides, box,
                     estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
@@ -506,6 +506,214 @@ int launch_radon_tma(const SSPlan &p, const float2 *prow, const float2 *pcol, fl
         return launch_tma_epi<kEpiTransmission>(p, tr, tc, out_am, out_ld, y_am, y_ld, nz, zo,
                                                 d_err, st);
     return launch_tma_epi<kEpiSum>(p, tr, tc, out_am, out_ld, nullptr, 0, nz, zo, d_err, st);
+}
+
+
+// ============================================================================
+// Tile-driven Radon for plans of scattered views (OSEM subsets).
+//
+// The view-block windows above need adjacent views; a subset's views are S
+// apart, so their positions on a line spread too far for one window.  Here
+// the loop order is turned around: a CTA owns an image tile -- kTtLines lines
+// x kTtWin line-pair entries [p0, p0 + kTtWin) of one orientation -- staged
+// once by TMA (one row copy per line, zero-filled outside the array), and
+// every view of the plan with that orientation sends through it the rays
+// that cross it.  Each staged entry then serves every view (tens to
+// hundreds), not the few views of a block.
+//
+// Ownership: a sample (ray, line) belongs to the tile whose line block holds
+// the line and whose window holds the sample's entry.  Each smem row carries
+// kTtPad zero entries on both sides of the window, wide enough for any
+// crossing ray's positions on the tile's lines (checked per plan on the host
+// and per ray in the kernel), so a ray adds exactly its owned samples with
+// the plain 7-instruction walk of the other kernels, and samples outside
+// the window read zeros.  Each (ray, view, tile) partial, times Delta, is
+// added to the sinogram with one atomic add (the zeroing pass before and
+// the epilogue pass after are separate launches); the order of those adds
+// varies between runs, at the level of FP32 rounding.
+constexpr int kTtLines = 32;                  // lines per tile
+constexpr int kTtWin = 160;                   // owned entries per tile row
+constexpr int kTtPad = 48;                    // zero entries on each side
+constexpr int kTtRow = kTtWin + 2 * kTtPad;   // smem row stride (entries): 2 KB
+
+template <int R0>
+__device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, float &part)
+{
+    if constexpr (R0 < kTtLines) {
+        const float2 pr = lds_pair_at<R0 * kTtRow * 8>(sb + ((L >> 23) << 3));
+        part += fmaf(frac_plus_one(L), pr.y, pr.x);
+        L += dq;
+        tt_walk<R0 + 1>(sb, L, dq, part);
+    }
+}
+
+__global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUtensorMap tm_rows,
+                                                     const __grid_constant__ CUtensorMap tm_cols,
+                                                     int N, const View *__restrict__ views,
+                                                     const int *__restrict__ ovid, int n_rows,
+                                                     int n_cols, int R,
+                                                     float *__restrict__ out_am, int out_ld,
+                                                     long long zo, int *__restrict__ err)
+{
+    extern __shared__ __align__(128) float2 tile[];   // [kTtLines][kTtRow]
+    __shared__ __align__(8) unsigned long long full;
+    const int o = blockIdx.z & 1, z = blockIdx.z >> 1;
+    const int nvo = o ? n_cols : n_rows;
+    if (nvo == 0) return;                              // CTA-uniform, before any barrier
+    const int *__restrict__ vid = ovid + (o ? n_rows : 0);
+    const CUtensorMap *tm = o ? &tm_cols : &tm_rows;
+    const int p0 = blockIdx.x * kTtWin, i0 = blockIdx.y * kTtLines;
+    const unsigned sbase = smem_addr(tile);
+    out_am += (long long)z * zo;
+
+    if (threadIdx.x == 0) {
+        mbar_init(smem_addr(&full), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // zero pads (the TMA rows fill the middle of each row)
+    for (int e = threadIdx.x; e < kTtLines * 2 * kTtPad; e += blockDim.x) {
+        const int r = e / (2 * kTtPad), c = e - r * (2 * kTtPad);
+        tile[r * kTtRow + (c < kTtPad ? c : kTtWin + c)] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(smem_addr(&full), kTtLines * kTtWin * 8);
+        for (int r = 0; r < kTtLines; ++r)
+            tma_load_3d(sbase + (r * kTtRow + kTtPad) * 8, tm, p0, i0 + r, z, smem_addr(&full));
+    }
+    const bool ok = mbar_wait(smem_addr(&full), 0);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) {
+            if (err) atomicOr(err, 2);
+            mbar_wait(smem_addr(&full), 0);            // bounded: copies still in flight
+        }
+        return;
+    }
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int i1 = i0 + kTtLines - 1;
+    // window samples [a, b): entry p0 holds sample p0 - 1
+    const double a = p0 - 1.0, b = p0 - 1.0 + kTtWin;
+    const long long base_q = (long long)(p0 - kTtPad - 1) << 32;   // smem index 0
+    for (int j = warp; j < nvo; j += 8) {
+        const View &v = views[vid[j]];
+        // rays whose positions on lines i0..i1 meet [a, b), +-1 ray of margin
+        const double rk = (double)v.rk * 2.3283064365386963e-10;
+        const double c0 = ((double)v.r0 + (double)i0 * (double)v.ri) * 2.3283064365386963e-10;
+        const double c1 = ((double)v.r0 + (double)i1 * (double)v.ri) * 2.3283064365386963e-10;
+        const double cmin = fmin(c0, c1), cmax = fmax(c0, c1);
+        double ka = (a - cmax) / rk, kb = (b - cmin) / rk;
+        if (ka > kb) { const double t = ka; ka = kb; kb = t; }
+        const int k_lo = max(0, (int)floor(fmin(fmax(ka, -1.0), (double)R)) - 1);
+        const int k_hi = min(R - 1, (int)ceil(fmax(fmin(kb, (double)R), -1.0)) + 1);
+        const unsigned dq = (unsigned)((v.ri + 256) >> 9);
+        const float delta = v.delta;
+        float *__restrict__ orow = out_am + (size_t)v.view * out_ld;
+        for (int k = k_lo + lane; k <= k_hi; k += 32) {
+            const long long u = v.r0 + (long long)k * v.rk + (long long)i0 * v.ri - base_q;
+            const long long ue = u + (long long)(kTtLines - 1) * v.ri;
+            // one entry of slack on both sides for the Q9.23 stepping
+            const long long lo_q = 1LL << 32, hi_q = (long long)(kTtRow - 1) << 32;
+            if (u < lo_q || u >= hi_q || ue < lo_q || ue >= hi_q) {
+                // a ray that crosses the window stays within the pads; this
+                // one does not cross it (margin ray), or the plan's pad check
+                // failed (flagged): it adds nothing here
+                if (err && u >= (long long)kTtPad << 32 && u < (long long)(kTtPad + kTtWin) << 32)
+                    atomicOr(err, 1);
+                continue;
+            }
+            unsigned L = (unsigned)(u >> 9);
+            float part = 0.f;
+            tt_walk<0>(sbase, L, dq, part);
+            if (part != 0.f) atomicAdd(orow + k, part * delta);
+        }
+    }
+}
+
+// out[view][k] = 0 (zeroing pass) or the epilogue of the summed rays, for
+// the plan's views only.
+template <int EPI, bool ZERO>
+__global__ __launch_bounds__(256) void k_views_rows(const View *__restrict__ views, int nv, int R,
+                                                    float *__restrict__ out_am, int out_ld,
+                                                    const float *__restrict__ y_am, int y_ld,
+                                                    long long zo)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (k >= R || j >= nv) return;
+    const int view = views[j].view;
+    float *o = out_am + (long long)blockIdx.z * zo + (size_t)view * out_ld + k;
+    if (ZERO) *o = 0.f;
+    else *o = radon_epilogue(EPI, *o, y_am, (size_t)view * y_ld + k);
+}
+
+int tt_build(SSPlan &p, const View *hv)
+{
+    p.tt_ok = false;
+    p.n_ovid[0] = p.n_ovid[1] = 0;
+    const int nv = p.nv;
+    if (nv < 1) return RG_OK;
+    std::vector<int> ids;
+    for (int o = 0; o < 2; ++o)
+        for (int e = 0; e < nv; ++e)
+            if (((hv[e].flags & kLinesAreRows) ? 0 : 1) == o) {
+                ids.push_back(e);
+                ++p.n_ovid[o];
+            }
+    // pads must hold any crossing ray's positions on the tile's lines: the
+    // walk across the tile's lines plus the margin rays
+    double need = 0.0;
+    for (int e = 0; e < nv; ++e) {
+        const double ri = fabs((double)hv[e].ri) * 2.3283064365386963e-10;
+        const double rk = fabs((double)hv[e].rk) * 2.3283064365386963e-10;
+        need = std::max(need, (kTtLines - 1) * ri + 2.0 * rk + 3.0);
+    }
+    if (need > kTtPad) return RG_OK;
+    RG_CK(cudaMalloc(&p.d_ovid, sizeof(int) * ids.size()));
+    RG_CK(cudaMemcpy(p.d_ovid, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice));
+    p.tt_ok = true;
+    return RG_OK;
+}
+
+bool radon_tiles_usable(const SSPlan &p)
+{
+    const char *e = getenv("RG_RADON_KERNEL");
+    if (e && !strcmp(e, "direct")) return false;
+    if (!p.tt_ok || !p.d_ovid) return false;
+    if (e && !strcmp(e, "tiles")) return true;
+    return !radon_tma_usable(p) && p.nv >= 16;
+}
+
+int launch_radon_tiles(const SSPlan &p, const float2 *prow, const float2 *pcol, float *out_am,
+                       int out_ld, const float *y_am, int y_ld, cudaStream_t st, int nz,
+                       long long zp, long long zo, int epi)
+{
+    const int N = p.g.N, R = p.g.R;
+    CUtensorMap tr, tc;
+    int rc = encode_pairs_map(&tr, prow, N, nz, zp, kTtWin, 1);
+    if (!rc) rc = encode_pairs_map(&tc, pcol, N, nz, zp, kTtWin, 1);
+    if (rc) return rc;
+    const dim3 gv((R + 255) / 256, p.nv, nz);
+    k_views_rows<kEpiSum, true><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am, out_ld, nullptr,
+                                                    0, zo);
+    RG_CK_LAUNCH("k_views_rows (zero)");
+    const size_t smem = (size_t)kTtLines * kTtRow * 8;
+    RG_CK(cudaFuncSetAttribute(k_radon_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+    const dim3 grid((pairs_pitch(N) + kTtWin - 1) / kTtWin, (N + kTtLines - 1) / kTtLines,
+                    2 * nz);
+    k_radon_tiles<<<grid, 256, smem, st>>>(tr, tc, N, p.d_views, (const int *)p.d_ovid,
+                                           p.n_ovid[0], p.n_ovid[1], R, out_am, out_ld, zo,
+                                           device_error_word());
+    RG_CK_LAUNCH("k_radon_tiles");
+    if (epi == kEpiRatio)
+        k_views_rows<kEpiRatio, false><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am, out_ld,
+                                                           y_am, y_ld, zo);
+    else if (epi == kEpiTransmission)
+        k_views_rows<kEpiTransmission, false><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am,
+                                                                  out_ld, y_am, y_ld, zo);
+    RG_CK_LAUNCH("k_views_rows (epilogue)");
+    return RG_OK;
 }
 
 }  // namespace rg

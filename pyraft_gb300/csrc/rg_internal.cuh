@@ -110,6 +110,11 @@ struct SSPlan {
     // windows fit st_bw entries (nblocks == 0: the direct kernels are used)
     void *d_blocks = nullptr;      // StBlock[nblocks], device
     int nblocks = 0, st_bw = 0;
+    // tile-driven Radon (radon_tma.cu): view indices grouped by orientation
+    // (rows first), device
+    void *d_ovid = nullptr;
+    int n_ovid[2] = {0, 0};
+    bool tt_ok = false;
 };
 
 // A block of the TMA-staged Radon: views [first, first + count) of a plan,
@@ -148,6 +153,12 @@ int launch_radon(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_
 // radon_tma.cu: view blocks of a plan (after its views are computed), and
 // the staged Radon over them (same arguments as launch_radon).
 int st_blocks_build(SSPlan &p, const View *hv);
+// Tile-driven Radon over plans of scattered views (same arguments).
+int tt_build(SSPlan &p, const View *hv);
+bool radon_tiles_usable(const SSPlan &p);
+int launch_radon_tiles(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
+                       float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,
+                       int nz, long long zp, long long zo, int epi);
 bool radon_tma_usable(const SSPlan &p);
 int launch_radon_tma(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
                      float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,

@@ -154,6 +154,7 @@ int ss_plan_build(SSPlan &p, const SSGeom &g, const int *views, int nv)
         RG_CK(cudaMemcpy(p.d_views, hv.data(), sizeof(View) * nv, cudaMemcpyHostToDevice));
         if ((rc = ensure_device_error_word())) return rc;
         if ((rc = st_blocks_build(p, hv.data()))) return rc;
+        if ((rc = tt_build(p, hv.data()))) return rc;
     }
     return RG_OK;
 }
@@ -165,6 +166,9 @@ void ss_plan_free(SSPlan &p)
     if (p.d_blocks) cudaFree(p.d_blocks);
     p.d_blocks = nullptr;
     p.nblocks = 0;
+    if (p.d_ovid) cudaFree(p.d_ovid);
+    p.d_ovid = nullptr;
+    p.tt_ok = false;
 }
 
 // ============================================================================
@@ -308,6 +312,8 @@ int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float 
     if (epi < 0) epi = y_am ? kEpiRatio : kEpiSum;
     if (radon_tma_usable(p))
         return launch_radon_tma(p, prow, pcol, out_am, out_ld, y_am, y_ld, st, nz, zp, zo, epi);
+    if (radon_tiles_usable(p))
+        return launch_radon_tiles(p, prow, pcol, out_am, out_ld, y_am, y_ld, st, nz, zp, zo, epi);
     const int N = p.g.N, R = p.g.R;
     if (radon_views_per_thread(p) == 2) {
         dim3 grid((R + 31) / 32, (p.nv + 7) / 8, nz);
