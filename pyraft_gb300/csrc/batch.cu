@@ -25,6 +25,8 @@
 // loads, no staging and no fusion; they compute the same operators as the
 // batched path (slant-stack Radon, matched adjoint) so both reconstruct the
 // same iterate.
+#include <string.h>
+
 #include <algorithm>
 #include <numeric>
 #include <vector>
@@ -43,10 +45,12 @@ struct BatchSlice {
     float2 *prow, *pcol;   // line pairs of the iterate
     float *x;              // iterate, N x N contiguous
     float *inv_sens;       // 1 / A_s^T 1 of this subset, N x N
-    int begin[4];          // first item of this slice in each work list
+    const int *ovid;       // tile-driven Radon: view indices by orientation
+    int n_rows, n_cols;
+    int begin[6];          // first item of this slice in each work list
 };
 
-enum { kLP = 0, kRadon = 1, kGather = 2, kEdges = 3 };
+enum { kLP = 0, kRadon = 1, kGather = 2, kEdges = 3, kTiles = 4, kRows = 5 };
 
 __device__ __forceinline__ int find_slice(const BatchSlice *__restrict__ d, int n, int item, int w)
 {
@@ -98,6 +102,57 @@ __global__ __launch_bounds__(128) void k_batch_radon(const BatchSlice *__restric
             radon_tile<kEpiRatio>(b.prow, b.pcol, b.N, b.views, b.nv, b.R, b.ratio_am, b.R, b.y_am,
                              b.R, local % rb, local / rb);
     }
+}
+
+// Tile-driven Radon of one subset for every slice (tt_views, ss_tiles.cuh):
+// items are slice x orientation x tile; a CTA stages the tile (kTtLines
+// lines x kTtWin line-pair entries, with zero pads) with plain loads -- one
+// staging serves every view of the subset with that orientation -- and adds
+// each crossing ray's partial to the slice's ratio buffer atomically.
+__global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restrict__ d, int n,
+                                                     int total, int *counter, int *err)
+{
+    extern __shared__ __align__(128) float2 tile[];   // [kTtLines][kTtRow]
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(tile);
+    for (;;) {
+        const int item = next_item(counter);          // its barriers also end the last item
+        if (item >= total) break;
+        const BatchSlice &b = d[find_slice(d, n, item, kTiles)];
+        const int local = item - b.begin[kTiles];
+        const int N = b.N, pitch = pairs_pitch(N);
+        const int tx = (pitch + kTtWin - 1) / kTtWin, ty = (N + kTtLines - 1) / kTtLines;
+        const int o = local / (tx * ty), rem = local - o * (tx * ty);
+        const int p0 = (rem % tx) * kTtWin, i0 = (rem / tx) * kTtLines;
+        const int nvo = o ? b.n_cols : b.n_rows;
+        if (nvo == 0) continue;                        // CTA-uniform
+        const float2 *__restrict__ src = o ? b.pcol : b.prow;
+        for (int e = threadIdx.x; e < kTtLines * kTtRow; e += blockDim.x) {
+            const int r = e / kTtRow, c = e - r * kTtRow;
+            const int ent = p0 + c - kTtPad, line = i0 + r;
+            float2 v = make_float2(0.f, 0.f);
+            if (c >= kTtPad && c < kTtPad + kTtWin && line < N && ent < pitch)
+                v = src[(size_t)line * pitch + ent];
+            tile[e] = v;
+        }
+        __syncthreads();
+        tt_views(sbase, p0, i0, b.views, b.ovid + (o ? b.n_rows : 0), nvo, b.R, b.ratio_am, b.R,
+                 err);
+    }
+}
+
+// The subset's rows of every slice's ratio buffer (one CTA per row): zeroed
+// before the tile-driven Radon, or turned into the EM ratio y / (A x)
+// (0 where A x == 0) after it.
+template <bool ZERO>
+__global__ __launch_bounds__(256) void k_batch_rows(const BatchSlice *__restrict__ d, int n)
+{
+    const int item = blockIdx.x;
+    const BatchSlice &b = d[find_slice(d, n, item, kRows)];
+    const int view = b.views[item - b.begin[kRows]].view;
+    float *__restrict__ o = b.ratio_am + (size_t)view * b.R;
+    const float *__restrict__ y = b.y_am + (size_t)view * b.R;
+    for (int k = threadIdx.x; k < b.R; k += blockDim.x)
+        o[k] = ZERO ? 0.f : radon_epilogue(kEpiRatio, o[k], y, k);
 }
 
 // MODE 1: adjoint with the EM update; MODE 2: FP64 sensitivity -> inv_sens.
@@ -160,8 +215,9 @@ int persistent_grid(K kernel, int threads, size_t smem, int items, int *out)
 
 struct BatchRun {
     int n = 0, S = 0, wmax = 64, vpt = 2;
-    int total[4][64] = {};            // [kind][subset] item counts (subset 0 for pairs)
-    int grid[4][64] = {};             // persistent grids: pairs, radon[s], gather1, gather2
+    bool tiles = false;               // tile-driven Radon (else the direct walks)
+    int total[6][64] = {};            // [kind][subset] item counts (subset 0 for pairs)
+    int grid[5][64] = {};             // persistent grids: pairs, radon[s], gather1, gather2, tiles
     BatchSlice *d_desc = nullptr;     // S x n descriptors (device, in scratch)
     int *counter = nullptr;
 };
@@ -172,6 +228,10 @@ int prepare_grids(BatchRun &br)
 {
     const size_t smem = (size_t)kSlots * WMAX * sizeof(float2);
     if (int rc = persistent_grid(k_batch_pairs, 256, 0, br.total[kLP][0], &br.grid[0][0])) return rc;
+    if (br.tiles)
+        if (int rc = persistent_grid(k_batch_tiles, 256, (size_t)kTtLines * kTtRow * 8,
+                                     br.total[kTiles][0], &br.grid[4][0]))
+            return rc;
     for (int s = 0; s < br.S; ++s)
         if (int rc = persistent_grid(br.vpt == 2 ? k_batch_radon<2> : k_batch_radon<1>, 128, 0,
                                      br.total[kRadon][s], &br.grid[1][s]))
@@ -192,14 +252,25 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
         RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
         k_batch_pairs<<<br.grid[0][0], 256, 0, st>>>(d, br.n, br.total[kLP][0], br.counter);
         RG_CK_LAUNCH("k_batch_pairs");
-        RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
-        if (br.vpt == 2)
-            k_batch_radon<2><<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s],
-                                                            br.counter);
-        else
-            k_batch_radon<1><<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s],
-                                                            br.counter);
-        RG_CK_LAUNCH("k_batch_radon");
+        if (br.tiles) {
+            k_batch_rows<true><<<br.total[kRows][s], 256, 0, st>>>(d, br.n);
+            RG_CK_LAUNCH("k_batch_rows (zero)");
+            RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
+            k_batch_tiles<<<br.grid[4][0], 256, (size_t)kTtLines * kTtRow * 8, st>>>(
+                d, br.n, br.total[kTiles][0], br.counter, device_error_word());
+            RG_CK_LAUNCH("k_batch_tiles");
+            k_batch_rows<false><<<br.total[kRows][s], 256, 0, st>>>(d, br.n);
+            RG_CK_LAUNCH("k_batch_rows (ratio)");
+        } else {
+            RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
+            if (br.vpt == 2)
+                k_batch_radon<2><<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s],
+                                                                br.counter);
+            else
+                k_batch_radon<1><<<br.grid[1][s], 128, 0, st>>>(d, br.n, br.total[kRadon][s],
+                                                                br.counter);
+            RG_CK_LAUNCH("k_batch_radon");
+        }
         RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
         k_batch_gather<1, WMAX><<<br.grid[2][0], 256, smem, st>>>(d, br.n, br.total[kGather][0],
                                                                   br.counter,
@@ -238,6 +309,8 @@ int set_smem_attrs()
                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     RG_CK(cudaFuncSetAttribute(k_batch_gather<2, WMAX>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    RG_CK(cudaFuncSetAttribute(k_batch_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kTtLines * kTtRow * 8));
     return RG_OK;
 }
 
@@ -442,6 +515,13 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
     // (RG_RADON_VIEWS=1|2 overrides)
     br.vpt = getenv("RG_RADON_VIEWS") ? radon_views_per_thread(*plans[0]) : 2;
     const int vpb = br.vpt == 2 ? 8 : 4;   // views per Radon item
+    // tile-driven Radon when every subset plan supports it (its pads cover
+    // the geometry); RG_RADON_KERNEL=direct keeps the direct walks
+    {
+        const char *e = getenv("RG_RADON_KERNEL");
+        br.tiles = !(e && !strcmp(e, "direct"));
+        for (const SSPlan *p : plans) br.tiles = br.tiles && p->tt_ok && p->d_ovid;
+    }
     br.wmax = wneed <= 64 ? 64 : wneed <= 128 ? 128 : wneed <= 256 ? 256 : 512;
     if (wneed > 512) return set_error(RG_EUNSUPPORTED, "gather window of %d exceeds 512", wneed);
 
@@ -452,8 +532,8 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
     br.counter = (int *)sc.take(sizeof(int));
     br.d_desc = (BatchSlice *)sc.take(sizeof(BatchSlice) * S * nslices);
     std::vector<BatchSlice> hd((size_t)S * nslices);
-    int items_lp = 0, items_g = 0, items_e = 0;
-    std::vector<int> items_r(S, 0);
+    int items_lp = 0, items_g = 0, items_e = 0, items_t = 0;
+    std::vector<int> items_r(S, 0), items_rows(S, 0);
     std::vector<float *> xs(nslices);
     for (int q = 0; q < nslices && !rc; ++q) {
         const int k = order[q];
@@ -489,15 +569,24 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
             d.begin[kRadon] = items_r[s];
             d.begin[kGather] = items_g;
             d.begin[kEdges] = items_e;
+            d.begin[kTiles] = items_t;
+            d.begin[kRows] = items_rows[s];
+            d.ovid = (const int *)p->d_ovid;
+            d.n_rows = p->n_ovid[0];
+            d.n_cols = p->n_ovid[1];
+            items_rows[s] += p->nv;
             items_r[s] += ((R + 31) / 32) * ((p->nv + vpb - 1) / vpb);
         }
         items_lp += tiles * tiles;
         items_g += tiles * tiles_y;
         items_e += 4 * N - 4;
+        items_t += 2 * ((pairs_pitch(N) + kTtWin - 1) / kTtWin) * ((N + kTtLines - 1) / kTtLines);
     }
     br.total[kLP][0] = items_lp;
     br.total[kGather][0] = items_g;
     br.total[kEdges][0] = items_e;
+    br.total[kTiles][0] = items_t;
+    for (int s = 0; s < S; ++s) br.total[kRows][s] = items_rows[s];
     for (int s = 0; s < S; ++s) br.total[kRadon][s] = items_r[s];
     if (!rc) {
         cudaError_t e = cudaMemcpyAsync(br.d_desc, hd.data(), sizeof(BatchSlice) * hd.size(),

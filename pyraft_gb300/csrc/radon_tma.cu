@@ -104,16 +104,6 @@ __device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *tm,
         : "memory");
 }
 
-template <int OFF>
-__device__ __forceinline__ float2 lds_pair_at(unsigned addr)
-{
-    float2 v;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];"
-                 : "=f"(v.x), "=f"(v.y)
-                 : "r"(addr), "n"(OFF));
-    return v;
-}
-
 // One full strip of a (ray, view): 16 lines, line r of the strip buffer at
 // byte offset r * BW * 8 (an immediate of the load).
 template <int BW, int R0>
@@ -531,21 +521,6 @@ int launch_radon_tma(const SSPlan &p, const float2 *prow, const float2 *pcol, fl
 // added to the sinogram with one atomic add (the zeroing pass before and
 // the epilogue pass after are separate launches); the order of those adds
 // varies between runs, at the level of FP32 rounding.
-constexpr int kTtLines = 32;                  // lines per tile
-constexpr int kTtWin = 160;                   // owned entries per tile row
-constexpr int kTtPad = 48;                    // zero entries on each side
-constexpr int kTtRow = kTtWin + 2 * kTtPad;   // smem row stride (entries): 2 KB
-
-template <int R0>
-__device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, float &part)
-{
-    if constexpr (R0 < kTtLines) {
-        const float2 pr = lds_pair_at<R0 * kTtRow * 8>(sb + ((L >> 23) << 3));
-        part += fmaf(frac_plus_one(L), pr.y, pr.x);
-        L += dq;
-        tt_walk<R0 + 1>(sb, L, dq, part);
-    }
-}
 
 __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUtensorMap tm_rows,
                                                      const __grid_constant__ CUtensorMap tm_cols,
@@ -591,44 +566,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
         return;
     }
 
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int i1 = i0 + kTtLines - 1;
-    // window samples [a, b): entry p0 holds sample p0 - 1
-    const double a = p0 - 1.0, b = p0 - 1.0 + kTtWin;
-    const long long base_q = (long long)(p0 - kTtPad - 1) << 32;   // smem index 0
-    for (int j = warp; j < nvo; j += 8) {
-        const View &v = views[vid[j]];
-        // rays whose positions on lines i0..i1 meet [a, b), +-1 ray of margin
-        const double rk = (double)v.rk * 2.3283064365386963e-10;
-        const double c0 = ((double)v.r0 + (double)i0 * (double)v.ri) * 2.3283064365386963e-10;
-        const double c1 = ((double)v.r0 + (double)i1 * (double)v.ri) * 2.3283064365386963e-10;
-        const double cmin = fmin(c0, c1), cmax = fmax(c0, c1);
-        double ka = (a - cmax) / rk, kb = (b - cmin) / rk;
-        if (ka > kb) { const double t = ka; ka = kb; kb = t; }
-        const int k_lo = max(0, (int)floor(fmin(fmax(ka, -1.0), (double)R)) - 1);
-        const int k_hi = min(R - 1, (int)ceil(fmax(fmin(kb, (double)R), -1.0)) + 1);
-        const unsigned dq = (unsigned)((v.ri + 256) >> 9);
-        const float delta = v.delta;
-        float *__restrict__ orow = out_am + (size_t)v.view * out_ld;
-        for (int k = k_lo + lane; k <= k_hi; k += 32) {
-            const long long u = v.r0 + (long long)k * v.rk + (long long)i0 * v.ri - base_q;
-            const long long ue = u + (long long)(kTtLines - 1) * v.ri;
-            // one entry of slack on both sides for the Q9.23 stepping
-            const long long lo_q = 1LL << 32, hi_q = (long long)(kTtRow - 1) << 32;
-            if (u < lo_q || u >= hi_q || ue < lo_q || ue >= hi_q) {
-                // a ray that crosses the window stays within the pads; this
-                // one does not cross it (margin ray), or the plan's pad check
-                // failed (flagged): it adds nothing here
-                if (err && u >= (long long)kTtPad << 32 && u < (long long)(kTtPad + kTtWin) << 32)
-                    atomicOr(err, 1);
-                continue;
-            }
-            unsigned L = (unsigned)(u >> 9);
-            float part = 0.f;
-            tt_walk<0>(sbase, L, dq, part);
-            if (part != 0.f) atomicAdd(orow + k, part * delta);
-        }
-    }
+    tt_views(sbase, p0, i0, views, vid, nvo, R, out_am, out_ld, err);
 }
 
 // out[view][k] = 0 (zeroing pass) or the epilogue of the summed rays, for
@@ -661,12 +599,12 @@ int tt_build(SSPlan &p, const View *hv)
                 ++p.n_ovid[o];
             }
     // pads must hold any crossing ray's positions on the tile's lines: the
-    // walk across the tile's lines plus the margin rays
+    // walk across the tile's lines plus the margin rays (two each side)
     double need = 0.0;
     for (int e = 0; e < nv; ++e) {
         const double ri = fabs((double)hv[e].ri) * 2.3283064365386963e-10;
         const double rk = fabs((double)hv[e].rk) * 2.3283064365386963e-10;
-        need = std::max(need, (kTtLines - 1) * ri + 2.0 * rk + 3.0);
+        need = std::max(need, (kTtLines - 1) * ri + 3.0 * rk + 3.0);
     }
     if (need > kTtPad) return RG_OK;
     RG_CK(cudaMalloc(&p.d_ovid, sizeof(int) * ids.size()));

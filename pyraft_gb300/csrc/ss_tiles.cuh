@@ -364,6 +364,110 @@ __device__ __forceinline__ void accumulate(float (&part)[ROWS], const float2 *__
     }
 }
 
+template <int OFF>
+__device__ __forceinline__ float2 lds_pair_at(unsigned addr)
+{
+    float2 v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];"
+                 : "=f"(v.x), "=f"(v.y)
+                 : "r"(addr), "n"(OFF));
+    return v;
+}
+
+constexpr int kTtLines = 32;                  // lines per tile
+constexpr int kTtWin = 160;                   // owned entries per tile row
+constexpr int kTtPad = 48;                    // zero entries on each side
+constexpr int kTtRow = kTtWin + 2 * kTtPad;   // smem row stride (entries): 2 KB
+
+template <int R0>
+__device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, float &part)
+{
+    if constexpr (R0 < kTtLines) {
+        const float2 pr = lds_pair_at<R0 * kTtRow * 8>(sb + ((L >> 23) << 3));
+        part += fmaf(frac_plus_one(L), pr.y, pr.x);
+        L += dq;
+        tt_walk<R0 + 1>(sb, L, dq, part);
+    }
+}
+
+// The views loop of the tile-driven Radon (radon_tma.cu, k_radon_tiles, and
+// the batched OSEM): the tile of kTtLines lines x kTtRow entries is staged
+// at shared address sbase (entry p0 - kTtPad at index 0, zero pads around
+// the window [p0, p0 + kTtWin)).  Views are taken in batches of up to 256:
+// thread t finds view t's rays that cross the window on lines
+// [i0, i0 + kTtLines) (FP32, two rays of margin; the exact int64 check below
+// drops rays that do not cross), the batch's 32-ray chunks are numbered by
+// a prefix sum, and the warps take chunks round robin, so the work spreads
+// evenly whatever the number of views and rays.  A lane walks its ray
+// across the tile's lines and adds partial * Delta to out_am[view][ray].
+// Must be reached by every thread of the CTA (it has barriers).
+constexpr int kTtBatch = 256;
+
+__device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
+                                         const View *__restrict__ views,
+                                         const int *__restrict__ vid, int nvo, int R,
+                                         float *__restrict__ out_am, int out_ld,
+                                         int *__restrict__ err)
+{
+    __shared__ int s_klo[kTtBatch], s_off[kTtBatch + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int i1 = i0 + kTtLines - 1;
+    const float a = p0 - 1.0f, b = p0 - 1.0f + kTtWin;     // window samples [a, b)
+    const long long base_q = (long long)(p0 - kTtPad - 1) << 32;   // smem index 0
+    const long long lo_q = 1LL << 32, hi_q = (long long)(kTtRow - 1) << 32;
+    for (int v0 = 0; v0 < nvo; v0 += kTtBatch) {
+        const int nb = min(kTtBatch, nvo - v0);
+        int nch = 0;
+        if ((int)threadIdx.x < nb) {
+            const View &v = views[vid[v0 + threadIdx.x]];
+            const float rk = (float)v.rk * 2.3283064365386963e-10f;
+            const float c0 = ((float)v.r0 + (float)i0 * (float)v.ri) * 2.3283064365386963e-10f;
+            const float c1 = ((float)v.r0 + (float)i1 * (float)v.ri) * 2.3283064365386963e-10f;
+            float ka = (a - fmaxf(c0, c1)) / rk, kb = (b - fminf(c0, c1)) / rk;
+            if (ka > kb) { const float t = ka; ka = kb; kb = t; }
+            const int klo = max(0, (int)floorf(fminf(fmaxf(ka, -2.f), R + 2.f)) - 2);
+            const int khi = min(R - 1, (int)ceilf(fmaxf(fminf(kb, R + 2.f), -2.f)) + 2);
+            s_klo[threadIdx.x] = klo;
+            nch = khi >= klo ? (khi - klo + 32) >> 5 : 0;
+        }
+        // exclusive prefix sum of the chunk counts (blockDim.x >= kTtBatch)
+        s_off[threadIdx.x + 1] = nch;
+        if (threadIdx.x == 0) s_off[0] = 0;
+        __syncthreads();
+        for (int d = 1; d < kTtBatch; d <<= 1) {
+            const int t = threadIdx.x + 1;
+            const int add = (t > d && t <= kTtBatch) ? s_off[t - d] : 0;
+            __syncthreads();
+            if (t <= kTtBatch) s_off[t] += add;
+            __syncthreads();
+        }
+        const int nchunks = s_off[nb];
+        int t = 0;                                      // view of the current chunk
+        for (int g = warp; g < nchunks; g += nw) {
+            while (s_off[t + 1] <= g) ++t;              // chunks grow, so t only advances
+            const View &v = views[vid[v0 + t]];
+            const int k = s_klo[t] + ((g - s_off[t]) << 5) + lane;
+            if (k >= R) continue;
+            const long long u = v.r0 + (long long)k * v.rk + (long long)i0 * v.ri - base_q;
+            const long long ue = u + (long long)(kTtLines - 1) * v.ri;
+            // a crossing ray stays inside the pads (one entry of slack for the
+            // Q9.23 stepping); others are margin rays, or (flagged) the plan's
+            // pad check failed: they add nothing here
+            if (u < lo_q || u >= hi_q || ue < lo_q || ue >= hi_q) {
+                if (err && u >= (long long)kTtPad << 32 && u < (long long)(kTtPad + kTtWin) << 32)
+                    atomicOr(err, 1);
+                continue;
+            }
+            unsigned L = (unsigned)(u >> 9);
+            const unsigned dq = (unsigned)((v.ri + 256) >> 9);
+            float part = 0.f;
+            tt_walk<0>(sbase, L, dq, part);
+            if (part != 0.f) atomicAdd(out_am + (size_t)v.view * out_ld + k, part * v.delta);
+        }
+        __syncthreads();                                // s_klo / s_off reused
+    }
+}
+
 // Edge pixel e (of 4N - 4: rows 0 and N-1, then columns 0 and N-1) of the
 // matched adjoint (MODE 1, optionally with the EM update) or of its
 // FP64-accumulated sensitivity (MODE 2), computed by one warp.  The image's
