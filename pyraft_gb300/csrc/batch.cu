@@ -106,13 +106,20 @@ __global__ __launch_bounds__(128) void k_batch_radon(const BatchSlice *__restric
 
 // Tile-driven Radon of one subset for every slice (tt_views, ss_tiles.cuh):
 // items are slice x orientation x tile; a CTA stages the tile (kTtLines
-// lines x kTtWin line-pair entries, with zero pads) with plain loads -- one
-// staging serves every view of the subset with that orientation -- and adds
-// each crossing ray's partial to the slice's ratio buffer atomically.
+// lines x kTtWin line-pair entries, with zero pads) -- one staging serves
+// every view of the subset with that orientation -- and adds each crossing
+// ray's partial to the slice's ratio buffer atomically.  The line pairs are
+// formed while staging, straight from the iterate x (N x N, row-major): an
+// image-row line reads consecutive floats of one row, an image-column line
+// reads a 32-column strip row by row, both coalesced.  Rows of the staged
+// tile are kTtRowB = kTtRow + 1 entries apart, so the column-strip staging
+// (consecutive threads on consecutive lines) hits distinct banks.
+constexpr int kTtRowB = kTtRow + 1;
+
 __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restrict__ d, int n,
                                                      int total, int *counter, int *err)
 {
-    extern __shared__ __align__(128) float2 tile[];   // [kTtLines][kTtRow]
+    extern __shared__ __align__(128) float2 tile[];   // [kTtLines][kTtRowB]
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(tile);
     for (;;) {
         const int item = next_item(counter);          // its barriers also end the last item
@@ -125,18 +132,24 @@ __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restric
         const int p0 = (rem % tx) * kTtWin, i0 = (rem / tx) * kTtLines;
         const int nvo = o ? b.n_cols : b.n_rows;
         if (nvo == 0) continue;                        // CTA-uniform
-        const float2 *__restrict__ src = o ? b.pcol : b.prow;
-        for (int e = threadIdx.x; e < kTtLines * kTtRow; e += blockDim.x) {
-            const int r = e / kTtRow, c = e - r * kTtRow;
-            const int ent = p0 + c - kTtPad, line = i0 + r;
+        const float *__restrict__ x = b.x;
+        for (int e = threadIdx.x; e < kTtLines * kTtRowB; e += blockDim.x) {
+            int r, c;
+            if (o == 0) { r = e / kTtRowB; c = e - r * kTtRowB; }    // along image rows
+            else { c = e / kTtLines; r = e - c * kTtLines; }         // across a column strip
+            const int line = i0 + r, smp = p0 + c - kTtPad - 1;    // sample of entry p0 + c - pad
             float2 v = make_float2(0.f, 0.f);
-            if (c >= kTtPad && c < kTtPad + kTtWin && line < N && ent < pitch)
-                v = src[(size_t)line * pitch + ent];
-            tile[e] = v;
+            if (c >= kTtPad && c < kTtPad + kTtWin && line < N && smp >= 0 && smp <= N - 2) {
+                const float s0 = o ? __ldg(x + (size_t)smp * N + line) : __ldg(x + (size_t)line * N + smp);
+                const float s1 = o ? __ldg(x + (size_t)(smp + 1) * N + line)
+                                   : __ldg(x + (size_t)line * N + smp + 1);
+                v = make_pair(s0, s1, true);
+            }
+            tile[r * kTtRowB + c] = v;
         }
         __syncthreads();
-        tt_views(sbase, p0, i0, b.views, b.ovid + (o ? b.n_rows : 0), nvo, b.R, b.ratio_am, b.R,
-                 err);
+        tt_views<kTtRowB>(sbase, p0, i0, b.views, b.ovid + (o ? b.n_rows : 0), nvo, b.R,
+                          b.ratio_am, b.R, err);
     }
 }
 
@@ -229,7 +242,7 @@ int prepare_grids(BatchRun &br)
     const size_t smem = (size_t)kSlots * WMAX * sizeof(float2);
     if (int rc = persistent_grid(k_batch_pairs, 256, 0, br.total[kLP][0], &br.grid[0][0])) return rc;
     if (br.tiles)
-        if (int rc = persistent_grid(k_batch_tiles, 256, (size_t)kTtLines * kTtRow * 8,
+        if (int rc = persistent_grid(k_batch_tiles, 256, (size_t)kTtLines * kTtRowB * 8,
                                      br.total[kTiles][0], &br.grid[4][0]))
             return rc;
     for (int s = 0; s < br.S; ++s)
@@ -249,14 +262,16 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
     const size_t smem = (size_t)kSlots * WMAX * sizeof(float2);
     for (int s = 0; s < br.S; ++s) {
         const BatchSlice *d = br.d_desc + (size_t)s * br.n;
-        RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
-        k_batch_pairs<<<br.grid[0][0], 256, 0, st>>>(d, br.n, br.total[kLP][0], br.counter);
-        RG_CK_LAUNCH("k_batch_pairs");
+        if (!br.tiles) {   // the tile-driven Radon forms its line pairs while staging
+            RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
+            k_batch_pairs<<<br.grid[0][0], 256, 0, st>>>(d, br.n, br.total[kLP][0], br.counter);
+            RG_CK_LAUNCH("k_batch_pairs");
+        }
         if (br.tiles) {
             k_batch_rows<true><<<br.total[kRows][s], 256, 0, st>>>(d, br.n);
             RG_CK_LAUNCH("k_batch_rows (zero)");
             RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
-            k_batch_tiles<<<br.grid[4][0], 256, (size_t)kTtLines * kTtRow * 8, st>>>(
+            k_batch_tiles<<<br.grid[4][0], 256, (size_t)kTtLines * kTtRowB * 8, st>>>(
                 d, br.n, br.total[kTiles][0], br.counter, device_error_word());
             RG_CK_LAUNCH("k_batch_tiles");
             k_batch_rows<false><<<br.total[kRows][s], 256, 0, st>>>(d, br.n);
@@ -310,7 +325,7 @@ int set_smem_attrs()
     RG_CK(cudaFuncSetAttribute(k_batch_gather<2, WMAX>,
                                cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     RG_CK(cudaFuncSetAttribute(k_batch_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               kTtLines * kTtRow * 8));
+                               kTtLines * kTtRowB * 8));
     return RG_OK;
 }
 

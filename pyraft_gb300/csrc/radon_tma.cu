@@ -566,7 +566,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
         return;
     }
 
-    tt_views(sbase, p0, i0, views, vid, nvo, R, out_am, out_ld, err);
+    tt_views<kTtRow>(sbase, p0, i0, views, vid, nvo, R, out_am, out_ld, err);
 }
 
 // out[view][k] = 0 (zeroing pass) or the epilogue of the summed rays, for

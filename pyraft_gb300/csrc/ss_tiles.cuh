@@ -379,14 +379,15 @@ constexpr int kTtWin = 160;                   // owned entries per tile row
 constexpr int kTtPad = 48;                    // zero entries on each side
 constexpr int kTtRow = kTtWin + 2 * kTtPad;   // smem row stride (entries): 2 KB
 
-template <int R0>
+// ROW: smem row stride of the staged tile in entries (>= kTtRow).
+template <int ROW, int R0>
 __device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, float &part)
 {
     if constexpr (R0 < kTtLines) {
-        const float2 pr = lds_pair_at<R0 * kTtRow * 8>(sb + ((L >> 23) << 3));
+        const float2 pr = lds_pair_at<R0 * ROW * 8>(sb + ((L >> 23) << 3));
         part += fmaf(frac_plus_one(L), pr.y, pr.x);
         L += dq;
-        tt_walk<R0 + 1>(sb, L, dq, part);
+        tt_walk<ROW, R0 + 1>(sb, L, dq, part);
     }
 }
 
@@ -403,6 +404,7 @@ __device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, f
 // Must be reached by every thread of the CTA (it has barriers).
 constexpr int kTtBatch = 256;
 
+template <int ROW>
 __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                                          const View *__restrict__ views,
                                          const int *__restrict__ vid, int nvo, int R,
@@ -461,7 +463,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             unsigned L = (unsigned)(u >> 9);
             const unsigned dq = (unsigned)((v.ri + 256) >> 9);
             float part = 0.f;
-            tt_walk<0>(sbase, L, dq, part);
+            tt_walk<ROW, 0>(sbase, L, dq, part);
             if (part != 0.f) atomicAdd(out_am + (size_t)v.view * out_ld + k, part * v.delta);
         }
         __syncthreads();                                // s_klo / s_off reused
