@@ -170,7 +170,8 @@ __global__ __launch_bounds__(256) void k_batch_rows(const BatchSlice *__restrict
 
 // MODE 1: adjoint with the EM update; MODE 2: FP64 sensitivity -> inv_sens.
 // Tiles are 32 columns x 8*kBatchRows rows.
-constexpr int kBatchRows = 8;
+// 16 rows per thread measured 2 % faster than 8 on the config-5 batch.
+constexpr int kBatchRows = 16;
 
 template <int MODE, int WMAX>
 __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restrict__ d, int n,

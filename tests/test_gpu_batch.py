@@ -2,8 +2,10 @@
 one-slice-per-call form.
 
 The batched path runs the same tile code as the one-slice path, so per slice
-it must agree with rg_em (OSEM) to FP32 rounding; against the FP64 oracle it
-is held to rel-L2 1e-4.  The plain form uses float positions and no
+it must agree with rg_em (OSEM) to FP32 rounding (1e-5: the tile-driven
+Radon adds its partial ray sums atomically, in an order that differs
+between runs and between the two paths, and the gather tiles may differ in
+height); against the FP64 oracle it is held to rel-L2 1e-4.  The plain form uses float positions and no
 compensated sums, so it is held to 1e-3."""
 import math
 
@@ -49,7 +51,7 @@ def test_batch_matches_per_slice_osem(slices, graph):
     for (n, r, a), s, o in zip(geo, sinos, out):
         ref = rg.osem(s, (n, n), it, S)
         assert o.shape == (n, n)
-        assert rel(o, ref) <= 1e-6
+        assert rel(o, ref) <= 1e-5
 
 
 def test_batch_vs_oracle(orc, slices):
