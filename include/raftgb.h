@@ -74,7 +74,8 @@ const char *rg_last_error(void);
 int rg_version(void);
 /* Error bits that kernels with in-kernel checks recorded on the current
  * device since the last call, then cleared (synchronises the device):
- * 1 = a staged Radon window check failed and its strip was skipped,
+ * 1 = a Radon window check failed (a TMA-staged strip, or a ray of the
+ *     tile-driven Radon, was skipped rather than read out of bounds),
  * 2 = a bounded wait for an asynchronous copy ran out.  0 = none; a
  * negative RG_E* code if the query itself failed.  No counterpart in the
  * reference, whose kernels have no such checks. */
