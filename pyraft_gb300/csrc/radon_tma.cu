@@ -585,6 +585,11 @@ __global__ __launch_bounds__(256) void k_views_rows(const View *__restrict__ vie
     else *o = radon_epilogue(EPI, *o, y_am, (size_t)view * y_ld + k);
 }
 
+bool tt_pads_fit(const SSPlan &p, int lines, int pad)
+{
+    return (lines - 1) * p.tt_ri_max + 3.0 * p.tt_rk_max + 3.0 <= pad;
+}
+
 int tt_build(SSPlan &p, const View *hv)
 {
     p.tt_ok = false;
@@ -600,13 +605,11 @@ int tt_build(SSPlan &p, const View *hv)
             }
     // pads must hold any crossing ray's positions on the tile's lines: the
     // walk across the tile's lines plus the margin rays (two each side)
-    double need = 0.0;
     for (int e = 0; e < nv; ++e) {
-        const double ri = fabs((double)hv[e].ri) * 2.3283064365386963e-10;
-        const double rk = fabs((double)hv[e].rk) * 2.3283064365386963e-10;
-        need = std::max(need, (kTtLines - 1) * ri + 3.0 * rk + 3.0);
+        p.tt_ri_max = std::max(p.tt_ri_max, fabs((double)hv[e].ri) * 2.3283064365386963e-10);
+        p.tt_rk_max = std::max(p.tt_rk_max, fabs((double)hv[e].rk) * 2.3283064365386963e-10);
     }
-    if (need > kTtPad) return RG_OK;
+    if (!tt_pads_fit(p, kTtLines, kTtPad)) return RG_OK;
     RG_CK(cudaMalloc(&p.d_ovid, sizeof(int) * ids.size()));
     RG_CK(cudaMemcpy(p.d_ovid, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice));
     p.tt_ok = true;

@@ -115,6 +115,7 @@ struct SSPlan {
     void *d_ovid = nullptr;
     int n_ovid[2] = {0, 0};
     bool tt_ok = false;
+    double tt_ri_max = 0.0, tt_rk_max = 0.0;   // max |ri|, |rk| over the views (samples)
 };
 
 // A block of the TMA-staged Radon: views [first, first + count) of a plan,
@@ -155,6 +156,9 @@ int launch_radon(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_
 int st_blocks_build(SSPlan &p, const View *hv);
 // Tile-driven Radon over plans of scattered views (same arguments).
 int tt_build(SSPlan &p, const View *hv);
+// Zero pads of `pad` entries hold every crossing ray's walk over `lines`
+// lines for this plan's views (with two margin rays each side).
+bool tt_pads_fit(const SSPlan &p, int lines, int pad);
 bool radon_tiles_usable(const SSPlan &p);
 int launch_radon_tiles(const SSPlan &p, const float2 *pairs_rows, const float2 *pairs_cols,
                        float *out_am, int out_ld, const float *y_am, int y_ld, cudaStream_t st,

@@ -379,15 +379,16 @@ constexpr int kTtWin = 160;                   // owned entries per tile row
 constexpr int kTtPad = 48;                    // zero entries on each side
 constexpr int kTtRow = kTtWin + 2 * kTtPad;   // smem row stride (entries): 2 KB
 
-// ROW: smem row stride of the staged tile in entries (>= kTtRow).
-template <int ROW, int R0>
+// ROW: smem row stride of the staged tile in entries (>= WIN + 2 PAD);
+// LINES: lines of the tile.
+template <int ROW, int LINES, int R0>
 __device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, float &part)
 {
-    if constexpr (R0 < kTtLines) {
+    if constexpr (R0 < LINES) {
         const float2 pr = lds_pair_at<R0 * ROW * 8>(sb + ((L >> 23) << 3));
         part += fmaf(frac_plus_one(L), pr.y, pr.x);
         L += dq;
-        tt_walk<ROW, R0 + 1>(sb, L, dq, part);
+        tt_walk<ROW, LINES, R0 + 1>(sb, L, dq, part);
     }
 }
 
@@ -404,7 +405,7 @@ __device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, f
 // Must be reached by every thread of the CTA (it has barriers).
 constexpr int kTtBatch = 256;
 
-template <int ROW>
+template <int ROW, int LINES = kTtLines, int PAD = kTtPad>
 __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                                          const View *__restrict__ views,
                                          const int *__restrict__ vid, int nvo, int R,
@@ -413,10 +414,10 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
 {
     __shared__ int s_klo[kTtBatch], s_off[kTtBatch + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const int i1 = i0 + kTtLines - 1;
+    const int i1 = i0 + LINES - 1;
     const float a = p0 - 1.0f, b = p0 - 1.0f + kTtWin;     // window samples [a, b)
-    const long long base_q = (long long)(p0 - kTtPad - 1) << 32;   // smem index 0
-    const long long lo_q = 1LL << 32, hi_q = (long long)(kTtRow - 1) << 32;
+    const long long base_q = (long long)(p0 - PAD - 1) << 32;      // smem index 0
+    const long long lo_q = 1LL << 32, hi_q = (long long)(kTtWin + 2 * PAD - 1) << 32;
     for (int v0 = 0; v0 < nvo; v0 += kTtBatch) {
         const int nb = min(kTtBatch, nvo - v0);
         int nch = 0;
@@ -451,19 +452,19 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             const int k = s_klo[t] + ((g - s_off[t]) << 5) + lane;
             if (k >= R) continue;
             const long long u = v.r0 + (long long)k * v.rk + (long long)i0 * v.ri - base_q;
-            const long long ue = u + (long long)(kTtLines - 1) * v.ri;
+            const long long ue = u + (long long)(LINES - 1) * v.ri;
             // a crossing ray stays inside the pads (one entry of slack for the
             // Q9.23 stepping); others are margin rays, or (flagged) the plan's
             // pad check failed: they add nothing here
             if (u < lo_q || u >= hi_q || ue < lo_q || ue >= hi_q) {
-                if (err && u >= (long long)kTtPad << 32 && u < (long long)(kTtPad + kTtWin) << 32)
+                if (err && u >= (long long)PAD << 32 && u < (long long)(PAD + kTtWin) << 32)
                     atomicOr(err, 1);
                 continue;
             }
             unsigned L = (unsigned)(u >> 9);
             const unsigned dq = (unsigned)((v.ri + 256) >> 9);
             float part = 0.f;
-            tt_walk<ROW, 0>(sbase, L, dq, part);
+            tt_walk<ROW, LINES, 0>(sbase, L, dq, part);
             if (part != 0.f) atomicAdd(out_am + (size_t)v.view * out_ld + k, part * v.delta);
         }
         __syncthreads();                                // s_klo / s_off reused
