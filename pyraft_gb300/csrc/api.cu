@@ -448,9 +448,9 @@ int rg_radon_slantstack_stack(rg_image phantom, long long phantom_stride, rg_ima
     if (!(rc = launch_line_pairs(phantom.data, phantom.column_stride, phantom.line_stride, N, prow,
                                  pcol, st, nstack, phantom_stride, zp)))
         rc = launch_radon(ph->p, prow, pcol, out_am, R, nullptr, 0, st, nstack, zp, zo);
-    for (int z = 0; z < nstack && !rc && !direct; ++z)
-        rc = launch_from_am(out_am + (size_t)z * R * A, R, A, radon.data + z * radon_stride,
-                            radon.column_stride, radon.line_stride, st);
+    if (!rc && !direct)
+        rc = launch_from_am(out_am, R, A, radon.data, radon.column_stride, radon.line_stride, st,
+                            nstack, (long long)R * A, radon_stride);
     scratch_end(s);
     return rc;
 }
@@ -481,9 +481,8 @@ int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg
     long long zs = sino_stride;
     if (!is_view_major(sino)) {
         float *t = (float *)s.take((size_t)R * A * sizeof(float) * nstack);
-        for (int z = 0; z < nstack && !rc; ++z)
-            rc = launch_to_am(sino.data + z * sino_stride, sino.column_stride, sino.line_stride, R,
-                              A, t + (size_t)z * R * A, st);
+        rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, t, st, nstack,
+                          sino_stride, (long long)R * A);
         s_am = t;
         zs = (long long)R * A;
     }
@@ -491,6 +490,10 @@ int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg
     zz.n = nstack;
     zz.in = zs;
     zz.out = image_stride;
+    // tile height tuned on the first slice (its output is rewritten below)
+    if (!rc)
+        rc = autotune_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
+                             st);
     if (!rc)
         rc = launch_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
                            nullptr, nullptr, nullptr, st, 0, zz);

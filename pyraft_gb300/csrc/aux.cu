@@ -14,10 +14,14 @@
 namespace rg {
 
 // out_am[j * R + k] = in[k * cs + j * ls]
+// blockIdx.z: one sinogram of a stack (zi, zo: strides in floats).
 __global__ __launch_bounds__(256) void k_to_am(const float *__restrict__ in, long long cs,
                                                long long ls, int R, int A,
-                                               float *__restrict__ out)
+                                               float *__restrict__ out, long long zi,
+                                               long long zo)
 {
+    in += blockIdx.z * zi;
+    out += blockIdx.z * zo;
     __shared__ float t[32][33];
     const int k0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -35,8 +39,10 @@ __global__ __launch_bounds__(256) void k_to_am(const float *__restrict__ in, lon
 // out[k * cs + j * ls] = am[j * R + k]
 __global__ __launch_bounds__(256) void k_from_am(const float *__restrict__ am, int R, int A,
                                                  float *__restrict__ out, long long cs,
-                                                 long long ls)
+                                                 long long ls, long long zi, long long zo)
 {
+    am += blockIdx.z * zi;
+    out += blockIdx.z * zo;
     __shared__ float t[32][33];
     const int k0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -52,19 +58,19 @@ __global__ __launch_bounds__(256) void k_from_am(const float *__restrict__ am, i
 }
 
 int launch_to_am(const float *in, long long cs, long long ls, int R, int A, float *out_am,
-                 cudaStream_t st)
+                 cudaStream_t st, int nz, long long zi, long long zo)
 {
-    dim3 grid((A + 31) / 32, (R + 31) / 32);
-    k_to_am<<<grid, 256, 0, st>>>(in, cs, ls, R, A, out_am);
+    dim3 grid((A + 31) / 32, (R + 31) / 32, nz);
+    k_to_am<<<grid, 256, 0, st>>>(in, cs, ls, R, A, out_am, zi, zo);
     RG_CK_LAUNCH("k_to_am");
     return RG_OK;
 }
 
 int launch_from_am(const float *am, int R, int A, float *out, long long cs, long long ls,
-                   cudaStream_t st)
+                   cudaStream_t st, int nz, long long zi, long long zo)
 {
-    dim3 grid((A + 31) / 32, (R + 31) / 32);
-    k_from_am<<<grid, 256, 0, st>>>(am, R, A, out, cs, ls);
+    dim3 grid((A + 31) / 32, (R + 31) / 32, nz);
+    k_from_am<<<grid, 256, 0, st>>>(am, R, A, out, cs, ls, zi, zo);
     RG_CK_LAUNCH("k_from_am");
     return RG_OK;
 }

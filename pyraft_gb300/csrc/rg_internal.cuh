@@ -199,10 +199,11 @@ int launch_radon_transpose_f64(const SSPlan &p, const double *sino, long long sc
                                double *img_c, cudaStream_t st);
 
 // aux.cu
+// nz > 1: a stack, consecutive inputs zi and outputs zo floats apart.
 int launch_to_am(const float *in, long long cs, long long ls, int R, int A, float *out_am,
-                 cudaStream_t st);
+                 cudaStream_t st, int nz = 1, long long zi = 0, long long zo = 0);
 int launch_from_am(const float *am, int R, int A, float *out, long long cs, long long ls,
-                   cudaStream_t st);
+                   cudaStream_t st, int nz = 1, long long zi = 0, long long zo = 0);
 int launch_copy2d(const float *in, long long ics, long long ils, float *out, long long ocs,
                   long long ols, int rows, int cols, cudaStream_t st);
 int launch_fill(float *p, size_t n, float v, cudaStream_t st);

@@ -495,6 +495,8 @@ __device__ __forceinline__ void adjoint_edge_pixel(const float *__restrict__ s_a
     else { row = e - (3 * N - 2) + 1; col = N - 1; }
     float acc = 0.f, comp = 0.f;
     double acc64 = 0.0;
+    // unrolled so that several views' loads are in flight per lane
+#pragma unroll 4
     for (int j = lane; j < nv; j += 32) {
         const View &v = views[j];
         const long long kap = v.k0 + (long long)row * v.krow + (long long)col * v.kcol;

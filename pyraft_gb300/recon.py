@@ -44,8 +44,8 @@ def tv_ls(sino, size, niter=200, lam=1e-3, lr=1e-2, eps=1e-3, x0=None,
         loss = 0.5 * (r * r).sum() + lam * total_variation(x, eps)
         loss.backward()
         opt.step()
-        losses.append(float(loss.detach()))
-    return x.detach(), losses
+        losses.append(loss.detach())       # kept on the device: no sync per step
+    return x.detach(), [float(v) for v in torch.stack(losses).cpu()] if losses else []
 
 
 def _em_segment(x, y, sens_inv, steps, size, R, A, ic, sc):
