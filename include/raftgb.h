@@ -286,6 +286,15 @@ int rg_em_plain_host(float *h_out, const float *h_sino, int size_image, int nray
  * raft/raft_radon_fromdesc.c:4).  desc: host (n x 6) row-major doubles
  * [alpha, a, b, x0, y0, theta]; results are ADDED into image / sino.         */
 int rg_phantom_fromdesc(rg_image image, const double *desc, int n, void *stream);
+
+/* Smoothed isotropic total variation of nslices contiguous size x size device
+ * images x: *value (device double) = sum sqrt(dx^2 + dy^2 + eps^2) with
+ * forward differences and the last row / column replicated; grad (device,
+ * same shape as x, or NULL) receives its gradient.  For TV-regularised
+ * reconstructions built on the operator pair; no counterpart in the
+ * reference.                                                                */
+int rg_tv(const float *x, int nslices, int size, float eps, double *value, float *grad,
+          void *stream);
 int rg_radon_fromdesc(rg_image sino, const double *desc, int n, void *stream);
 
 /* ----------------------------------------------------------------------

@@ -97,6 +97,7 @@ _SIGS = {
     "rg_osem_batch": ([_PI, _PI, _c_int, _c_int, _c_int, _c_int, _vp, _size_t, _vp], _c_int),
     "rg_em_plain_host": ([_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int], _c_int),
     "rg_phantom_fromdesc": ([_IMG, ctypes.POINTER(_c_double), _c_int, _vp], _c_int),
+    "rg_tv": ([_vp, _c_int, _c_int, ctypes.c_float, _vp, _vp, _vp], _c_int),
     "rg_radon_fromdesc": ([_IMG, ctypes.POINTER(_c_double), _c_int, _vp], _c_int),
     "rg_radon_slantstack_host": ([_vp, _vp, _c_int, _c_int, _c_int], _c_int),
     "rg_backprojection_slantstack_host": ([_vp, _vp, _c_int, _c_int, _c_int], _c_int),

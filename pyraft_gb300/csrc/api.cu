@@ -888,6 +888,17 @@ int rg_dda_trace(int lines, int columns, const double img_corners[4], const doub
     return rc;
 }
 
+// ---------------------------------------------------------------- TV
+int rg_tv(const float *x, int nslices, int size, float eps, double *value, float *grad,
+          void *stream)
+{
+    if (!x || !value) return set_error(RG_EINVAL, "rg_tv: null pointer");
+    if (nslices < 1 || nslices > 65535 || size < 1)
+        return set_error(RG_EINVAL, "rg_tv: need 1 <= nslices <= 65535 and size >= 1");
+    if (!(eps >= 0.f)) return set_error(RG_EINVAL, "rg_tv: eps must be >= 0");
+    return launch_tv(x, nslices, size, eps, value, grad, (cudaStream_t)stream);
+}
+
 // ---------------------------------------------------------------- phantoms
 int rg_phantom_fromdesc(rg_image image, const double *desc, int n, void *stream)
 {

@@ -251,4 +251,67 @@ int launch_invert(const float *sens, float *inv, size_t n, cudaStream_t st)
     return RG_OK;
 }
 
+
+// ----------------------------------------------------------------------------
+// Smoothed isotropic total variation of a stack of N x N images,
+// sum sqrt(dx^2 + dy^2 + eps^2) with forward differences and the last row /
+// column replicated (so its difference is identically 0), and its gradient.
+// One thread per pixel (32 x 8 per CTA, grid z = image): the pixel's own term
+// and those of its left and upper neighbours, whose differences it enters.
+// The value is summed per CTA in FP32 and across CTAs in FP64.
+__global__ __launch_bounds__(256) void k_tv(const float *__restrict__ x, int N, float eps,
+                                            double *__restrict__ value,
+                                            float *__restrict__ grad)
+{
+    const int j = blockIdx.x * 32 + (threadIdx.x & 31), i = blockIdx.y * 8 + (threadIdx.x >> 5);
+    const size_t off = (size_t)blockIdx.z * N * N;
+    x += off;
+    const float e2 = eps * eps;
+    float g = 0.f;
+    if (i < N && j < N) {
+        const float c = x[(size_t)i * N + j];
+        const float r = j + 1 < N ? x[(size_t)i * N + j + 1] : c;
+        const float d = i + 1 < N ? x[(size_t)(i + 1) * N + j] : c;
+        const float dx = r - c, dy = d - c;
+        g = sqrtf(dx * dx + dy * dy + e2);
+        if (grad) {
+            float gr = -(dx + dy) / g;
+            if (j >= 1) {                                 // left neighbour's dx = c - l
+                const float l = x[(size_t)i * N + j - 1];
+                const float ld = i + 1 < N ? x[(size_t)(i + 1) * N + j - 1] : l;
+                const float ax = c - l, ay = ld - l;
+                gr += ax / sqrtf(ax * ax + ay * ay + e2);
+            }
+            if (i >= 1) {                                 // upper neighbour's dy = c - u
+                const float u = x[(size_t)(i - 1) * N + j];
+                const float ur = j + 1 < N ? x[(size_t)(i - 1) * N + j + 1] : u;
+                const float bx = ur - u, by = c - u;
+                gr += by / sqrtf(bx * bx + by * by + e2);
+            }
+            grad[off + (size_t)i * N + j] = gr;
+        }
+    }
+    // CTA sum of the values
+    __shared__ float red[8];
+    float v = g;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < 8; ++w) t += red[w];
+        atomicAdd(value, (double)t);
+    }
+}
+
+int launch_tv(const float *x, int nz, int N, float eps, double *value, float *grad,
+              cudaStream_t st)
+{
+    RG_CK(cudaMemsetAsync(value, 0, sizeof(double), st));
+    dim3 grid((N + 31) / 32, (N + 7) / 8, nz);
+    k_tv<<<grid, 256, 0, st>>>(x, N, eps, value, grad);
+    RG_CK_LAUNCH("k_tv");
+    return RG_OK;
+}
+
 }  // namespace rg

@@ -207,6 +207,10 @@ int launch_from_am(const float *am, int R, int A, float *out, long long cs, long
 int launch_copy2d(const float *in, long long ics, long long ils, float *out, long long ocs,
                   long long ols, int rows, int cols, cudaStream_t st);
 int launch_fill(float *p, size_t n, float v, cudaStream_t st);
+// Smoothed isotropic TV of nz contiguous N x N images into *value (device
+// FP64, zeroed first) and, if grad != nullptr, its gradient.
+int launch_tv(const float *x, int nz, int N, float eps, double *value, float *grad,
+              cudaStream_t st);
 int launch_phantom(float *img, long long cs, long long ls, int lines, int cols,
                    double tl_x, double tl_y, double br_x, double br_y,
                    const double *d_desc, int n, cudaStream_t st);

@@ -2,8 +2,8 @@
 
 * ``tv_ls``: total-variation regularised least squares,
   min_x 0.5 ||R x - y||^2 + lam * sum sqrt(|grad x|^2 + eps^2), solved with
-  Adam; R and its gradient (the matched adjoint) are the library's kernels,
-  the TV term and the optimiser are PyTorch ops on the image stack.
+  Adam; R and its gradient (the matched adjoint) and the TV value and
+  gradient are the library's kernels, the optimiser PyTorch's Adam.
 * ``unrolled_em``: MLEM x <- x * A^T(y / A x) / A^T 1 written with the
   differentiable operator pair, so gradients flow through all iterations
   (e.g. with respect to the data); the iterations are checkpointed in
@@ -17,12 +17,44 @@ from __future__ import annotations
 import torch
 import torch.utils.checkpoint as cp
 
+from . import _native
 from .autograd import IMG, SINO, adjoint, radon
 
 
+class _TV(torch.autograd.Function):
+    """TV value and gradient from one fused kernel (rg_tv); the gradient is
+    computed with the value and kept for backward."""
+
+    @staticmethod
+    def forward(ctx, x, eps):
+        L = _native.load()
+        xc = x.detach().float().contiguous()
+        n = xc.shape[-1]
+        value = torch.empty((), dtype=torch.float64, device=xc.device)
+        grad = torch.empty_like(xc)
+        _native.check(L.rg_tv(xc.data_ptr(), xc.numel() // (n * n), n, float(eps),
+                              value.data_ptr(), grad.data_ptr(),
+                              torch.cuda.current_stream(xc.device).cuda_stream))
+        ctx.save_for_backward(grad)
+        return value.to(x.dtype)
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return g * grad, None
+
+
 def total_variation(x, eps):
-    """Smoothed isotropic TV of (..., N, N) images (forward differences,
-    replicated last row / column)."""
+    """Smoothed isotropic TV of (..., N, N) images, sum sqrt(dx^2 + dy^2 +
+    eps^2) with forward differences and the last row / column replicated;
+    differentiable, value and gradient from the library's fused kernel."""
+    if x.shape[-1] != x.shape[-2]:
+        raise ValueError("total_variation expects square images")
+    return _TV.apply(x, eps)
+
+
+def total_variation_reference(x, eps):
+    """The same TV written with PyTorch ops (for testing the fused kernel)."""
     dx = torch.diff(x, dim=-1, append=x[..., -1:])
     dy = torch.diff(x, dim=-2, append=x[..., -1:, :])
     return torch.sqrt(dx * dx + dy * dy + eps * eps).sum()
