@@ -268,11 +268,13 @@ static bool is_view_major(const rg_image &s)
 // ----------------------------------------------------------------------------
 // Autotuner for the gather tile height (rows per thread: 4 -> 32x32 tiles,
 // 8 -> 32x64 tiles, 16 -> 32x128 tiles).  The first out-of-place backprojection or adjoint of a
-// geometry times both variants on the caller's own buffers (two timed runs
-// each, CUDA events on the caller's stream; this first call synchronises)
-// and keeps the faster one for the process.  Calls made while the stream
-// is being captured never tune; they use the cached choice or 4.  The
-// environment variable RG_GATHER_ROWS=4|8|16 forces a choice.
+// geometry times the three variants on the caller's own buffers (two timed
+// runs each, CUDA events on the caller's stream; this first call
+// synchronises) and keeps the fastest for the process.  Calls that never
+// tune (inside a stream capture, the EM drivers' fused-update gathers) use
+// the cached choice, or a default by image size: 16 rows from N = 512 up
+// (the measured best on GB300 at 512^2, 1024^2 and 2048^2), 8 from 128, else
+// 4.  The environment variable RG_GATHER_ROWS=4|8|16 forces a choice.
 
 static std::mutex g_tune_mu;
 static std::map<std::string, int> g_tune;
@@ -298,7 +300,8 @@ int tuned_rows(const SSPlan &p, int mode)
     if (int v = env_rows()) return v;
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tune.find(tune_key(p, mode));
-    return it == g_tune.end() ? 4 : it->second;
+    if (it != g_tune.end()) return it->second;
+    return p.g.N >= 512 ? 16 : p.g.N >= 128 ? 8 : 4;
 }
 
 static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
