@@ -2,11 +2,19 @@
 //
 // Batched form (rg_osem_batch).  Many independent slices, each with its own
 // image size N, view count A and rays R, run OSEM with interleaved subsets.
-// One OSEM sub-iteration of ALL slices is three persistent launches:
-//   1. line pairs of every slice's iterate          (items: slice x 32^2 tile)
-//   2. Radon + EM ratio over the subset's views     (items: slice x 4 views x 32 rays)
-//   3. matched adjoint + EM update                   (items: slice x 32^2 tile)
-// Each launch sizes its grid to the resident-CTA capacity of the GPU; every
+// One OSEM sub-iteration of ALL slices is, with the tile-driven Radon (the
+// default):
+//   1. zero the subset's rows of every slice's ratio buffer  (one CTA per row)
+//   2. tile-driven Radon, line pairs formed while staging    (items: slice x
+//      orientation x image tile of 16 lines x 160 entries)
+//   3. ratio y / (A x) of those rows                          (one CTA per row)
+//   4. matched adjoint + EM update                            (items: slice x
+//      tile of 32 x 128 pixels)
+//   5. the adjoint's edge pixels                              (one warp each)
+// and, with the direct walks (RG_RADON_KERNEL=direct, or a geometry whose
+// pads do not fit), line pairs of every iterate, then a Radon with the ratio
+// fused (items: slice x 8 views x 32 rays), then steps 4 and 5.
+// Persistent launches size their grid to the resident-CTA capacity of the GPU; every
 // CTA pulls work items from one atomic counter until the list is exhausted,
 // so slices of very different cost share the SMs without tail effects.
 // Slices are ordered by decreasing cost, so the largest items are taken
