@@ -187,7 +187,8 @@ static int get_plan(const SSGeom &g, int stride, int first, std::shared_ptr<Plan
 
 struct DevTable {
     void *p = nullptr;
-    float h0 = 0.f;   // Ram-Lak centre tap (filter tables only)
+    float h0 = 0.f;   // Ram-Lak centre tap, or the FFT filter's DC gain / 2^fft_p
+    int fft_p = 0;    // Ram-Lak by FFT of size 2^fft_p (0: spatial taps)
     ~DevTable() { if (p) cudaFree(p); }
 };
 static Cache<DevTable> g_tables;
@@ -205,6 +206,27 @@ static int get_table(const std::string &key, const void *host, size_t bytes,
     auto t = std::make_shared<DevTable>();
     RG_CK(cudaMalloc(&t->p, bytes));
     RG_CK(cudaMemcpy(t->p, host, bytes, cudaMemcpyHostToDevice));
+    g_tables.put(kb.s, t);
+    out = t;
+    return RG_OK;
+}
+
+// Device copy of a host table that `fill(bytes, h0, fft_p)` builds only when
+// the key is not cached yet (for tables that are costly to compute).
+template <class F>
+static int get_table_lazy(const std::string &key, F fill, std::shared_ptr<DevTable> &out)
+{
+    KeyBuilder kb;
+    kb.add(current_device());
+    kb.s += key;
+    std::lock_guard<std::mutex> lock(g_tables.mu);
+    out = g_tables.find(kb.s);
+    if (out) return RG_OK;
+    auto t = std::make_shared<DevTable>();
+    std::vector<unsigned char> host;
+    fill(host, t->h0, t->fft_p);
+    RG_CK(cudaMalloc(&t->p, host.size()));
+    RG_CK(cudaMemcpy(t->p, host.data(), host.size(), cudaMemcpyHostToDevice));
     g_tables.put(kb.s, t);
     out = t;
     return RG_OK;
@@ -597,6 +619,53 @@ int rg_radon_transpose_slantstack(rg_image sino, rg_image img, void *ws, size_t 
 }
 
 // ---------------------------------------------------------------- filters
+// Ram-Lak by FFT for transforms of up to 2^kRamlakFftMaxLog points;
+// RG_RAMLAK=direct selects the spatial kernel.
+static bool ramlak_use_fft(int R)
+{
+    const char *e = getenv("RG_RAMLAK");
+    if (e && !strcmp(e, "direct")) return false;
+    return 2 * (long long)R - 1 <= (1LL << kRamlakFftMaxLog);
+}
+
+// Tables of launch_ramlak_fft for R rays at spacing dt: twiddles, then the
+// difference-domain filter G'[k] = G[k] / (M (1 - e^{-2 pi i k / M})) in
+// bit-reversed order (G'[0] = 0), all from FP64; g0 = G[0] / M.  G is the
+// DFT of the Ram-Lak taps dt h[m], |m| < R, wrapped to length M (real, as
+// the taps are even): G[k] = dt h[0] + 2 sum_{odd m < R} dt h[m] cos(2 pi k m / M).
+static void ramlak_fft_tables(int R, double dt, std::vector<unsigned char> &bytes, float &g0,
+                              int &p)
+{
+    const double pi = 3.14159265358979323846;
+    p = 2;
+    while ((1LL << p) < 2 * (long long)R - 1) ++p;
+    const int M = 1 << p, H = M / 2;
+    std::vector<double> ctab(M);
+    for (int i = 0; i < M; ++i) ctab[i] = cos(2.0 * pi * i / M);
+    std::vector<double> G(M), inv_m2((size_t)R / 2 + 1);
+    for (int m = 1; m < R; m += 2) inv_m2[m / 2] = 1.0 / ((double)m * (double)m);
+    const double h0 = dt / (4.0 * dt * dt);
+    for (int k = 0; k < M; ++k) {
+        double acc = 0.0;
+        for (int m = 1; m < R; m += 2)
+            acc += ctab[(size_t)((long long)k * m & (M - 1))] * inv_m2[m / 2];
+        G[k] = h0 - 2.0 * acc / (pi * pi * dt);
+    }
+    bytes.assign(sizeof(float2) * ((size_t)H + M), 0);
+    float2 *tw = reinterpret_cast<float2 *>(bytes.data());
+    float2 *gb = tw + H;
+    for (int i = 0; i < H; ++i) tw[i] = make_float2((float)cos(2.0 * pi * i / M), (float)-sin(2.0 * pi * i / M));
+    for (int k = 0; k < M; ++k) {
+        int r = 0;
+        for (int b = 0; b < p; ++b) r |= ((k >> b) & 1) << (p - 1 - b);
+        if (r == 0) { gb[k] = make_float2(0.f, 0.f); continue; }
+        // 1 / (1 - e^{-i th}) = (1 - i cot(th / 2)) / 2, th = 2 pi r / M
+        const double half = G[r] / (2.0 * M), a = pi * r / M;
+        gb[k] = make_float2((float)half, (float)(-half * cos(a) / sin(a)));
+    }
+    g0 = (float)(G[0] / M);
+}
+
 static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable> &out)
 {
     const int R = sino.lines;
@@ -605,50 +674,61 @@ static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable>
     if (!(std::isfinite(dt)) || dt == 0.0) return set_error(RG_EINVAL, "degenerate t extent");
     KeyBuilder kb;
     kb.add(kind).add(R).add(tmin).add(tmax);
-    std::vector<float> taps(2 * (size_t)R - 1);
+    const double pi = 3.14159265358979323846;
+    if (kind == RG_FILTER_RAMLAK && ramlak_use_fft(R)) {
+        return get_table_lazy("rlfft" + kb.s, [&](std::vector<unsigned char> &b, float &h0, int &p) {
+            ramlak_fft_tables(R, dt, b, h0, p);
+        }, out);
+    }
     if (kind == RG_FILTER_RAMLAK) {
         // Odd taps godd[q] = dt h[2q - 2R + 1], q in [0, 2R), then dt h[0]
         // (the layout k_ramlak_rows reads).
-        const double pi = 3.14159265358979323846;
-        taps.assign(2 * (size_t)R + 1, 0.f);
-        for (int q = 0; q < 2 * R; ++q) {
-            const int m = 2 * q - 2 * R + 1;
-            if (m >= -(R - 1) && m <= R - 1)
-                taps[q] = (float)(-dt / (pi * pi * (double)m * (double)m * dt * dt));
-        }
-        taps[2 * (size_t)R] = (float)(dt / (4.0 * dt * dt));
-    } else if (kind == RG_FILTER_LOWPASS) {
+        return get_table_lazy("taps" + kb.s, [&](std::vector<unsigned char> &b, float &h0, int &) {
+            b.assign(sizeof(float) * (2 * (size_t)R + 1), 0);
+            float *taps = reinterpret_cast<float *>(b.data());
+            for (int q = 0; q < 2 * R; ++q) {
+                const int m = 2 * q - 2 * R + 1;
+                if (m >= -(R - 1) && m <= R - 1)
+                    taps[q] = (float)(-dt / (pi * pi * (double)m * (double)m * dt * dt));
+            }
+            taps[2 * (size_t)R] = (float)(dt / (4.0 * dt * dt));
+            h0 = taps[2 * (size_t)R];
+        }, out);
+    }
+    if (kind == RG_FILTER_LOWPASS) {
         // g = Re(ifft(fftshift(|w| cos(pi w dt)))), w = linspace(-wc, wc, R), wc = 1/(2 dt):
         // applying g by circular convolution equals the FFT filter of
         // pyraft/filters/filters.py:13-68 (real part of the filtered data).
-        const double pi = 3.14159265358979323846;
-        const double wc = 1.0 / (2.0 * dt);
-        std::vector<double> h(R), G(R), g(R), ctab(R);
-        const double step = (R > 1) ? (2.0 * wc) / (R - 1) : 0.0;
-        for (int i = 0; i < R; ++i) {
-            double w = (i == R - 1) ? wc : -wc + i * step;
-            h[i] = fabs(w) * cos(pi * w * dt);
-        }
-        const int sh = R / 2;              // fftshift: G[k] = h[(k + R/2) mod R]... numpy
-        for (int k = 0; k < R; ++k) G[k] = h[(k + (R - sh)) % R];
-        for (int k = 0; k < R; ++k) ctab[k] = cos(2.0 * pi * (double)k / (double)R);
-        for (int m = 0; m < R; ++m) {
-            double acc = 0.0;
-            for (int k = 0; k < R; ++k) acc += G[k] * ctab[(size_t)k * m % R];
-            g[m] = acc / R;
-        }
-        for (int m = -(R - 1); m <= R - 1; ++m) taps[m + R - 1] = (float)g[((m % R) + R) % R];
-    } else {
-        return set_error(RG_EINVAL, "unknown filter kind %d", kind);
+        return get_table_lazy("taps" + kb.s, [&](std::vector<unsigned char> &b, float &, int &) {
+            const double wc = 1.0 / (2.0 * dt);
+            std::vector<double> h(R), G(R), g(R), ctab(R);
+            const double step = (R > 1) ? (2.0 * wc) / (R - 1) : 0.0;
+            for (int i = 0; i < R; ++i) {
+                double w = (i == R - 1) ? wc : -wc + i * step;
+                h[i] = fabs(w) * cos(pi * w * dt);
+            }
+            const int sh = R / 2;          // fftshift: G[k] = h[(k + R/2) mod R]... numpy
+            for (int k = 0; k < R; ++k) G[k] = h[(k + (R - sh)) % R];
+            for (int k = 0; k < R; ++k) ctab[k] = cos(2.0 * pi * (double)k / (double)R);
+            for (int m = 0; m < R; ++m) {
+                double acc = 0.0;
+                for (int k = 0; k < R; ++k) acc += G[k] * ctab[(size_t)k * m % R];
+                g[m] = acc / R;
+            }
+            b.assign(sizeof(float) * (2 * (size_t)R - 1), 0);
+            float *taps = reinterpret_cast<float *>(b.data());
+            for (int m = -(R - 1); m <= R - 1; ++m) taps[m + R - 1] = (float)g[((m % R) + R) % R];
+        }, out);
     }
-    int rc = get_table(std::string("taps") + kb.s, taps.data(), taps.size() * sizeof(float), out);
-    if (!rc && kind == RG_FILTER_RAMLAK) out->h0 = taps.back();
-    return rc;
+    return set_error(RG_EINVAL, "unknown filter kind %d", kind);
 }
 
 static int filter_rows(int kind, const float *in_am, float *out_am, int R, int A,
                        const std::shared_ptr<DevTable> &taps, cudaStream_t st)
 {
+    if (kind == RG_FILTER_RAMLAK && taps->fft_p)
+        return launch_ramlak_fft(in_am, out_am, R, A, taps->fft_p, (const float2 *)taps->p,
+                                 taps->h0, st);
     if (kind == RG_FILTER_RAMLAK)     // odd taps + centre tap (parity-split kernel)
         return launch_ramlak_rows(in_am, out_am, R, A, (const float *)taps->p, taps->h0, st);
     return launch_conv_rows(in_am, out_am, R, A, (const float *)taps->p, st);

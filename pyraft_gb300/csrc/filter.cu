@@ -1,4 +1,4 @@
-// filter.cu -- the FBP filter step as a row-wise spatial convolution.
+// filter.cu -- the FBP filter step as a row-wise convolution.
 //
 // out_am[a][n] = sum_{k=0}^{R-1} taps[n - k + R - 1] * in_am[a][k] for every
 // view a of a view-major sinogram (rows of length R).  The 2R-1 taps are
@@ -6,6 +6,11 @@
 // convolution, or the periodised spatial form of pyraft's lowpassino_fbp
 // filter (pyraft/filters/filters.py:13-68) for circular convolution.
 //
+// Kernels: k_conv_rows (any taps, direct sums), k_ramlak_rows (Ram-Lak,
+// direct sums over its odd taps) and k_ramlak_fft (Ram-Lak by FFT, the
+// default up to 8192 rays: O(R log R) per view and more accurate).
+//
+// k_conv_rows:
 // CTA = 256 outputs x 16 views.  The input is walked in tiles of 256
 // samples: the tile (16 views, stored [k][view] so one LDS.128 feeds four
 // FFMAs) and the 511 taps it meets are staged in shared memory; each thread
@@ -199,6 +204,292 @@ int launch_ramlak_rows(const float *in_am, float *out_am, int R, int A, const fl
     dim3 grid((R + kRN - 1) / kRN, (A + kRA - 1) / kRA);
     k_ramlak_rows<<<grid, 256, 0, st>>>(in_am, out_am, R, A, d_godd, h0);
     RG_CK_LAUNCH("k_ramlak_rows");
+    return RG_OK;
+}
+
+// ----------------------------------------------------------------------------
+// Ram-Lak by FFT: the same linear convolution, through a circular one of
+// length M = 2^p >= 2R - 1 (outputs [0, R) see no wrap-around).
+//
+// Two views per CTA, packed as one complex signal v = x + i y: the filter's
+// impulse response is real, so the real and imaginary parts of the result
+// are the two filtered views.
+//
+// Accuracy: the FFT's rounding error scales with the norm of what it
+// transforms, while Ram-Lak all but removes the low frequencies that carry
+// most of a sinogram's norm.  So the kernel transforms the first difference
+// D[n] = v[n] - v[n-1] (v zero outside [0, R)) and applies G'[k] =
+// G[k] / (M (1 - e^{-2 pi i k / M})) for k != 0, with G the filter's DFT;
+// the DC term G[0] sum(v) / M is added at the end.  On FP32 inputs this
+// keeps the result within a few 1e-7 (relative L2) of the FP64 convolution
+// even for smooth profiles, where transforming v itself loses 1e-5.
+//
+// Ordering: a decimation-in-frequency forward pass (natural order in,
+// bit-reversed out), the filter applied in bit-reversed order (G' is stored
+// that way), and a decimation-in-time inverse pass (bit-reversed in,
+// natural out), so no permutation pass is needed.
+//
+// Passes over shared memory: the first forward stage (span M/2) is fused
+// with the load and the last inverse stage with the store.  The other
+// radix-2 stages run in registers, up to four consecutive stages per pass:
+// a thread takes the 2^nst entries base + k q (q = the pass's smallest
+// span) that those stages combine, and writes them back in place.  The
+// forward stages of spans 4, 2, 1, the filter and the inverse stages of
+// spans 1, 2, 4 touch the same eight contiguous entries and form one pass.
+// So M = 4096 takes 6 passes, not 22.  Entry i lives at i + i/16 (one pad
+// per 16) so that strided groups and contiguous blocks spread over banks.
+//
+// Tables (host-computed in FP64): tw[t] = e^{-2 pi i t / M}, t < M/2, then
+// gb[k] = G'[bitrev_p(k)], k < M; g0 = G[0] / M.
+constexpr int kFftThreads = 256;
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 w)
+{
+    return make_float2(fmaf(a.x, w.x, -a.y * w.y), fmaf(a.x, w.y, a.y * w.x));
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 w)   // a * conj(w)
+{
+    return make_float2(fmaf(a.x, w.x, a.y * w.y), fmaf(a.y, w.x, -a.x * w.y));
+}
+__device__ __forceinline__ int fpad(int i) { return i + (i >> 4); }
+
+// e^{-i pi e / 8}, e in [0, 16): the roots of unity of order <= 16.
+__device__ __forceinline__ float2 root16(int e)
+{
+    constexpr float c[5] = {1.0f, 0.92387953251128674f, 0.70710678118654752f,
+                            0.38268343236508979f, 0.0f};
+    const int q = e & 7;
+    const float cs = q <= 4 ? c[q] : -c[8 - q];     // cos(pi q / 8)
+    const float sn = q <= 4 ? c[4 - q] : c[q - 4];  // sin(pi q / 8)
+    return e < 8 ? make_float2(cs, -sn) : make_float2(-cs, sn);
+}
+
+// w * e^{-i pi kl / d} (kl < d <= 8, both compile-time after unrolling).
+__device__ __forceinline__ float2 rot(float2 w, int kl, int d)
+{
+    if (kl == 0) return w;
+    const int e = kl * (8 / d);
+    if (e == 4) return make_float2(w.y, -w.x);      // times -i
+    return cmul(w, root16(e));
+}
+
+// Forward stages of spans 2^lt, 2^(lt-1), ..., 2^(lt-NST+1).  In the stage
+// of span h = d q (d = 2^(NST-1-s) in entries of the group), butterfly
+// (k, k + d) has twiddle index (r + kl q) (M / 2h), r = g mod q, kl = k mod
+// d: one table value W^{r M / 2h} times the constant e^{-i pi kl / d}.
+template <int NST>
+__device__ __forceinline__ void fft_fwd_pass(float2 *z, int p, int lt,
+                                             const float2 *__restrict__ tw)
+{
+    constexpr int K = 1 << NST;
+    const int lq = lt - NST + 1, q = 1 << lq;
+    for (int g = threadIdx.x; g < (1 << (p - NST)); g += kFftThreads) {
+        const int r = g & (q - 1);
+        const int base = ((g >> lq) << (lt + 1)) + r;
+        float2 v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = z[fpad(base + k * q)];
+#pragma unroll
+        for (int s = 0; s < NST; ++s) {
+            const int d = 1 << (NST - 1 - s);
+            const float2 w0 = __ldg(tw + (r << (p - 1 - (lt - s))));
+#pragma unroll
+            for (int kl = 0; kl < d; ++kl) {
+                const float2 w = rot(w0, kl, d);
+#pragma unroll
+                for (int k = kl; k < K; k += 2 * d) {
+                    const float2 a = v[k], c = v[k + d];
+                    v[k] = cadd(a, c);
+                    v[k + d] = cmul(csub(a, c), w);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) z[fpad(base + k * q)] = v[k];
+    }
+}
+
+// Inverse stages of spans 2^lb, ..., 2^(lb+NST-1) (conjugate twiddles).
+template <int NST>
+__device__ __forceinline__ void fft_inv_pass(float2 *z, int p, int lb,
+                                             const float2 *__restrict__ tw)
+{
+    constexpr int K = 1 << NST;
+    const int q = 1 << lb;
+    for (int g = threadIdx.x; g < (1 << (p - NST)); g += kFftThreads) {
+        const int r = g & (q - 1);
+        const int base = ((g >> lb) << (lb + NST)) + r;
+        float2 v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = z[fpad(base + k * q)];
+#pragma unroll
+        for (int s = 0; s < NST; ++s) {
+            const int d = 1 << s;
+            const float2 w0 = __ldg(tw + (r << (p - 1 - (lb + s))));
+#pragma unroll
+            for (int kl = 0; kl < d; ++kl) {
+                const float2 w = rot(w0, kl, d);
+#pragma unroll
+                for (int k = kl; k < K; k += 2 * d) {
+                    const float2 a = v[k], c = cmulc(v[k + d], w);
+                    v[k] = cadd(a, c);
+                    v[k + d] = csub(a, c);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) z[fpad(base + k * q)] = v[k];
+    }
+}
+
+// Forward stages of spans 2^(NM-1) .. 1, the filter, inverse stages of
+// spans 1 .. 2^(NM-1), on blocks of 2^NM contiguous entries (r = 0: the
+// twiddles are the constants e^{-i pi kl / d}).
+template <int NM>
+__device__ __forceinline__ void fft_mid_pass(float2 *z, int p, const float2 *__restrict__ gb)
+{
+    constexpr int K = 1 << NM;
+    const float2 one = make_float2(1.f, 0.f);
+    for (int g = threadIdx.x; g < (1 << (p - NM)); g += kFftThreads) {
+        const int base = g * K;
+        float2 v[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = z[fpad(base + k)];
+#pragma unroll
+        for (int s = 0; s < NM; ++s) {
+            const int d = 1 << (NM - 1 - s);
+#pragma unroll
+            for (int kl = 0; kl < d; ++kl) {
+                const float2 w = rot(one, kl, d);
+#pragma unroll
+                for (int k = kl; k < K; k += 2 * d) {
+                    const float2 a = v[k], c = v[k + d];
+                    v[k] = cadd(a, c);
+                    v[k + d] = kl ? cmul(csub(a, c), w) : csub(a, c);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) v[k] = cmul(v[k], __ldg(gb + base + k));
+#pragma unroll
+        for (int s = 0; s < NM; ++s) {
+            const int d = 1 << s;
+#pragma unroll
+            for (int kl = 0; kl < d; ++kl) {
+                const float2 w = rot(one, kl, d);
+#pragma unroll
+                for (int k = kl; k < K; k += 2 * d) {
+                    const float2 a = v[k], c = kl ? cmulc(v[k + d], w) : v[k + d];
+                    v[k] = cadd(a, c);
+                    v[k + d] = csub(a, c);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < K; ++k) z[fpad(base + k)] = v[k];
+    }
+}
+
+__global__ __launch_bounds__(kFftThreads) void k_ramlak_fft(const float *__restrict__ in,
+                                                            float *__restrict__ out, int R, int A,
+                                                            int p, const float2 *__restrict__ tab,
+                                                            float g0)
+{
+    extern __shared__ __align__(16) float2 z[];          // [M + M/16]
+    __shared__ float2 wsum[kFftThreads / 32];
+    const int M = 1 << p, H = M >> 1, t = threadIdx.x;
+    const float2 *__restrict__ tw = tab;
+    const float2 *__restrict__ gb = tab + H;
+    const int a0 = 2 * blockIdx.x;
+    const bool two = a0 + 1 < A;
+    const float *__restrict__ x = in + (size_t)a0 * R;
+    const float *__restrict__ y = x + R;                 // read only when `two`
+
+    // v[n] for n in [0, R), else 0
+    auto v = [&](int n) {
+        float2 r = make_float2(0.f, 0.f);
+        if (n >= 0 && n < R) {
+            r.x = __ldg(x + n);
+            if (two) r.y = __ldg(y + n);
+        }
+        return r;
+    };
+    // load D, forward stage of span H.  v[i - 1] comes from the lane below
+    // (lane 0 loads it); the loop runs warp-uniformly so that every lane
+    // takes part in the shuffles.
+    float2 s = make_float2(0.f, 0.f);
+    const int lane = t & 31;
+    for (int ib = t - lane; ib < H; ib += kFftThreads) {
+        const int i = ib + lane;
+        const float2 vi = v(i);                    // zero for i >= R (and so for i >= H)
+        float2 vp;
+        vp.x = __shfl_up_sync(0xffffffffu, vi.x, 1);
+        vp.y = __shfl_up_sync(0xffffffffu, vi.y, 1);
+        if (i >= H) continue;
+        if (lane == 0) vp = v(i - 1);
+        s = cadd(s, vi);
+        const float2 a = csub(vi, vp);
+        const float2 c = (i + H <= R) ? csub(v(i + H), v(i + H - 1)) : make_float2(0.f, 0.f);
+        z[fpad(i)] = cadd(a, c);
+        z[fpad(i + H)] = cmul(csub(a, c), __ldg(tw + i));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s.x += __shfl_xor_sync(0xffffffffu, s.x, o);
+        s.y += __shfl_xor_sync(0xffffffffu, s.y, o);
+    }
+    if ((t & 31) == 0) wsum[t >> 5] = s;
+    __syncthreads();
+
+    // forward stages of spans H/2 .. 2^nm, in passes of up to four
+    const int nm = min(3, p - 1);
+    for (int lt = p - 2; lt >= nm;) {
+        const int nst = min(4, lt - nm + 1);
+        if (nst == 4) fft_fwd_pass<4>(z, p, lt, tw);
+        else if (nst == 3) fft_fwd_pass<3>(z, p, lt, tw);
+        else if (nst == 2) fft_fwd_pass<2>(z, p, lt, tw);
+        else fft_fwd_pass<1>(z, p, lt, tw);
+        lt -= nst;
+        __syncthreads();
+    }
+    if (nm == 3) fft_mid_pass<3>(z, p, gb);
+    else if (nm == 2) fft_mid_pass<2>(z, p, gb);
+    else fft_mid_pass<1>(z, p, gb);
+    __syncthreads();
+    for (int lb = nm; lb <= p - 2;) {
+        const int nst = min(4, p - 1 - lb);
+        if (nst == 4) fft_inv_pass<4>(z, p, lb, tw);
+        else if (nst == 3) fft_inv_pass<3>(z, p, lb, tw);
+        else if (nst == 2) fft_inv_pass<2>(z, p, lb, tw);
+        else fft_inv_pass<1>(z, p, lb, tw);
+        lb += nst;
+        __syncthreads();
+    }
+    // inverse span H (outputs [0, R) only) and the DC term
+    float2 tot = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int w = 0; w < kFftThreads / 32; ++w) tot = cadd(tot, wsum[w]);
+    const float dcx = tot.x * g0, dcy = tot.y * g0;
+    float *__restrict__ ox = out + (size_t)a0 * R;
+    for (int n = t; n < R; n += kFftThreads) {
+        const float2 r = cadd(z[fpad(n)], cmulc(z[fpad(n + H)], __ldg(tw + n)));
+        ox[n] = r.x + dcx;
+        if (two) ox[R + n] = r.y + dcy;
+    }
+}
+
+int launch_ramlak_fft(const float *in_am, float *out_am, int R, int A, int p, const float2 *d_tab,
+                      float g0, cudaStream_t st)
+{
+    if (p < 2 || p > kRamlakFftMaxLog || (1 << p) < 2 * R - 1)
+        return set_error(RG_EUNSUPPORTED, "Ram-Lak FFT: bad transform size 2^%d for %d rays", p, R);
+    const size_t smem = sizeof(float2) * (((size_t)1 << p) + ((size_t)1 << p) / 16);
+    RG_CK(cudaFuncSetAttribute(k_ramlak_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+    k_ramlak_fft<<<(A + 1) / 2, kFftThreads, smem, st>>>(in_am, out_am, R, A, p, d_tab, g0);
+    RG_CK_LAUNCH("k_ramlak_fft");
     return RG_OK;
 }
 
