@@ -188,7 +188,8 @@ static int get_plan(const SSGeom &g, int stride, int first, std::shared_ptr<Plan
 struct DevTable {
     void *p = nullptr;
     float h0 = 0.f;   // Ram-Lak centre tap, or the FFT filter's DC gain / 2^fft_p
-    int fft_p = 0;    // Ram-Lak by FFT of size 2^fft_p (0: spatial taps)
+    int fft_p = 0;    // filter by FFT of size 2^fft_p (0: direct-sum taps)
+    bool fft_circ = false;   // ... as a circular convolution of length 2^fft_p
     ~DevTable() { if (p) cudaFree(p); }
 };
 static Cache<DevTable> g_tables;
@@ -211,11 +212,12 @@ static int get_table(const std::string &key, const void *host, size_t bytes,
     return RG_OK;
 }
 
-// Device copy of a host table that `fill(bytes, h0, fft_p)` builds only when
-// the key is not cached yet (for tables that are costly to compute).
+// Device copy of a host table that `fill` builds only when the key is not
+// cached yet (for tables that are costly to compute).
 template <class F>
 static int get_table_lazy(const std::string &key, F fill, std::shared_ptr<DevTable> &out)
 {
+    // fill(bytes, table): the host bytes, and the table's scalar fields
     KeyBuilder kb;
     kb.add(current_device());
     kb.s += key;
@@ -224,7 +226,7 @@ static int get_table_lazy(const std::string &key, F fill, std::shared_ptr<DevTab
     if (out) return RG_OK;
     auto t = std::make_shared<DevTable>();
     std::vector<unsigned char> host;
-    fill(host, t->h0, t->fft_p);
+    fill(host, *t);
     RG_CK(cudaMalloc(&t->p, host.size()));
     RG_CK(cudaMemcpy(t->p, host.data(), host.size(), cudaMemcpyHostToDevice));
     g_tables.put(kb.s, t);
@@ -619,38 +621,61 @@ int rg_radon_transpose_slantstack(rg_image sino, rg_image img, void *ws, size_t 
 }
 
 // ---------------------------------------------------------------- filters
-// Ram-Lak by FFT for transforms of up to 2^kRamlakFftMaxLog points;
-// RG_RAMLAK=direct selects the spatial kernel.
-static bool ramlak_use_fft(int R)
+// Filters by FFT for transforms of up to 2^kFilterFftMaxLog points: Ram-Lak
+// (zero-padded linear convolution) for any R, the lowpass filter (circular
+// convolution of length R) when R is a power of two >= 4.
+// RG_FILTER_KERNEL=direct selects the direct-sum kernels.
+static bool filter_use_fft(int kind, int R)
 {
-    const char *e = getenv("RG_RAMLAK");
+    const char *e = getenv("RG_FILTER_KERNEL");
     if (e && !strcmp(e, "direct")) return false;
-    return 2 * (long long)R - 1 <= (1LL << kRamlakFftMaxLog);
+    if (kind == RG_FILTER_LOWPASS)
+        return R >= 4 && (R & (R - 1)) == 0 && R <= (1 << kFilterFftMaxLog);
+    return 2 * (long long)R - 1 <= (1LL << kFilterFftMaxLog);
 }
 
-// Tables of launch_ramlak_fft for R rays at spacing dt: twiddles, then the
-// difference-domain filter G'[k] = G[k] / (M (1 - e^{-2 pi i k / M})) in
-// bit-reversed order (G'[0] = 0), all from FP64; g0 = G[0] / M.  G is the
-// DFT of the Ram-Lak taps dt h[m], |m| < R, wrapped to length M (real, as
-// the taps are even): G[k] = dt h[0] + 2 sum_{odd m < R} dt h[m] cos(2 pi k m / M).
-static void ramlak_fft_tables(int R, double dt, std::vector<unsigned char> &bytes, float &g0,
-                              int &p)
+// In-place radix-2 FFT (forward, e^{-2 pi i k n / M}) of length M = 2^p in
+// FP64, for the filter tables.
+static void host_fft(std::vector<std::complex<double>> &a, int p)
+{
+    const double pi = 3.14159265358979323846;
+    const int M = 1 << p;
+    for (int i = 0; i < M; ++i) {
+        int r = 0;
+        for (int b = 0; b < p; ++b) r |= ((i >> b) & 1) << (p - 1 - b);
+        if (i < r) std::swap(a[i], a[r]);
+    }
+    std::vector<std::complex<double>> w(M / 2);
+    for (int t = 0; t < M / 2; ++t) w[t] = std::complex<double>(cos(2.0 * pi * t / M), -sin(2.0 * pi * t / M));
+    for (int len = 2; len <= M; len <<= 1) {
+        const int half = len / 2, step = M / len;
+        for (int i = 0; i < M; i += len)
+            for (int j = 0; j < half; ++j) {
+                const std::complex<double> u = a[i + j], v = a[i + j + half] * w[(size_t)j * step];
+                a[i + j] = u + v;
+                a[i + j + half] = u - v;
+            }
+    }
+}
+
+// Tables of launch_filter_fft for the 2R-1 taps t[m] (taps[m + R - 1], |m| <
+// R): twiddles, then the difference-domain filter G'[k] = T[k] / (M (1 -
+// e^{-2 pi i k / M})) in bit-reversed order (G'[0] = 0), T the DFT of the
+// taps wrapped to length M = 2^p >= 2R - 1 (circ: of one period of
+// R-periodic taps, M = R); g0 = T[0] / M.  All in FP64.
+static void filter_fft_tables(const std::vector<double> &taps, int R, bool circ,
+                              std::vector<unsigned char> &bytes, float &g0, int &p)
 {
     const double pi = 3.14159265358979323846;
     p = 2;
-    while ((1LL << p) < 2 * (long long)R - 1) ++p;
+    while ((1LL << p) < (circ ? (long long)R : 2 * (long long)R - 1)) ++p;
     const int M = 1 << p, H = M / 2;
-    std::vector<double> ctab(M);
-    for (int i = 0; i < M; ++i) ctab[i] = cos(2.0 * pi * i / M);
-    std::vector<double> G(M), inv_m2((size_t)R / 2 + 1);
-    for (int m = 1; m < R; m += 2) inv_m2[m / 2] = 1.0 / ((double)m * (double)m);
-    const double h0 = dt / (4.0 * dt * dt);
-    for (int k = 0; k < M; ++k) {
-        double acc = 0.0;
-        for (int m = 1; m < R; m += 2)
-            acc += ctab[(size_t)((long long)k * m & (M - 1))] * inv_m2[m / 2];
-        G[k] = h0 - 2.0 * acc / (pi * pi * dt);
-    }
+    std::vector<std::complex<double>> T(M);
+    if (circ)             // one period of the R-periodic taps
+        for (int m = 0; m < R; ++m) T[m] = taps[(size_t)(m + R - 1)];
+    else
+        for (int m = -(R - 1); m <= R - 1; ++m) T[(m + M) & (M - 1)] = taps[(size_t)(m + R - 1)];
+    host_fft(T, p);
     bytes.assign(sizeof(float2) * ((size_t)H + M), 0);
     float2 *tw = reinterpret_cast<float2 *>(bytes.data());
     float2 *gb = tw + H;
@@ -660,10 +685,49 @@ static void ramlak_fft_tables(int R, double dt, std::vector<unsigned char> &byte
         for (int b = 0; b < p; ++b) r |= ((k >> b) & 1) << (p - 1 - b);
         if (r == 0) { gb[k] = make_float2(0.f, 0.f); continue; }
         // 1 / (1 - e^{-i th}) = (1 - i cot(th / 2)) / 2, th = 2 pi r / M
-        const double half = G[r] / (2.0 * M), a = pi * r / M;
-        gb[k] = make_float2((float)half, (float)(-half * cos(a) / sin(a)));
+        const double a = pi * r / M;
+        const std::complex<double> g = T[r] * std::complex<double>(1.0, -cos(a) / sin(a)) / (2.0 * M);
+        gb[k] = make_float2((float)g.real(), (float)g.imag());
     }
-    g0 = (float)(G[0] / M);
+    g0 = (float)(T[0].real() / M);
+}
+
+// The 2R-1 taps in FP64 (index m + R - 1, |m| < R): dt h[m] for the
+// discrete Ram-Lak kernel h (linear convolution), or g[m mod R] for pyraft's
+// lowpassino_fbp (circular convolution): g = Re(ifft(fftshift(|w| cos(pi w
+// dt)))), w = linspace(-wc, wc, R), wc = 1/(2 dt), so that applying g equals
+// the FFT filter of pyraft/filters/filters.py:13-68 (real part of the
+// filtered data).
+static std::vector<double> filter_taps64(int kind, int R, double dt)
+{
+    const double pi = 3.14159265358979323846;
+    std::vector<double> taps(2 * (size_t)R - 1, 0.0);
+    if (kind == RG_FILTER_RAMLAK) {
+        taps[R - 1] = dt / (4.0 * dt * dt);
+        for (int m = 1; m < R; m += 2) {
+            const double v = -dt / (pi * pi * (double)m * (double)m * dt * dt);
+            taps[(size_t)(R - 1 + m)] = v;
+            taps[(size_t)(R - 1 - m)] = v;
+        }
+        return taps;
+    }
+    const double wc = 1.0 / (2.0 * dt);
+    std::vector<double> h(R), G(R), g(R), ctab(R);
+    const double step = (R > 1) ? (2.0 * wc) / (R - 1) : 0.0;
+    for (int i = 0; i < R; ++i) {
+        double w = (i == R - 1) ? wc : -wc + i * step;
+        h[i] = fabs(w) * cos(pi * w * dt);
+    }
+    const int sh = R / 2;              // fftshift: G[k] = h[(k + R/2) mod R]... numpy
+    for (int k = 0; k < R; ++k) G[k] = h[(k + (R - sh)) % R];
+    for (int k = 0; k < R; ++k) ctab[k] = cos(2.0 * pi * (double)k / (double)R);
+    for (int m = 0; m < R; ++m) {
+        double acc = 0.0;
+        for (int k = 0; k < R; ++k) acc += G[k] * ctab[(size_t)k * m % R];
+        g[m] = acc / R;
+    }
+    for (int m = -(R - 1); m <= R - 1; ++m) taps[(size_t)(m + R - 1)] = g[((m % R) + R) % R];
+    return taps;
 }
 
 static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable> &out)
@@ -672,63 +736,43 @@ static int filter_taps(const rg_image &sino, int kind, std::shared_ptr<DevTable>
     const double tmin = sino.br_y, tmax = sino.tl_y;
     const double dt = (tmax - tmin) / (R - 1);
     if (!(std::isfinite(dt)) || dt == 0.0) return set_error(RG_EINVAL, "degenerate t extent");
+    if (kind != RG_FILTER_RAMLAK && kind != RG_FILTER_LOWPASS)
+        return set_error(RG_EINVAL, "unknown filter kind %d", kind);
     KeyBuilder kb;
     kb.add(kind).add(R).add(tmin).add(tmax);
-    const double pi = 3.14159265358979323846;
-    if (kind == RG_FILTER_RAMLAK && ramlak_use_fft(R)) {
-        return get_table_lazy("rlfft" + kb.s, [&](std::vector<unsigned char> &b, float &h0, int &p) {
-            ramlak_fft_tables(R, dt, b, h0, p);
+    if (filter_use_fft(kind, R)) {
+        return get_table_lazy("fft" + kb.s, [&](std::vector<unsigned char> &b, DevTable &t) {
+            t.fft_circ = kind == RG_FILTER_LOWPASS;
+            filter_fft_tables(filter_taps64(kind, R, dt), R, t.fft_circ, b, t.h0, t.fft_p);
         }, out);
     }
-    if (kind == RG_FILTER_RAMLAK) {
-        // Odd taps godd[q] = dt h[2q - 2R + 1], q in [0, 2R), then dt h[0]
-        // (the layout k_ramlak_rows reads).
-        return get_table_lazy("taps" + kb.s, [&](std::vector<unsigned char> &b, float &h0, int &) {
+    return get_table_lazy("taps" + kb.s, [&](std::vector<unsigned char> &b, DevTable &tab) {
+        const std::vector<double> t = filter_taps64(kind, R, dt);
+        if (kind == RG_FILTER_RAMLAK) {
+            // odd taps godd[q] = dt h[2q - 2R + 1], q in [0, 2R), then dt h[0]
+            // (the layout k_ramlak_rows reads)
             b.assign(sizeof(float) * (2 * (size_t)R + 1), 0);
-            float *taps = reinterpret_cast<float *>(b.data());
+            float *g = reinterpret_cast<float *>(b.data());
             for (int q = 0; q < 2 * R; ++q) {
                 const int m = 2 * q - 2 * R + 1;
-                if (m >= -(R - 1) && m <= R - 1)
-                    taps[q] = (float)(-dt / (pi * pi * (double)m * (double)m * dt * dt));
+                if (m >= -(R - 1) && m <= R - 1) g[q] = (float)t[(size_t)(m + R - 1)];
             }
-            taps[2 * (size_t)R] = (float)(dt / (4.0 * dt * dt));
-            h0 = taps[2 * (size_t)R];
-        }, out);
-    }
-    if (kind == RG_FILTER_LOWPASS) {
-        // g = Re(ifft(fftshift(|w| cos(pi w dt)))), w = linspace(-wc, wc, R), wc = 1/(2 dt):
-        // applying g by circular convolution equals the FFT filter of
-        // pyraft/filters/filters.py:13-68 (real part of the filtered data).
-        return get_table_lazy("taps" + kb.s, [&](std::vector<unsigned char> &b, float &, int &) {
-            const double wc = 1.0 / (2.0 * dt);
-            std::vector<double> h(R), G(R), g(R), ctab(R);
-            const double step = (R > 1) ? (2.0 * wc) / (R - 1) : 0.0;
-            for (int i = 0; i < R; ++i) {
-                double w = (i == R - 1) ? wc : -wc + i * step;
-                h[i] = fabs(w) * cos(pi * w * dt);
-            }
-            const int sh = R / 2;          // fftshift: G[k] = h[(k + R/2) mod R]... numpy
-            for (int k = 0; k < R; ++k) G[k] = h[(k + (R - sh)) % R];
-            for (int k = 0; k < R; ++k) ctab[k] = cos(2.0 * pi * (double)k / (double)R);
-            for (int m = 0; m < R; ++m) {
-                double acc = 0.0;
-                for (int k = 0; k < R; ++k) acc += G[k] * ctab[(size_t)k * m % R];
-                g[m] = acc / R;
-            }
-            b.assign(sizeof(float) * (2 * (size_t)R - 1), 0);
-            float *taps = reinterpret_cast<float *>(b.data());
-            for (int m = -(R - 1); m <= R - 1; ++m) taps[m + R - 1] = (float)g[((m % R) + R) % R];
-        }, out);
-    }
-    return set_error(RG_EINVAL, "unknown filter kind %d", kind);
+            g[2 * (size_t)R] = (float)t[R - 1];
+            tab.h0 = g[2 * (size_t)R];
+        } else {
+            b.assign(sizeof(float) * t.size(), 0);
+            float *g = reinterpret_cast<float *>(b.data());
+            for (size_t i = 0; i < t.size(); ++i) g[i] = (float)t[i];
+        }
+    }, out);
 }
 
 static int filter_rows(int kind, const float *in_am, float *out_am, int R, int A,
                        const std::shared_ptr<DevTable> &taps, cudaStream_t st)
 {
-    if (kind == RG_FILTER_RAMLAK && taps->fft_p)
-        return launch_ramlak_fft(in_am, out_am, R, A, taps->fft_p, (const float2 *)taps->p,
-                                 taps->h0, st);
+    if (taps->fft_p)
+        return launch_filter_fft(in_am, out_am, R, A, taps->fft_p, (const float2 *)taps->p,
+                                 taps->h0, taps->fft_circ, st);
     if (kind == RG_FILTER_RAMLAK)     // odd taps + centre tap (parity-split kernel)
         return launch_ramlak_rows(in_am, out_am, R, A, (const float *)taps->p, taps->h0, st);
     return launch_conv_rows(in_am, out_am, R, A, (const float *)taps->p, st);

@@ -6,9 +6,9 @@
 // convolution, or the periodised spatial form of pyraft's lowpassino_fbp
 // filter (pyraft/filters/filters.py:13-68) for circular convolution.
 //
-// Kernels: k_conv_rows (any taps, direct sums), k_ramlak_rows (Ram-Lak,
-// direct sums over its odd taps) and k_ramlak_fft (Ram-Lak by FFT, the
-// default up to 8192 rays: O(R log R) per view and more accurate).
+// Kernels: k_filter_fft (either filter by FFT, the default up to 8192 rays:
+// O(R log R) per view and more accurate), and above that the direct sums of
+// k_ramlak_rows (Ram-Lak, its odd taps only) and k_conv_rows (any taps).
 //
 // k_conv_rows:
 // CTA = 256 outputs x 16 views.  The input is walked in tiles of 256
@@ -208,17 +208,22 @@ int launch_ramlak_rows(const float *in_am, float *out_am, int R, int A, const fl
 }
 
 // ----------------------------------------------------------------------------
-// Ram-Lak by FFT: the same linear convolution, through a circular one of
-// length M = 2^p >= 2R - 1 (outputs [0, R) see no wrap-around).
+// Filter by FFT: the same sum over the 2R-1 taps, through a circular
+// convolution of length M = 2^p >= 2R - 1 (outputs [0, R) see no
+// wrap-around).  The circular form (circ; R = M a power of two) computes
+// pyraft's lowpass filter as what it is, a circular convolution of length
+// R: its taps are R-periodic, and their zero-padded transform would
+// oscillate and amplify rounding at low frequencies.
 //
-// Two views per CTA, packed as one complex signal v = x + i y: the filter's
-// impulse response is real, so the real and imaginary parts of the result
-// are the two filtered views.
+// Two views per CTA, packed as one complex signal v = x + i y: the taps are
+// real, so the real and imaginary parts of the result are the two filtered
+// views.
 //
 // Accuracy: the FFT's rounding error scales with the norm of what it
-// transforms, while Ram-Lak all but removes the low frequencies that carry
-// most of a sinogram's norm.  So the kernel transforms the first difference
-// D[n] = v[n] - v[n-1] (v zero outside [0, R)) and applies G'[k] =
+// transforms, while a ramp filter all but removes the low frequencies that
+// carry most of a sinogram's norm.  So the kernel transforms the first difference
+// D[n] = v[n] - v[n-1] (v zero outside [0, R); circular: v[-1] = v[R-1])
+// and applies G'[k] =
 // G[k] / (M (1 - e^{-2 pi i k / M})) for k != 0, with G the filter's DFT;
 // the DC term G[0] sum(v) / M is added at the end.  On FP32 inputs this
 // keeps the result within a few 1e-7 (relative L2) of the FP64 convolution
@@ -392,10 +397,10 @@ __device__ __forceinline__ void fft_mid_pass(float2 *z, int p, const float2 *__r
     }
 }
 
-__global__ __launch_bounds__(kFftThreads) void k_ramlak_fft(const float *__restrict__ in,
+__global__ __launch_bounds__(kFftThreads) void k_filter_fft(const float *__restrict__ in,
                                                             float *__restrict__ out, int R, int A,
                                                             int p, const float2 *__restrict__ tab,
-                                                            float g0)
+                                                            float g0, bool circ)
 {
     extern __shared__ __align__(16) float2 z[];          // [M + M/16]
     __shared__ float2 wsum[kFftThreads / 32];
@@ -428,10 +433,15 @@ __global__ __launch_bounds__(kFftThreads) void k_ramlak_fft(const float *__restr
         vp.x = __shfl_up_sync(0xffffffffu, vi.x, 1);
         vp.y = __shfl_up_sync(0xffffffffu, vi.y, 1);
         if (i >= H) continue;
-        if (lane == 0) vp = v(i - 1);
+        if (lane == 0) vp = v(i == 0 && circ ? R - 1 : i - 1);
         s = cadd(s, vi);
         const float2 a = csub(vi, vp);
-        const float2 c = (i + H <= R) ? csub(v(i + H), v(i + H - 1)) : make_float2(0.f, 0.f);
+        float2 c = make_float2(0.f, 0.f);
+        if (i + H <= R) {                          // circular: always; else i = 0, R = H
+            const float2 vh = v(i + H);
+            if (circ) s = cadd(s, vh);
+            c = csub(vh, v(i + H - 1));
+        }
         z[fpad(i)] = cadd(a, c);
         z[fpad(i + H)] = cmul(csub(a, c), __ldg(tw + i));
     }
@@ -474,22 +484,26 @@ __global__ __launch_bounds__(kFftThreads) void k_ramlak_fft(const float *__restr
     const float dcx = tot.x * g0, dcy = tot.y * g0;
     float *__restrict__ ox = out + (size_t)a0 * R;
     for (int n = t; n < R; n += kFftThreads) {
-        const float2 r = cadd(z[fpad(n)], cmulc(z[fpad(n + H)], __ldg(tw + n)));
+        // n >= H only in the circular form (R = M)
+        const int n0 = n < H ? n : n - H;
+        const float2 u = cmulc(z[fpad(n0 + H)], __ldg(tw + n0));
+        const float2 r = n < H ? cadd(z[fpad(n0)], u) : csub(z[fpad(n0)], u);
         ox[n] = r.x + dcx;
         if (two) ox[R + n] = r.y + dcy;
     }
 }
 
-int launch_ramlak_fft(const float *in_am, float *out_am, int R, int A, int p, const float2 *d_tab,
-                      float g0, cudaStream_t st)
+int launch_filter_fft(const float *in_am, float *out_am, int R, int A, int p, const float2 *d_tab,
+                      float g0, bool circ, cudaStream_t st)
 {
-    if (p < 2 || p > kRamlakFftMaxLog || (1 << p) < 2 * R - 1)
-        return set_error(RG_EUNSUPPORTED, "Ram-Lak FFT: bad transform size 2^%d for %d rays", p, R);
+    if (p < 2 || p > kFilterFftMaxLog || (circ ? (1 << p) != R : (1 << p) < 2 * R - 1))
+        return set_error(RG_EUNSUPPORTED, "filter FFT: bad transform size 2^%d for %d rays", p, R);
     const size_t smem = sizeof(float2) * (((size_t)1 << p) + ((size_t)1 << p) / 16);
-    RG_CK(cudaFuncSetAttribute(k_ramlak_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    RG_CK(cudaFuncSetAttribute(k_filter_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
-    k_ramlak_fft<<<(A + 1) / 2, kFftThreads, smem, st>>>(in_am, out_am, R, A, p, d_tab, g0);
-    RG_CK_LAUNCH("k_ramlak_fft");
+    k_filter_fft<<<(A + 1) / 2, kFftThreads, smem, st>>>(in_am, out_am, R, A, p, d_tab, g0,
+                                                         circ);
+    RG_CK_LAUNCH("k_filter_fft");
     return RG_OK;
 }
 

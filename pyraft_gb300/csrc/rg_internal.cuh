@@ -226,12 +226,13 @@ int launch_conv_rows(const float *in_am, float *out_am, int R, int A, const floa
 int launch_ramlak_rows(const float *in_am, float *out_am, int R, int A, const float *d_godd,
                        float h0, cudaStream_t st);
 
-// Ram-Lak by FFT of size 2^p (2^p >= 2R - 1, p <= kRamlakFftMaxLog): d_tab =
-// twiddles e^{-2 pi i t / 2^p} (t < 2^(p-1)), then the difference-domain
-// filter in bit-reversed order (2^p entries); g0 = the DC gain / 2^p.
-constexpr int kRamlakFftMaxLog = 14;
-int launch_ramlak_fft(const float *in_am, float *out_am, int R, int A, int p, const float2 *d_tab,
-                      float g0, cudaStream_t st);
+// A filter by FFT of size 2^p (2^p >= 2R - 1; circ: 2^p = R, a circular
+// convolution of length R; p <= kFilterFftMaxLog): d_tab = twiddles
+// e^{-2 pi i t / 2^p} (t < 2^(p-1)), then the difference-domain filter in
+// bit-reversed order (2^p entries); g0 = the DC gain / 2^p.
+constexpr int kFilterFftMaxLog = 14;
+int launch_filter_fft(const float *in_am, float *out_am, int R, int A, int p, const float2 *d_tab,
+                      float g0, bool circ, cudaStream_t st);
 
 // bresenham.cu
 struct DDAGeom {

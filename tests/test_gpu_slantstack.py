@@ -187,39 +187,58 @@ def _ramlak_cases(R):
     return s, len(smooth)
 
 
-@pytest.mark.parametrize("R", [2, 3, 5, 64, 200, 1025, 2048, 4096, 4097, 8192])
-def test_ramlak_fft_vs_oracle(orc, R):
-    """The FFT Ram-Lak kernel (2R - 1 <= 16384) against the FP64 convolution,
-    on smooth profiles (the hard case for an FFT filter: Ram-Lak removes most
-    of their norm) and rough ones.  The oracle gets the FP32 inputs the
-    kernel sees, so the bound measures the kernel alone.  Two views share
-    one complex transform, so a view's error also carries a rounding-level
-    share of its partner's norm: the bound adds 1e-7 of the largest view."""
+def _filter(orc, kind, s):
+    R = s.shape[0]
+    if kind == "ramlak":
+        return (np.asarray(rg.ramlak(sino_img(s)), np.float64), orc.ramlak(s, 2.0 / (R - 1)))
+    return (np.asarray(rg.lowpassino_fbp(sino_img(s)), np.float64), orc.lowpassino_fbp(s))
+
+
+@pytest.mark.parametrize("kind,R", [("ramlak", R) for R in (2, 3, 5, 64, 200, 1025, 2048, 4096,
+                                                              4097, 8192)] +
+                         [("lowpass", R) for R in (4, 8, 64, 256, 2048, 4096, 8192)])
+def test_filter_fft_vs_oracle(orc, kind, R):
+    """The FFT filter kernel against the FP64 filters (the Ram-Lak
+    convolution; pyraft's lowpassino_fbp by numpy FFT): Ram-Lak up to 8192
+    rays, the lowpass filter (a circular convolution of length R) for R a
+    power of two.  Smooth profiles are the hard case for an FFT filter (a
+    ramp filter removes most of their norm), rough ones the easy case.  The
+    oracle gets the FP32 inputs the kernel sees, so the bound measures the
+    kernel alone.  Two views share one complex transform, so a view's error
+    also carries a rounding-level share of its partner's norm: the bound
+    adds 1e-7 of the largest view.  The lowpass bound is 5e-6: its circular
+    difference carries the jump between a profile's two ends (2e-6 for
+    5 + t at 8192 rays)."""
     s, _ = _ramlak_cases(R)
-    out = np.asarray(rg.ramlak(sino_img(s)), np.float64)
-    ref = orc.ramlak(s, 2.0 / (R - 1))
+    out, ref = _filter(orc, kind, s)
+    tol = 2e-6 if kind == "ramlak" else 5e-6
     big = max(np.linalg.norm(ref[:, c]) for c in range(s.shape[1]))
     for c in range(s.shape[1]):
         err = np.linalg.norm(out[:, c] - ref[:, c])
-        assert err <= 2e-6 * np.linalg.norm(ref[:, c]) + 1e-7 * big, (c, err)
+        assert err <= tol * np.linalg.norm(ref[:, c]) + 1e-7 * big, (c, err)
 
 
-@pytest.mark.parametrize("R", [3, 200, 2048, 4097])
-def test_ramlak_direct_vs_oracle(orc, monkeypatch, R):
-    """The spatial Ram-Lak kernel (RG_RAMLAK=direct; the default above 8192
-    rays).  It sums the taps' products directly, so on smooth profiles its
-    FP32 cancellation error grows with R (1.4e-4 relative at 4097 rays); on
-    rough ones it stays at the 1e-7 level."""
-    monkeypatch.setenv("RG_RAMLAK", "direct")
+@pytest.mark.parametrize("kind,R", [("ramlak", 3), ("ramlak", 200), ("ramlak", 2048),
+                                    ("ramlak", 4097), ("lowpass", 3), ("lowpass", 200),
+                                    ("lowpass", 1025), ("lowpass", 2048)])
+def test_filter_direct_vs_oracle(orc, monkeypatch, kind, R):
+    """The direct-sum filter kernels (RG_FILTER_KERNEL=direct; the default
+    above 8192 rays, and for the lowpass filter when R is not a power of
+    two).  They sum the taps' products directly, so on smooth profiles
+    their FP32 cancellation error grows with R (Ram-Lak: 1.4e-4 relative at
+    4097 rays); on rough ones it stays at the 1e-7 level."""
+    monkeypatch.setenv("RG_FILTER_KERNEL", "direct")
     s, ns = _ramlak_cases(R)
-    out = np.asarray(rg.ramlak(sino_img(s)), np.float64)
-    ref = orc.ramlak(s, 2.0 / (R - 1))
+    out, ref = _filter(orc, kind, s)
     for c in range(s.shape[1]):
         bound = 3e-4 if c < ns else 2e-6
         assert rel(out[:, c], ref[:, c]) <= bound, (c, rel(out[:, c], ref[:, c]))
 
 
-def test_lowpass_vs_numpy_fft(orc):
+@pytest.mark.parametrize("path", ["fft", "direct"])
+def test_lowpass_vs_numpy_fft(orc, monkeypatch, path):
+    if path == "direct":
+        monkeypatch.setenv("RG_FILTER_KERNEL", "direct")
     rng = np.random.default_rng(4)
     for R in (64, 257):
         s = rng.random((R, 21))
