@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libraftgb.so")
 UNITS = ("api", "slantstack", "aux", "filter", "bresenham", "em", "batch", "noalloc", "f64", "mesh",
-         "radon_tma")
+         "radon_tma", "gather_rot")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

@@ -1,0 +1,332 @@
+// gather_rot.cu -- the slant-stack backprojection with views paired a
+// quarter turn apart.
+//
+// The backprojection (raft/raft_backprojection_slantstack.c:43-180) samples
+// view theta of the sinogram at t = x cos(theta) + y sin(theta) for every
+// pixel.  When the views come in pairs theta, theta' = theta + pi/2 (an
+// even number of views over [theta0, theta0 + pi)) and the pixel grid is
+// symmetric (x and y on the same points, centred on 0), the quarter turn
+// maps the grid onto itself, and
+//     x cos(theta') + y sin(theta') = y cos(theta) + (-x) sin(theta):
+// pixel (x, y) at theta' meets the detector where pixel (y, -x) meets it at
+// theta.  In the indices of the N x N grid (x = xmin + col dx, y = ymin +
+// row dy): pixel (col N-1-r, row c) at theta' sits at the detector position
+// of pixel (col c, row r) at theta.
+//
+// So one position -- its sample index, interpolation weight and step to
+// the next pixel -- serves two views: a thread that walks the pixels (col
+// c, row r), (c, r + 4), ... of its tile for view theta reads the partner
+// view's staged window at the same entries and accumulates the pixels (col
+// N-1-r, row c), (N-5-r, c), ... of the quarter-turned tile for view
+// theta + pi/2.  The partner's window covers the same
+// sample indices, so its load is the same shared address plus a constant
+// offset.  Per update this leaves a shared load and two FP32 adds of the
+// seven instructions of the one-view inner loop (gather_tile<0>), and the
+// per-view set-up is shared too.
+//
+// Each pixel then gets two partial sums: views [theta0, theta0 + pi/2) from
+// the CTA whose tile holds it, views [theta0 + pi/2, theta0 + pi) from the
+// CTA whose quarter-turned tile holds it.  The output is zeroed first and
+// both partials are added atomically: two adds onto zero give the same
+// float in either order, so the result does not depend on timing.
+//
+// Precision: FP32 partial sums over a chunk of 16 view pairs, added across
+// chunks in FP32 (no compensation: the two-level sum keeps the error near
+// 1e-7 of the pixel values).
+#include <algorithm>
+
+#include "ss_tiles.cuh"
+
+namespace rg {
+
+namespace {
+
+constexpr int kPairSlots = kSlots / 2;    // view pairs per staged chunk
+
+__global__ void k_zero_image(float *__restrict__ out, int N, long long cs, long long ls,
+                             long long zo)
+{
+    out += (long long)blockIdx.z * zo;
+    const long long n = (long long)N * N;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int r = (int)(e / N), c = (int)(e - (long long)r * N);
+        out[(long long)r * cs + (long long)c * ls] = 0.f;
+    }
+}
+
+// MODE 0: backprojection; MODE 1: matched adjoint (edge pixels left to
+// k_adjoint_edges, as in gather_tile with edge_fixup).
+template <int MODE, int WMAX, int ROWS>
+__device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, int s_ld, int R,
+                                                const View *__restrict__ views, int half, int N,
+                                                float scale, float *__restrict__ out, long long cs,
+                                                long long ls, int *__restrict__ err, int tx,
+                                                int ty, float2 *__restrict__ pairs,
+                                                unsigned pair_bytes, int split, int rank)
+{
+    constexpr int TH = kWarps * ROWS;                     // tile height
+    constexpr unsigned kPartner = kPairSlots * WMAX * 8;  // byte offset of the partner windows
+    __shared__ SlotInfo slot[kPairSlots];
+    __shared__ int slotW[kPairSlots];
+    __shared__ int slotView[kPairSlots];
+    __shared__ float slotP[kPairSlots];
+    __shared__ float slotDelta[2 * kPairSlots];           // views, then partners
+
+    // Warp w covers columns 8 (w & 3) .. + 8 and rows 4 ROWS (w >> 2) .. +
+    // 4 ROWS of the tile; lane l takes column l & 7 and rows l >> 3, + 4,
+    // + 8, ...  So the 32 lanes of one load read 8 columns x 4 adjacent rows,
+    // whose positions lie within about 9 entries of the window: about one
+    // shared-memory wavefront per load, where 32 columns of one row span up
+    // to 32 entries (two wavefronts).
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int row0 = ty * TH, col0 = tx * kTile;
+    const int cofs = 8 * (warp & 3) + (lane & 7);
+    const int rofs = 4 * ROWS * (warp >> 2) + (lane >> 3);
+    const int col = col0 + cofs;
+    const int myrow = row0 + rofs;             // rows myrow + 4 r
+
+    float accB[ROWS], accA[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) { accB[r] = 0.f; accA[r] = 0.f; }
+
+    const int vbeg = (int)((long long)half * rank / split);
+    const int vend = (int)((long long)half * (rank + 1) / split);
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(pairs);
+    for (int chunk = vbeg; chunk < vend; chunk += kPairSlots) {
+        const int nslot = min(kPairSlots, vend - chunk);
+        if (warp == 0 && lane < kPairSlots) {
+            SlotInfo si = {0u, 0, 0, INT_MIN};
+            int W = 0, view = 0;
+            float P = 0.f, d0 = 0.f, d1 = 0.f;
+            if (lane < nslot) {
+                const View &v = views[chunk + lane];
+                long long cr, cc, c0;
+                if (MODE == 0) { cr = v.brow; cc = v.bcol; c0 = v.b0; }
+                else           { cr = v.krow; cc = v.kcol; c0 = v.k0; }
+                const long long origin = c0 + (long long)row0 * cr + (long long)col0 * cc;
+                const long long dr = (long long)(TH - 1) * cr, dc = (long long)(kTile - 1) * cc;
+                const long long mn = origin + min(0LL, dr) + min(0LL, dc);
+                const long long mx = origin + max(0LL, dr) + max(0LL, dc);
+                const int nlo = (int)(mn >> 32) - 1;
+                const int nhi = (int)(mx >> 32) + 1;
+                if (nhi - nlo + 1 <= WMAX) {
+                    si.nlo = nlo;
+                    si.base = (unsigned)((origin - ((long long)nlo << 32)) >> 9);
+                    si.a = (int)((cc + 256) >> 9);
+                    si.b = (int)((cr + 256) >> 9);
+                    W = nhi - nlo + 1;
+                } else if (err) {
+                    atomicOr(err, 1);
+                }
+                view = v.view;
+                P = v.P;
+                d0 = v.delta;
+                d1 = views[chunk + lane + half].delta;
+            }
+            slot[lane] = si;
+            slotW[lane] = W;
+            slotView[lane] = view;
+            slotP[lane] = P;
+            slotDelta[lane] = d0;
+            slotDelta[kPairSlots + lane] = d1;
+        }
+        __syncthreads();
+
+        // Stage the windows: q < kPairSlots the view of slot q, else the
+        // partner view of slot q - kPairSlots, over the same entries.
+        for (int q = warp; q < 2 * kPairSlots; q += kWarps) {
+            const int s = q < kPairSlots ? q : q - kPairSlots;
+            if (s >= nslot) continue;
+            const int nlo = slot[s].nlo, W = slotW[s];
+            const float *__restrict__ row =
+                s_am + (size_t)(slotView[s] + (q < kPairSlots ? 0 : half)) * s_ld;
+            const float d = slotDelta[q];
+            for (int e = lane; e < W; e += 32) {
+                const int n = nlo + e;
+                float2 pr = make_float2(0.f, 0.f);
+                if (MODE == 0) {
+                    if (n >= 0 && n <= R - 2) pr = make_pair(__ldg(row + n), __ldg(row + n + 1), true);
+                } else {
+                    const float s0 = (n >= 0 && n < R) ? __ldg(row + n) : 0.f;
+                    const float s1 = (n + 1 >= 0 && n + 1 < R) ? __ldg(row + n + 1) : 0.f;
+                    pr = make_float2(s0 * d, s1 * d);
+                }
+                pairs[q * WMAX + e] = pr;
+            }
+        }
+        __syncthreads();
+
+        float partB[ROWS], partA[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) { partB[r] = 0.f; partA[r] = 0.f; }
+        for (int s = 0; s < nslot; ++s) {
+            const SlotInfo si = slot[s];
+            if (si.nlo == INT_MIN) continue;
+            const unsigned pw = sbase + (unsigned)(s * WMAX) * pair_bytes;
+            unsigned vpos = si.base + (unsigned)(cofs * si.a) + (unsigned)(rofs * si.b);
+            const unsigned step = 4u * (unsigned)si.b;
+            // adjoint hat weights (gather_tile): sat(-P w1 + 1 + P), sat(P w1 + 1 - 2P);
+            // P is the same for a view and its partner
+            const float P = MODE == 0 ? 0.f : slotP[s];
+            const float c0 = 1.f + P, c1 = 1.f - 2.f * P;
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r) {
+                const unsigned addr = (vpos >> 23) * pair_bytes + pw;
+                float2 pb, pa;
+                asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
+                             : "=f"(pb.x), "=f"(pb.y) : "r"(addr));
+                asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];"
+                             : "=f"(pa.x), "=f"(pa.y) : "r"(addr), "n"(kPartner));
+                const float w1 = frac_plus_one(vpos);
+                if (MODE == 0) {
+                    partB[r] += fmaf(w1, pb.y, pb.x);
+                    partA[r] += fmaf(w1, pa.y, pa.x);
+                } else {
+                    const float wa = fma_sat(-P, w1, c0), wb = fma_sat(P, w1, c1);
+                    partB[r] = fmaf(pb.y, wb, fmaf(pb.x, wa, partB[r]));
+                    partA[r] = fmaf(pa.y, wb, fmaf(pa.x, wa, partA[r]));
+                }
+                vpos += step;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) { accB[r] += partB[r]; accA[r] += partA[r]; }
+        __syncthreads();
+    }
+
+    if (split > 1) {
+        // The last chunk ended with a barrier: the staging area is free.
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        float *red = reinterpret_cast<float *>(pairs);    // [2 ROWS][256]
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            red[r * 256 + threadIdx.x] = accB[r];
+            red[(ROWS + r) * 256 + threadIdx.x] = accA[r];
+        }
+        cl.sync();
+        const int per = ROWS / split;
+        for (int q = 0; q < per; ++q) {
+            const int r = rank * per + q;
+            float sb = 0.f, sa = 0.f;
+            for (int src = 0; src < split; ++src) {
+                const float *peer = cl.map_shared_rank(red, src);
+                sb += peer[r * 256 + threadIdx.x];
+                sa += peer[(ROWS + r) * 256 + threadIdx.x];
+            }
+            const int row = myrow + 4 * r;
+            const bool edge = MODE != 0 && (row == 0 || col == 0 || row == N - 1 || col == N - 1);
+            if (row < N && col < N && !edge) {
+                atomicAdd(out + (long long)row * cs + (long long)col * ls, sb * scale);
+                atomicAdd(out + (long long)col * cs + (long long)(N - 1 - row) * ls, sa * scale);
+            }
+        }
+        cl.sync();    // no CTA leaves while a peer still reads its partials
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const int row = myrow + 4 * r;
+        if (row >= N || col >= N) break;
+        // a quarter turn maps edge pixels onto edge pixels
+        if (MODE != 0 && (row == 0 || col == 0 || row == N - 1 || col == N - 1)) continue;
+        atomicAdd(out + (long long)row * cs + (long long)col * ls, accB[r] * scale);
+        atomicAdd(out + (long long)col * cs + (long long)(N - 1 - row) * ls, accA[r] * scale);
+    }
+}
+
+template <int MODE, int WMAX, int ROWS>
+__global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_am, int s_ld, int R,
+                                                    const View *__restrict__ views, int half,
+                                                    int N, float scale, float *__restrict__ out,
+                                                    long long cs, long long ls,
+                                                    int *__restrict__ err, long long zs,
+                                                    long long zo, unsigned pair_bytes, int split)
+{
+    extern __shared__ float2 pairs[];          // [kSlots][WMAX]: views, then partners
+    gather_tile_rot<MODE, WMAX, ROWS>(s_am + blockIdx.z * zs, s_ld, R, views, half, N, scale,
+                                out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
+                                blockIdx.y, pairs, pair_bytes, split, blockIdx.x % split);
+}
+
+template <int MODE, int WMAX, int ROWS>
+int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
+                 long long ls, int *d_err, cudaStream_t st, const Stack &z)
+{
+    const int N = p.g.N, half = p.nv / 2;
+    // the staging area, which also holds the cluster reduction's partials
+    const size_t smem = std::max((size_t)kSlots * WMAX * sizeof(float2),
+                                 (size_t)2 * ROWS * 256 * sizeof(float));
+    dim3 grid((N + kTile - 1) / kTile, (N + kWarps * ROWS - 1) / (kWarps * ROWS), z.n);
+    auto k = k_gather_rot<MODE, WMAX, ROWS>;
+    RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
+    const unsigned pb = (unsigned)sizeof(float2);
+    const float scale = MODE == 0 ? p.dth : 1.f;
+    if (split == 1) {
+        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, half, N, scale, out, cs, ls,
+                                   d_err, z.in, z.out, pb, 1);
+        RG_CK_LAUNCH("k_gather_rot");
+        return RG_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, half, N, scale,
+                             out, cs, ls, d_err, z.in, z.out, pb, split));
+    RG_CK_LAUNCH("k_gather_rot (cluster)");
+    return RG_OK;
+}
+
+template <int MODE, int ROWS>
+int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
+                    long long ls, int *d_err, cudaStream_t st, const Stack &z)
+{
+    const int t = ROWS == 16 ? 2 : ROWS == 8 ? 1 : 0;
+    const int w = MODE == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
+    if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    if (w <= 512) return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    return set_error(RG_EUNSUPPORTED,
+                     "gather window of %d samples per tile exceeds 512 "
+                     "(image much coarser than the ray spacing)", w);
+}
+
+}  // namespace
+
+int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_t st,
+                      const Stack &z)
+{
+    const long long n = (long long)N * N;
+    const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
+    k_zero_image<<<dim3(blocks, 1, z.n), 256, 0, st>>>(out, N, cs, ls, z.out);
+    RG_CK_LAUNCH("k_zero_image");
+    return RG_OK;
+}
+
+int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
+                      long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
+                      const Stack &z)
+{
+    if (mode == 0) {
+        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    }
+    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+}
+
+}  // namespace rg

@@ -105,6 +105,8 @@ struct SSPlan {
     float dth = 0.f;               // view spacing (backprojection scale)
     bool adj_ok = true;            // every |rk| >= 1 (two-tap adjoint)
     bool contiguous = true;        // views are consecutive (not an OSEM subset)
+    bool rot_ok = false;           // all views of [theta0, theta0 + pi), an even count, on a
+                                   // grid symmetric under a quarter turn (gather_rot.cu)
     int device = -1;
     // TMA-staged Radon (radon_tma.cu): blocks of adjacent views whose line
     // windows fit st_bw entries (nblocks == 0: the direct kernels are used)
@@ -191,6 +193,19 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
                   int rows = 0, Stack z = Stack());
 // Rows per thread picked for (geometry, mode) by the autotuner (api.cu).
 int tuned_rows(const SSPlan &p, int mode);
+// Cluster size (1, 2 or 4) for the view split of a gather kernel k launched
+// on `grid` with `smem` bytes of shared memory (slantstack.cu).
+int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st);
+// Backprojection (mode 0) or matched adjoint (mode 1, interior pixels: the
+// edge pixels are left to the caller) with views paired a quarter turn
+// apart (p.rot_ok).  The output must be zeroed first; two partial sums are
+// added to each pixel.
+int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
+                      long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
+                      const Stack &z);
+// Zero an N x N strided image (a stack of z.n, z.out apart).
+int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_t st,
+                      const Stack &z);
 
 // f64.cu: FP64 operator pair (exact transposes), one thread per (ray, view).
 int launch_radon_f64(const SSPlan &p, const double *img, long long ics, long long ils,

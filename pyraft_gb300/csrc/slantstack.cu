@@ -136,6 +136,12 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         if ((views ? views[e] : e) != (views ? views[e - 1] : e - 1) + 1) p.contiguous = false;
     p.dth = (float)dth;
     p.adj_ok = adj_ok;
+    // views j and j + A/2 a quarter turn apart, and a grid that the turn
+    // maps onto itself (x and y on the same points, centred on 0)
+    const double pi = 3.14159265358979323846;
+    p.rot_ok = p.contiguous && nv == g.A && nv >= 2 && g.A % 2 == 0 &&
+               (views ? views[0] : 0) == 0 && fabs((thf - th0) - pi) <= 1e-12 * pi &&
+               g.itl_x == g.ibr_y && g.ibr_x == g.itl_y && g.itl_x == -g.ibr_x;
     for (int t = 0; t < 3; ++t) {
         p.wmax_bp[t] = (int)ceil(wbp[t] + 1e-6) + 4;
         p.wmax_adj[t] = (int)ceil(wadj[t] + 1e-6) + 4;
@@ -411,11 +417,16 @@ static int env_split()
 template <typename K>
 static int pick_split(K k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st)
 {
+    return gather_pick_split((const void *)k, smem, rows, nv, grid, st);
+}
+
+int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st)
+{
     const int forced = env_split();
     if (forced) return (rows % forced == 0 && nv >= forced) ? forced : 1;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 1;
-    const auto key = std::make_pair((const void *)k, dev * 4096 + (int)(smem >> 10));
+    const auto key = std::make_pair(k, dev * 4096 + (int)(smem >> 10));
     SplitOcc occ;
     bool have = false;
     {
@@ -539,12 +550,24 @@ static int gather_rows(const SSPlan &p, int rows, const float *s_am, int s_ld, f
     return gather_mode<MODE, 4, EM>(p, w, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
 }
 
+// RG_GATHER_ROT=0 keeps the one-view backprojection and adjoint where the
+// paired ones apply.
+static bool rot_enabled()
+{
+    const char *e = getenv("RG_GATHER_ROT");
+    return !(e && !strcmp(e, "0"));
+}
+
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                   long long cs, long long ls, float *em_x, const float *inv_sens, int *d_err,
                   cudaStream_t st, int rows, Stack z)
 {
     if (rows == 0) rows = tuned_rows(p, mode);
     if (mode == 0) {
+        if (!em_x && p.rot_ok && rot_enabled()) {
+            if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
+            return launch_gather_rot(p, 0, s_am, s_ld, out, cs, ls, d_err, st, rows, z);
+        }
         if (em_x)
             return gather_rows<0, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
         return gather_rows<0, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
@@ -554,6 +577,12 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                          "matched adjoint needs ray spacing >= pixel spacing along each line "
                          "(nrays <= size for the default extents)");
     if (mode == 1) {
+        if (!em_x && p.rot_ok && rot_enabled()) {
+            if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
+            if (int rc = adjoint_edges<1, false>(p, s_am, s_ld, out, cs, ls, nullptr, nullptr, st, z))
+                return rc;
+            return launch_gather_rot(p, 1, s_am, s_ld, out, cs, ls, d_err, st, rows, z);
+        }
         if (em_x)
             return gather_rows<1, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
         return gather_rows<1, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);

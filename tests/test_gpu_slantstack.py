@@ -304,6 +304,53 @@ def test_gather_cluster_split(orc, monkeypatch, split):
     assert rel(em_split, em_one) <= 1e-5
 
 
+# ---------------------------------------------------------------- paired views
+@pytest.mark.parametrize("n,r,a", [(64, 64, 48), (255, 256, 180), (97, 90, 64), (96, 120, 40)])
+@pytest.mark.parametrize("rows,split", [("4", "1"), ("8", "2"), ("16", "1"), ("16", "4")])
+def test_gathers_quarter_turn_pairs(orc, monkeypatch, n, r, a, rows, split):
+    """The backprojection and the matched adjoint with views paired a quarter
+    turn apart (an even number of views over [0, pi) on the symmetric
+    default grid) against the one-view kernels (RG_GATHER_ROT=0) and the
+    oracle, for each tile height and cluster split.  The adjoint's sinogram
+    has every ray nonzero except the one exact grid tie (see
+    test_adjoint_vs_oracle_transpose), so its edge pixels are exercised."""
+    rng = np.random.default_rng(n + 3 * a)
+    s = inner_sino(rng, r, a)
+    sf = rng.random((r, a))
+    sf[-1, 0] = 0.0
+    monkeypatch.setenv("RG_GATHER_ROWS", rows)
+    monkeypatch.setenv("RG_GATHER_SPLIT", split)
+    adjoint = r <= n                             # the two-tap adjoint's condition
+    paired = np.asarray(rg.backprojection(sino_img(s), (SLANT, (n, n), 0)))
+    if adjoint:
+        adj = np.asarray(rg.radon_transpose(sino_img(sf), (n, n), SLANT))
+    monkeypatch.setenv("RG_GATHER_ROT", "0")
+    single = np.asarray(rg.backprojection(sino_img(s), (SLANT, (n, n), 0)))
+    assert rel(paired, orc.backprojection_slantstack(s, n)) <= 1e-5
+    assert rel(paired, single) <= 1e-6
+    if adjoint:
+        adj1 = np.asarray(rg.radon_transpose(sino_img(sf), (n, n), SLANT))
+        assert rel(adj, orc.radon_slantstack_transpose(sf, n)) <= 1e-5
+        assert rel(adj, adj1) <= 1e-6
+
+
+def test_backprojection_quarter_turn_not_applicable(orc):
+    """Odd view counts, spans other than pi and off-centre grids keep the
+    one-view kernel; results match the oracle either way."""
+    rng = np.random.default_rng(77)
+    s = inner_sino(rng, 64, 41)
+    assert rel(rg.backprojection(sino_img(s), (SLANT, (64, 64), 0)),
+               orc.backprojection_slantstack(s, 64)) <= 1e-5
+    s = inner_sino(rng, 64, 40)
+    tl, br = (0.0, 1.0), (0.75 * math.pi, -1.0)
+    bp = rg.backprojection(sino_img(s, tl, br), (SLANT, (64, 64), 0))
+    assert rel(bp, orc.backprojection_slantstack(s, 64, sino_corners=tl + br)) <= 1e-5
+    ic = ((-1.0, 0.8), (0.8, -1.0))
+    bp = rg.backprojection(sino_img(s), (SLANT, (64, 64), 0), top_left=ic[0], bottom_right=ic[1])
+    ref = orc.backprojection_slantstack(s, 64, img_corners=ic[0] + ic[1])
+    assert rel(bp, ref) <= 1e-5
+
+
 # ---------------------------------------------------------------- TMA-staged Radon
 @pytest.mark.parametrize("n,r,a", [(64, 64, 48), (255, 256, 180), (200, 300, 90), (512, 512, 360)])
 def test_radon_tma_vs_direct_and_oracle(orc, monkeypatch, n, r, a):
