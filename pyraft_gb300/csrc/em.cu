@@ -11,7 +11,10 @@
 //   2. Radon over the subset's views with the EM ratio fused into the
 //      epilogue: r = y / (A x), 0 where A x == 0;
 //   3. matched-adjoint gather of r over the subset's views with the update
-//      fused into the epilogue: x <- x * (A^T r) * (1 / A^T 1).
+//      fused into the epilogue: x <- x * (A^T r) * (1 / A^T 1).  Where the
+//      subset's views pair up a quarter turn apart (gather_rot.cu), the
+//      paired gather writes A^T r to scratch and the update is its own
+//      elementwise pass.
 // The sensitivities A_s^T 1 of each subset are accumulated in FP64 once per
 // call and stored as reciprocals (0 where the sensitivity is 0, which also
 // zeroes pixels that no ray of the subset reaches).
@@ -38,7 +41,7 @@ struct Holders {
 size_t em_ss_ws(int N, int R, int A, int S)
 {
     const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)N * N * sizeof(float);
-    return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S});
+    return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S, img});
 }
 
 size_t em_dda_ws(int L, int C, int R, int A, int S)
@@ -74,6 +77,9 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
     float2 *prow = (float2 *)s.take(radon_pairs_bytes(N));
     float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N));
     float *inv = (float *)s.take((size_t)N * N * sizeof(float) * S);
+    // gather output of the paired kernels, whose two partial sums per pixel
+    // rule out the fused update: x <- x * g * inv follows as its own pass
+    float *gsum = (float *)s.take((size_t)N * N * sizeof(float));
     int rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
     for (int k = 0; k < S && !rc; ++k) {
         float *ik = inv + (size_t)k * N * N;
@@ -88,8 +94,14 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
         for (int k = 0; k < S && !rc; ++k) {
             if ((rc = launch_line_pairs(x, N, 1, N, prow, pcol, st))) break;
             if ((rc = launch_radon(*plans[k], prow, pcol, ratio, R, y_am, R, st))) break;
-            rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, nullptr, 0, 0, x,
-                               inv + (size_t)k * N * N, nullptr, st);
+            if (plans[k]->rot_ok && gather_rot_enabled()) {
+                rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, gsum, N, 1, nullptr, nullptr,
+                                   nullptr, st);
+                if (!rc) rc = launch_em_update(x, gsum, inv + (size_t)k * N * N, (size_t)N * N, st);
+            } else {
+                rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, nullptr, 0, 0, x,
+                                   inv + (size_t)k * N * N, nullptr, st);
+            }
         }
     return rc;
 }

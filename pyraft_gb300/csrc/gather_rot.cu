@@ -69,7 +69,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
     constexpr unsigned kPartner = kPairSlots * WMAX * 8;  // byte offset of the partner windows
     __shared__ SlotInfo slot[kPairSlots];
     __shared__ int slotW[kPairSlots];
-    __shared__ int slotView[kPairSlots];
+    __shared__ int slotView[2 * kPairSlots];             // sinogram rows: views, then partners
     __shared__ float slotP[kPairSlots];
     __shared__ float slotDelta[2 * kPairSlots];           // views, then partners
 
@@ -97,7 +97,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
         const int nslot = min(kPairSlots, vend - chunk);
         if (warp == 0 && lane < kPairSlots) {
             SlotInfo si = {0u, 0, 0, INT_MIN};
-            int W = 0, view = 0;
+            int W = 0, view = 0, view2 = 0;
             float P = 0.f, d0 = 0.f, d1 = 0.f;
             if (lane < nslot) {
                 const View &v = views[chunk + lane];
@@ -120,6 +120,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
                     atomicOr(err, 1);
                 }
                 view = v.view;
+                view2 = views[chunk + lane + half].view;
                 P = v.P;
                 d0 = v.delta;
                 d1 = views[chunk + lane + half].delta;
@@ -127,6 +128,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             slot[lane] = si;
             slotW[lane] = W;
             slotView[lane] = view;
+            slotView[kPairSlots + lane] = view2;
             slotP[lane] = P;
             slotDelta[lane] = d0;
             slotDelta[kPairSlots + lane] = d1;
@@ -139,8 +141,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             const int s = q < kPairSlots ? q : q - kPairSlots;
             if (s >= nslot) continue;
             const int nlo = slot[s].nlo, W = slotW[s];
-            const float *__restrict__ row =
-                s_am + (size_t)(slotView[s] + (q < kPairSlots ? 0 : half)) * s_ld;
+            const float *__restrict__ row = s_am + (size_t)slotView[q] * s_ld;
             const float d = slotDelta[q];
             for (int e = lane; e < W; e += 32) {
                 const int n = nlo + e;

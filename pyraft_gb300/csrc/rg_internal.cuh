@@ -105,8 +105,8 @@ struct SSPlan {
     float dth = 0.f;               // view spacing (backprojection scale)
     bool adj_ok = true;            // every |rk| >= 1 (two-tap adjoint)
     bool contiguous = true;        // views are consecutive (not an OSEM subset)
-    bool rot_ok = false;           // all views of [theta0, theta0 + pi), an even count, on a
-                                   // grid symmetric under a quarter turn (gather_rot.cu)
+    bool rot_ok = false;           // second half of the views = first half + pi/2, on a grid
+                                   // symmetric under a quarter turn (gather_rot.cu)
     int device = -1;
     // TMA-staged Radon (radon_tma.cu): blocks of adjacent views whose line
     // windows fit st_bw entries (nblocks == 0: the direct kernels are used)
@@ -203,6 +203,9 @@ int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, c
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
                       const Stack &z);
+// Whether launch_gather takes the paired path where a plan allows it
+// (RG_GATHER_ROT=0 turns it off).
+bool gather_rot_enabled();
 // Zero an N x N strided image (a stack of z.n, z.out apart).
 int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_t st,
                       const Stack &z);

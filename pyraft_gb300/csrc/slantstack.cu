@@ -136,12 +136,17 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
         if ((views ? views[e] : e) != (views ? views[e - 1] : e - 1) + 1) p.contiguous = false;
     p.dth = (float)dth;
     p.adj_ok = adj_ok;
-    // views j and j + A/2 a quarter turn apart, and a grid that the turn
-    // maps onto itself (x and y on the same points, centred on 0)
+    // The plan's second half of views is its first half a quarter turn on
+    // (view j + A/2 for view j: all views, or an OSEM subset when the
+    // subset count divides A/2), over a span of pi, on a grid that the turn
+    // maps onto itself (x and y on the same points, centred on 0).
     const double pi = 3.14159265358979323846;
-    p.rot_ok = p.contiguous && nv == g.A && nv >= 2 && g.A % 2 == 0 &&
-               (views ? views[0] : 0) == 0 && fabs((thf - th0) - pi) <= 1e-12 * pi &&
+    p.rot_ok = nv >= 2 && nv % 2 == 0 && g.A % 2 == 0 && fabs((thf - th0) - pi) <= 1e-12 * pi &&
                g.itl_x == g.ibr_y && g.ibr_x == g.itl_y && g.itl_x == -g.ibr_x;
+    for (int e = 0; e < nv / 2 && p.rot_ok; ++e) {
+        const int j = views ? views[e] : e, j2 = views ? views[e + nv / 2] : e + nv / 2;
+        p.rot_ok = j2 == j + g.A / 2;
+    }
     for (int t = 0; t < 3; ++t) {
         p.wmax_bp[t] = (int)ceil(wbp[t] + 1e-6) + 4;
         p.wmax_adj[t] = (int)ceil(wadj[t] + 1e-6) + 4;
@@ -552,7 +557,7 @@ static int gather_rows(const SSPlan &p, int rows, const float *s_am, int s_ld, f
 
 // RG_GATHER_ROT=0 keeps the one-view backprojection and adjoint where the
 // paired ones apply.
-static bool rot_enabled()
+bool gather_rot_enabled()
 {
     const char *e = getenv("RG_GATHER_ROT");
     return !(e && !strcmp(e, "0"));
@@ -564,7 +569,7 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
 {
     if (rows == 0) rows = tuned_rows(p, mode);
     if (mode == 0) {
-        if (!em_x && p.rot_ok && rot_enabled()) {
+        if (!em_x && p.rot_ok && gather_rot_enabled()) {
             if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
             return launch_gather_rot(p, 0, s_am, s_ld, out, cs, ls, d_err, st, rows, z);
         }
@@ -577,7 +582,7 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                          "matched adjoint needs ray spacing >= pixel spacing along each line "
                          "(nrays <= size for the default extents)");
     if (mode == 1) {
-        if (!em_x && p.rot_ok && rot_enabled()) {
+        if (!em_x && p.rot_ok && gather_rot_enabled()) {
             if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
             if (int rc = adjoint_edges<1, false>(p, s_am, s_ld, out, cs, ls, nullptr, nullptr, st, z))
                 return rc;
