@@ -39,8 +39,25 @@ METRIC = "FBP GUPS (2048^2 image, 1800 views, 2048 rays; Ram-Lak + slant-stack B
 UNIT = "GUPS"
 UPDATES = N * N * A
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) of one backprojection
-# launch at this size (profiles/bp_2048x1800_ncu.md).
-BP_TRAFFIC_BYTES = 14961152
+# launch at this size (profiles/bp_rot_2048x1800_ncu.md): the sinogram and
+# the zeroed image that the two partial sums per pixel are added to.
+BP_TRAFFIC_BYTES = 31808512
+# kernels of one FBP step: k_to_am, k_filter_fft, k_zero_image, k_gather_rot
+LAUNCHES_PER_FBP = 4
+
+
+def smem_ceiling(updates, ms, sms, sm_mhz):
+    """The gathers' shared-memory roofline: each update reads one 8-byte
+    pair from shared memory, and a warp's 64-bit load takes two 128-byte
+    wavefronts, at one wavefront per SM per clock: 16 updates per SM per
+    clock."""
+    mhz = sm_mhz or 2070.0
+    peak = 16.0 * sms * mhz * 1e6 / 1e9
+    got = updates / (ms * 1e-3) / 1e9
+    return {"unit": "GUPS", "achieved": round(got, 1), "peak": round(peak, 1),
+            "frac": round(got / peak, 3), "sms": sms, "sm_mhz": mhz,
+            "model": "8 B of shared memory per update; 2 wavefronts per warp-wide 64-bit "
+                     "load; 1 wavefront per SM per clock"}
 
 
 def env_rank():
@@ -470,6 +487,7 @@ def main():
     alg_bytes = 8 * UPDATES + compulsory
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / (bp_ms * 1e-3) / 1e9
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
 
     # ---- the other operators of the path at the same size (one call each)
     def timed(fn, reps=5):
@@ -611,24 +629,25 @@ def main():
                            "mode": "upload, FBP, download back to back on one stream, "
                                    "per-step CUDA events"},
                 "finite_and_equal": ok},
-        "roofline": {"bound": "hbm", "kernel": "k_gather<0> (backprojection)",
+        "roofline": {"bound": "hbm",
+                     "kernel": "k_gather_rot<0> (backprojection, views paired a quarter turn "
+                               "apart; timed as the call, with its k_zero_image)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "traffic": BP_TRAFFIC_BYTES,
                      "algorithmic_bytes": alg_bytes, "kernel_ms": round(bp_ms, 4),
                      "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
                      "model": "8 B per (pixel, view) update + image and sinogram bytes once",
                      "note": "frac > 1 because every staged sinogram sample serves ~1000 "
-                             "updates from shared memory: ncu measures only the compulsory "
-                             "15 MB of DRAM traffic per launch; the kernel is bound by "
-                             "instruction issue (87 % of issue slots, profiles/"
-                             "bp_2048x1800_ncu.md)"},
+                             "updates from shared memory, so DRAM carries only the compulsory "
+                             "bytes; the bound is shared-memory bandwidth (smem_ceiling)",
+                     "smem_ceiling": smem_ceiling(UPDATES, bp_ms, sms, clk["sm_mhz"])},
         "ops": {"radon_gups": round(R * A * N / (radon_ms * 1e-3) / 1e9, 1),
                 "radon_ms": round(radon_ms, 4),
                 "adjoint_gups": round(UPDATES / (adj_ms * 1e-3) / 1e9, 1),
                 "adjoint_ms": round(adj_ms, 4),
                 "backprojection_gups": round(UPDATES / (bp_ms * 1e-3) / 1e9, 1),
                 "note": "single calls at 2048^2 x 1800 (view-major sinogram), L2 flushed"},
-        "gpu_launches": 3 * args.steps,
+        "gpu_launches": LAUNCHES_PER_FBP * args.steps,
         "clocks": clk,
         "wall_s_timed_region": round(wall, 3),
     }

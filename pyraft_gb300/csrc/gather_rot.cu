@@ -59,8 +59,9 @@ __global__ void k_zero_image(float *__restrict__ out, int N, long long cs, long 
 // k_adjoint_edges, as in gather_tile with edge_fixup).
 template <int MODE, int WMAX, int ROWS>
 __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, int s_ld, int R,
-                                                const View *__restrict__ views, int half, int N,
-                                                float scale, float *__restrict__ out, long long cs,
+                                                const View *__restrict__ views, int half,
+                                                int roff, int N, float scale,
+                                                float *__restrict__ out, long long cs,
                                                 long long ls, int *__restrict__ err, int tx,
                                                 int ty, float2 *__restrict__ pairs,
                                                 unsigned pair_bytes, int split, int rank)
@@ -69,7 +70,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
     constexpr unsigned kPartner = kPairSlots * WMAX * 8;  // byte offset of the partner windows
     __shared__ SlotInfo slot[kPairSlots];
     __shared__ int slotW[kPairSlots];
-    __shared__ int slotView[2 * kPairSlots];             // sinogram rows: views, then partners
+    __shared__ int slotView[kPairSlots];
     __shared__ float slotP[kPairSlots];
     __shared__ float slotDelta[2 * kPairSlots];           // views, then partners
 
@@ -97,7 +98,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
         const int nslot = min(kPairSlots, vend - chunk);
         if (warp == 0 && lane < kPairSlots) {
             SlotInfo si = {0u, 0, 0, INT_MIN};
-            int W = 0, view = 0, view2 = 0;
+            int W = 0, view = 0;
             float P = 0.f, d0 = 0.f, d1 = 0.f;
             if (lane < nslot) {
                 const View &v = views[chunk + lane];
@@ -120,7 +121,6 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
                     atomicOr(err, 1);
                 }
                 view = v.view;
-                view2 = views[chunk + lane + half].view;
                 P = v.P;
                 d0 = v.delta;
                 d1 = views[chunk + lane + half].delta;
@@ -128,7 +128,6 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             slot[lane] = si;
             slotW[lane] = W;
             slotView[lane] = view;
-            slotView[kPairSlots + lane] = view2;
             slotP[lane] = P;
             slotDelta[lane] = d0;
             slotDelta[kPairSlots + lane] = d1;
@@ -141,7 +140,8 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             const int s = q < kPairSlots ? q : q - kPairSlots;
             if (s >= nslot) continue;
             const int nlo = slot[s].nlo, W = slotW[s];
-            const float *__restrict__ row = s_am + (size_t)slotView[q] * s_ld;
+            const float *__restrict__ row =
+                s_am + (size_t)(slotView[s] + (q < kPairSlots ? 0 : roff)) * s_ld;
             const float d = slotDelta[q];
             for (int e = lane; e < W; e += 32) {
                 const int n = nlo + e;
@@ -240,13 +240,14 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
 template <int MODE, int WMAX, int ROWS>
 __global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_am, int s_ld, int R,
                                                     const View *__restrict__ views, int half,
-                                                    int N, float scale, float *__restrict__ out,
+                                                    int roff, int N, float scale,
+                                                    float *__restrict__ out,
                                                     long long cs, long long ls,
                                                     int *__restrict__ err, long long zs,
                                                     long long zo, unsigned pair_bytes, int split)
 {
     extern __shared__ float2 pairs[];          // [kSlots][WMAX]: views, then partners
-    gather_tile_rot<MODE, WMAX, ROWS>(s_am + blockIdx.z * zs, s_ld, R, views, half, N, scale,
+    gather_tile_rot<MODE, WMAX, ROWS>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
                                 out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
                                 blockIdx.y, pairs, pair_bytes, split, blockIdx.x % split);
 }
@@ -255,7 +256,8 @@ template <int MODE, int WMAX, int ROWS>
 int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                  long long ls, int *d_err, cudaStream_t st, const Stack &z)
 {
-    const int N = p.g.N, half = p.nv / 2;
+    // half: view pairs; roff: sinogram rows between a view and its partner
+    const int N = p.g.N, half = p.nv / 2, roff = p.g.A / 2;
     // the staging area, which also holds the cluster reduction's partials
     const size_t smem = std::max((size_t)kSlots * WMAX * sizeof(float2),
                                  (size_t)2 * ROWS * 256 * sizeof(float));
@@ -266,7 +268,7 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     const unsigned pb = (unsigned)sizeof(float2);
     const float scale = MODE == 0 ? p.dth : 1.f;
     if (split == 1) {
-        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, half, N, scale, out, cs, ls,
+        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, half, roff, N, scale, out, cs, ls,
                                    d_err, z.in, z.out, pb, 1);
         RG_CK_LAUNCH("k_gather_rot");
         return RG_OK;
@@ -283,8 +285,8 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     cfg.stream = st;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, half, N, scale,
-                             out, cs, ls, d_err, z.in, z.out, pb, split));
+    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, half, roff, N,
+                             scale, out, cs, ls, d_err, z.in, z.out, pb, split));
     RG_CK_LAUNCH("k_gather_rot (cluster)");
     return RG_OK;
 }
