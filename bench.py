@@ -41,7 +41,7 @@ UPDATES = N * N * A
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) of one backprojection
 # launch at this size (profiles/bp_rot_2048x1800_ncu.md): the sinogram and
 # the zeroed image that the two partial sums per pixel are added to.
-BP_TRAFFIC_BYTES = 31808512
+BP_TRAFFIC_BYTES = 31642880
 # kernels of one FBP step: k_to_am, k_filter_fft, k_zero_image, k_gather_rot
 LAUNCHES_PER_FBP = 4
 
