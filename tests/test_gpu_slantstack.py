@@ -334,6 +334,28 @@ def test_gathers_quarter_turn_pairs(orc, monkeypatch, n, r, a, rows, split):
         assert rel(adj, adj1) <= 1e-6
 
 
+@pytest.mark.parametrize("n,r,a", [(2, 2, 2), (5, 5, 4), (17, 17, 10), (33, 20, 30), (40, 40, 2)])
+def test_gathers_quarter_turn_small_geometries(orc, monkeypatch, n, r, a):
+    """Paired gathers on images much smaller than a tile, and with a single
+    view pair, against the one-view kernels and the oracle.  The views start
+    1e-3 rad past 0 (the span stays pi, so they still pair): at exact
+    multiples of 45 degrees these tiny grids put many samples exactly on the
+    validity limits, where the oracle's FP64 rounding decides."""
+    rng = np.random.default_rng(n * 7 + a)
+    s = rng.random((r, a))
+    tl, br = (1e-3, 1.0), (math.pi + 1e-3, -1.0)
+    sc = tl + br
+    monkeypatch.setenv("RG_GATHER_ROT", "1")
+    bp = np.asarray(rg.backprojection(sino_img(s, tl, br), (SLANT, (n, n), 0)))
+    adj = np.asarray(rg.radon_transpose(sino_img(s, tl, br), (n, n), SLANT))
+    monkeypatch.setenv("RG_GATHER_ROT", "0")
+    bp1 = np.asarray(rg.backprojection(sino_img(s, tl, br), (SLANT, (n, n), 0)))
+    adj1 = np.asarray(rg.radon_transpose(sino_img(s, tl, br), (n, n), SLANT))
+    assert rel(bp, bp1) <= 1e-6 and rel(adj, adj1) <= 1e-6
+    assert rel(bp, orc.backprojection_slantstack(s, n, sino_corners=sc)) <= 1e-5
+    assert rel(adj, orc.radon_slantstack_transpose(s, n, sino_corners=sc)) <= 1e-5
+
+
 def test_backprojection_quarter_turn_not_applicable(orc):
     """Odd view counts, spans other than pi and off-centre grids keep the
     one-view kernel; results match the oracle either way."""
