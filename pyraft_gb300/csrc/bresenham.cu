@@ -14,7 +14,8 @@
 //
 // Radon: one thread per (ray, view); lanes run over rays, so the
 // view-major output is written coalesced.  Sums are FP32 products of the
-// FP32 image and the FP64 sigma rounded to FP32, accumulated in FP32 with
+// FP32 image and an FP32 sigma (dda_update: the reference's sigma to within
+// FP32 rounding, without its FP64 divisions), accumulated in FP32 with
 // Kahan compensation.  Transpose: same walk, FP32 atomicAdd scatter into
 // the image (order of additions varies between runs, at FP32 rounding level).
 //
@@ -33,6 +34,8 @@ struct DDA {
     double epsilon, epsilon_update, delta_x, delta_y, delta_slow;
     int Delta_i, Delta_j, Delta_slow, Delta_fast;
     double sigma_tilde;
+    double sigma_per_eps;        // sigma_tilde / epsilon_update (0 when the update is 0)
+    float sigma32, sigma_tilde32, sigma_per_eps32;   // FP32 sigma (kDdaSigma32)
     int lines, columns;
     double bbox_tl_x, bbox_tl_y, bbox_br_x, bbox_br_y;
     double tl_x, tl_y;
@@ -92,35 +95,68 @@ __device__ __forceinline__ void dda_set_theta(DDA &it, double c, double s)
     it.epsilon_update = fabs(__ddiv_rn(__dmul_rn(df, sm), lg));
     it.delta_slow = fabs(ds);
     it.sigma_tilde = fabs(__ddiv_rn(df, lg));
+    it.sigma_per_eps = it.epsilon_update > 0.0 ? __ddiv_rn(it.sigma_tilde, it.epsilon_update) : 0.0;
+    it.sigma_tilde32 = (float)it.sigma_tilde;
+    it.sigma_per_eps32 = (float)it.sigma_per_eps;
 }
 
+// Forms of the walk's sigma (the pixel decisions are the same in all).
+constexpr int kDdaExact = 0;     // the reference's FP64 sigma (traced sequences)
+constexpr int kDdaSigma64 = 1;   // FP64 sigma without divisions (FP64 sums)
+constexpr int kDdaSigma32 = 2;   // FP32 sigma without divisions (FP32 sums)
+
+// One step of the walk.  The pixel decisions (epsilon's adds, subtracts and
+// comparison) are the reference's FP64 operations in every form; epsilon
+// and delta_slow are never negative, so the comparison is made on their bit
+// patterns, whose integer order is theirs.  kDdaExact also splits sigma at
+// a slow move as the reference does, with two divisions: alpha =
+// (delta_slow - eps_prev) / eps, sigma = sigma_tilde alpha / (1 + alpha).
+// Since eps + delta_slow - eps_prev = epsilon_update, that is sigma =
+// (delta_slow - eps_prev) * sigma_tilde / epsilon_update, which the other
+// forms compute with one subtract and one multiply by a per-ray constant
+// (equal to within rounding: FP64 for kDdaSigma64, FP32 for kDdaSigma32,
+// whose kernels sum in FP32).  FP64 division is a long sequence on a slow
+// pipe, and a slow move can come every other step.
+template <int FORM>
 __device__ __forceinline__ void dda_update(DDA &it)
 {
     if (it.slow_move) {
         if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
-        it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
+        if (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32 - it.sigma32;
+        else it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
         it.slow_move = 0;
     } else {
         if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
         const double eps_prev = it.epsilon;
         it.epsilon = __dadd_rn(it.epsilon, it.epsilon_update);
-        it.slow_move = (it.epsilon > it.delta_slow);
+        if (FORM == kDdaExact)
+            it.slow_move = (it.epsilon > it.delta_slow);
+        else
+            it.slow_move = __double_as_longlong(it.epsilon) > __double_as_longlong(it.delta_slow);
         if (it.slow_move) {
             it.epsilon = __dsub_rn(it.epsilon, it.delta_slow);
-            double alpha;
-            if (it.epsilon != 0.0) {
-                alpha = __ddiv_rn(__dsub_rn(it.delta_slow, eps_prev), it.epsilon);
-                alpha = __ddiv_rn(alpha, __dadd_rn(1.0, alpha));
+            if (FORM == kDdaExact) {
+                double alpha;
+                if (it.epsilon != 0.0) {
+                    alpha = __ddiv_rn(__dsub_rn(it.delta_slow, eps_prev), it.epsilon);
+                    alpha = __ddiv_rn(alpha, __dadd_rn(1.0, alpha));
+                } else {
+                    alpha = 1.0;
+                }
+                it.sigma = __dmul_rn(alpha, it.sigma_tilde);
+            } else if (FORM == kDdaSigma64) {
+                it.sigma = __dmul_rn(__dsub_rn(it.delta_slow, eps_prev), it.sigma_per_eps);
             } else {
-                alpha = 1.0;
+                it.sigma32 = (float)__dsub_rn(it.delta_slow, eps_prev) * it.sigma_per_eps32;
             }
-            it.sigma = __dmul_rn(alpha, it.sigma_tilde);
         } else {
-            it.sigma = it.sigma_tilde;
+            if (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32;
+            else it.sigma = it.sigma_tilde;
         }
     }
 }
 
+template <int FORM>
 __device__ __forceinline__ void dda_set_t(DDA &it, double t)
 {
     it.slow_move = 0;
@@ -130,6 +166,7 @@ __device__ __forceinline__ void dda_set_t(DDA &it, double t)
         it.epsilon = 0.0;
         it.epsilon_update = 0.0;
         it.sigma = it.sigma_tilde;
+        it.sigma32 = it.sigma_tilde32;
         return;
     }
     if (it.cos_theta == 0.0) {
@@ -138,6 +175,7 @@ __device__ __forceinline__ void dda_set_t(DDA &it, double t)
         it.epsilon = 0.0;
         it.epsilon_update = 0.0;
         it.sigma = it.sigma_tilde;
+        it.sigma32 = it.sigma_tilde32;
         return;
     }
     const double sx = __ddiv_rn(__dsub_rn(__dmul_rn(t, it.cos_theta), it.x0), it.sin_theta);
@@ -150,11 +188,12 @@ __device__ __forceinline__ void dda_set_t(DDA &it, double t)
                                          __dmul_rn(0.5, (double)it.Delta_i)), it.delta_y))));
         if (!it.fast_is_i) {
             it.j -= it.Delta_j;
-            dda_update(it);
+            dda_update<FORM>(it);
         } else {
             it.epsilon = __dsub_rn(it.epsilon, fabs(it.delta_y));
             it.epsilon = __ddiv_rn(it.epsilon, it.cos_theta);
             it.sigma = fabs(it.epsilon);
+            it.sigma32 = (float)it.sigma;
             it.epsilon = fabs(__dmul_rn(it.sigma, it.sin_theta));
         }
     } else {
@@ -165,11 +204,12 @@ __device__ __forceinline__ void dda_set_t(DDA &it, double t)
                                          __dmul_rn(0.5, (double)it.Delta_j)), it.delta_x))));
         if (it.fast_is_i) {
             it.i -= it.Delta_i;
-            dda_update(it);
+            dda_update<FORM>(it);
         } else {
             it.epsilon = __dsub_rn(it.epsilon, fabs(it.delta_x));
             it.epsilon = __ddiv_rn(it.epsilon, it.sin_theta);
             it.sigma = fabs(it.epsilon);
+            it.sigma32 = (float)it.sigma;
             it.epsilon = fabs(__dmul_rn(it.sigma, it.cos_theta));
         }
     }
@@ -197,15 +237,15 @@ __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__r
     dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
     dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
     const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
-    dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     float acc = 0.f, comp = 0.f;
     const int cap = 2 * (g.lines + g.columns) + 8;
     for (int step = 0; step < cap && !dda_end(it); ++step) {
-        const float x = __ldg(img + (long long)it.i * ics + (long long)it.j * ils) * (float)it.sigma;
+        const float x = __ldg(img + (long long)it.i * ics + (long long)it.j * ils) * it.sigma32;
         const float y = x - comp, t = acc + y;
         comp = (t - acc) - y;
         acc = t;
-        dda_update(it);
+        dda_update<kDdaSigma32>(it);
     }
     float val = acc - comp;
     if (RATIO) {
@@ -248,13 +288,13 @@ __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double 
     dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
     dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
     const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
-    dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
     for (int step = 0; step < cap && !dda_end(it); ++step) {
         const size_t e = (size_t)it.i * g.columns + it.j;
-        if (sv != 0.f) atomicAdd(img_c + e, sv * (float)it.sigma);
-        if (den) atomicAdd(den + e, (float)it.sigma);
-        dda_update(it);
+        if (sv != 0.f) atomicAdd(img_c + e, sv * it.sigma32);
+        if (den) atomicAdd(den + e, it.sigma32);
+        dda_update<kDdaSigma32>(it);
     }
 }
 
@@ -275,13 +315,13 @@ __global__ __launch_bounds__(128) void k_bres_norm_sums(DDAGeom g, const double 
     dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
     dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
     const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
-    dda_set_t(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    dda_set_t<kDdaSigma64>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
     for (int step = 0; step < cap && !dda_end(it); ++step) {
         const size_t e = (size_t)it.i * g.columns + it.j;
         if (sv != 0.0) atomicAdd(num + e, sv * it.sigma);
         atomicAdd(den + e, it.sigma);
-        dda_update(it);
+        dda_update<kDdaSigma64>(it);
     }
 }
 
@@ -330,7 +370,7 @@ __global__ void k_dda_trace(int lines, int columns, double tl_x, double tl_y, do
     DDA it;
     dda_set_image(it, lines, columns, tl_x, tl_y, br_x, br_y);
     dda_set_theta(it, cst[3 * r], cst[3 * r + 1]);
-    dda_set_t(it, cst[3 * r + 2]);
+    dda_set_t<kDdaExact>(it, cst[3 * r + 2]);
     int cnt = 0;
     const int limit = 2 * (lines + columns) + 8;
     while (!dda_end(it) && cnt < limit) {
@@ -340,7 +380,7 @@ __global__ void k_dda_trace(int lines, int columns, double tl_x, double tl_y, do
             os[(size_t)r * cap + cnt] = it.sigma;
         }
         ++cnt;
-        dda_update(it);
+        dda_update<kDdaExact>(it);
     }
     ocount[r] = cnt;
 }
