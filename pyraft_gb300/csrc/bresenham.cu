@@ -23,6 +23,9 @@
 // monotone in both indices, so the cap is never reached by a valid ray.
 #include <math.h>
 
+#include <algorithm>
+#include <vector>
+
 #include "rg_internal.cuh"
 
 namespace rg {
@@ -392,6 +395,200 @@ int launch_dda_trace(int lines, int columns, const double *corners, const double
                                                   corners[2], corners[3], d_cst, n, cap, oi, oj,
                                                   os, ocount);
     RG_CK_LAUNCH("k_dda_trace");
+    return RG_OK;
+}
+
+// ============================================================================
+// Recorded walks (DDAPlan).  Iterative reconstruction walks the same rays
+// in every sub-iteration, and the walk is bound by the FP64 pipe.  A plan
+// records each ray's walk once: per step one FP32 word, the step's sigma
+// (kDdaSigma32, what the walking kernels use) whose lowest mantissa bit is
+// replaced by the move flag (1: the step moved along the slow axis; the
+// weight changes by at most one unit in the last place, and unlike the
+// sign bit the flag survives a sigma of zero or a rounding just below
+// zero, which a slow move's remainder can be); per ray its entry pixel, the
+// pixel-index increments of a fast and a slow move, and its steps' offset
+// and count.  Replaying a ray is then a streamed read: a warp takes a ray,
+// its lanes consecutive steps, and a ballot over the slow bits gives each
+// lane its pixel (entry + s fast moves + (slow moves so far) x (slow - fast
+// increment)).  The pixel sequences are those of the walk, and the sigmas
+// within one unit in the last place, so results match the walking kernels
+// to FP32 rounding.
+
+struct DDARayRec {
+    long long off;     // first step in the step array
+    int count;         // steps (pixels) of the ray; 0 if it misses the image
+    int start;         // entry pixel, row-major index
+    int dfast, dslow;  // pixel-index increment of a fast / slow move
+};
+
+// Walk (ray i of view first + y * stride) and count (W = false) or record
+// (W = true) its steps.
+template <bool W>
+__global__ __launch_bounds__(128) void k_dda_plan(DDAGeom g, const double *__restrict__ cs_tab,
+                                                  int first, int stride,
+                                                  DDARayRec *__restrict__ rays,
+                                                  float *__restrict__ steps)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = first + blockIdx.y * stride;
+    if (i >= g.R) return;
+    const size_t r = (size_t)blockIdx.y * g.R + i;
+    DDA it;
+    dda_set_image(it, g.lines, g.columns, g.itl_x, g.itl_y, g.ibr_x, g.ibr_y);
+    dda_set_theta(it, cs_tab[2 * j], cs_tab[2 * j + 1]);
+    const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
+    dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
+    const int cap = 2 * (g.lines + g.columns) + 8;
+    const long long off = W ? rays[r].off : 0;
+    int n = 0;
+    if (!W) {
+        rays[r].start = it.i * g.columns + it.j;
+        rays[r].dfast = it.fast_is_i ? it.Delta_fast * g.columns : it.Delta_fast;
+        rays[r].dslow = it.fast_is_i ? it.Delta_slow : it.Delta_slow * g.columns;
+    }
+    int moved_slow = 0;
+    for (; n < cap && !dda_end(it); ++n) {
+        if (W) steps[off + n] = __uint_as_float((__float_as_uint(it.sigma32) & ~1u) | moved_slow);
+        moved_slow = it.slow_move;
+        dda_update<kDdaSigma32>(it);
+    }
+    if (!W) rays[r].count = n;
+}
+
+// Replay: warp per ray.  Radon: out_am[view row][i] = sum img * sigma (the
+// EM ratio y / Ax if y_am); transpose: img_c += s * sigma (atomics).
+template <int OP>
+__device__ __forceinline__ void dda_replay(const DDARayRec &rec, const float *__restrict__ steps,
+                                           const float *__restrict__ img_c, float *__restrict__ img_o,
+                                           float sv, float &sum)
+{
+    const int lane = threadIdx.x & 31;
+    const int dd = rec.dslow - rec.dfast;
+    int slows = 0;                     // slow moves before this chunk
+    for (int c = 0; c < rec.count; c += 32) {
+        const int s = c + lane;
+        const float w = s < rec.count ? __ldg(steps + rec.off + s) : 0.f;
+        const unsigned sb = __ballot_sync(0xffffffffu, __float_as_uint(w) & 1u);
+        const int mine = slows + __popc(sb & (0xffffffffu >> (31 - lane)));
+        slows += __popc(sb);
+        if (s < rec.count) {
+            const int pix = rec.start + s * rec.dfast + mine * dd;
+            if (OP == 0) sum = fmaf(__ldg(img_c + pix), w, sum);
+            else atomicAdd(img_o + pix, sv * w);
+        }
+    }
+}
+
+__global__ __launch_bounds__(256) void k_dda_plan_radon(const DDARayRec *__restrict__ rays,
+                                                        const float *__restrict__ steps,
+                                                        long long nrays, int R, int first,
+                                                        int stride, const float *__restrict__ img,
+                                                        float *__restrict__ out_am,
+                                                        const float *__restrict__ y_am)
+{
+    const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r >= nrays) return;                        // warp-uniform
+    const DDARayRec rec = rays[r];
+    float sum = 0.f;
+    dda_replay<0>(rec, steps, img, nullptr, 0.f, sum);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0) {
+        const int i = (int)(r % R), j = first + (int)(r / R) * stride;
+        const size_t e = (size_t)j * R + i;
+        float val = sum;
+        if (y_am) val = (val != 0.f) ? y_am[e] / val : 0.f;
+        out_am[e] = val;
+    }
+}
+
+__global__ __launch_bounds__(256) void k_dda_plan_transpose(const DDARayRec *__restrict__ rays,
+                                                            const float *__restrict__ steps,
+                                                            long long nrays, int R, int first,
+                                                            int stride,
+                                                            const float *__restrict__ s_am,
+                                                            float *__restrict__ img_c)
+{
+    const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r >= nrays) return;                        // warp-uniform
+    const int i = (int)(r % R), j = first + (int)(r / R) * stride;
+    const float sv = s_am[(size_t)j * R + i];
+    if (sv == 0.f) return;                         // warp-uniform
+    float unused = 0.f;
+    dda_replay<1>(rays[r], steps, nullptr, img_c, sv, unused);
+}
+
+void dda_plan_free(DDAPlan &p)
+{
+    if (p.rays) cudaFree(p.rays);
+    if (p.steps) cudaFree(p.steps);
+    p.rays = nullptr;
+    p.steps = nullptr;
+    p.nrays = 0;
+    p.total = 0;
+}
+
+// Builds the plan of views first, first + stride, ... (two walks: count,
+// then record).  Leaves p empty (and returns RG_OK) when its steps would
+// take more than `max_bytes` or more than a third of the free device memory.
+int dda_plan_build(const DDAGeom &g, const double *d_cs, int first, int stride,
+                   size_t max_bytes, DDAPlan &p, cudaStream_t st)
+{
+    dda_plan_free(p);
+    const int nv = (g.A - first + stride - 1) / stride;
+    if (nv <= 0) return RG_OK;
+    p.first = first;
+    p.stride = stride;
+    p.nrays = (long long)g.R * nv;
+    RG_CK(cudaMalloc(&p.rays, sizeof(DDARayRec) * (size_t)p.nrays));
+    DDARayRec *rays = (DDARayRec *)p.rays;
+    dim3 grid((g.R + 127) / 128, nv);
+    k_dda_plan<false><<<grid, 128, 0, st>>>(g, d_cs, first, stride, rays, nullptr);
+    RG_CK_LAUNCH("k_dda_plan (count)");
+    std::vector<DDARayRec> h((size_t)p.nrays);
+    RG_CK(cudaMemcpyAsync(h.data(), rays, sizeof(DDARayRec) * h.size(), cudaMemcpyDeviceToHost, st));
+    RG_CK(cudaStreamSynchronize(st));
+    long long total = 0;
+    for (auto &rec : h) {
+        rec.off = total;
+        total += rec.count;
+    }
+    size_t freeb = 0, totb = 0;
+    RG_CK(cudaMemGetInfo(&freeb, &totb));
+    const size_t bytes = sizeof(float) * (size_t)std::max(total, 1LL);
+    if (bytes > max_bytes || bytes > freeb / 3) {
+        dda_plan_free(p);
+        return RG_OK;
+    }
+    RG_CK(cudaMemcpyAsync(rays, h.data(), sizeof(DDARayRec) * h.size(), cudaMemcpyHostToDevice, st));
+    RG_CK(cudaMalloc(&p.steps, bytes));
+    k_dda_plan<true><<<grid, 128, 0, st>>>(g, d_cs, first, stride, rays, (float *)p.steps);
+    RG_CK_LAUNCH("k_dda_plan (record)");
+    RG_CK(cudaStreamSynchronize(st));   // h is released on return
+    p.total = total;
+    return RG_OK;
+}
+
+int launch_dda_plan_radon(const DDAGeom &g, const DDAPlan &p, const float *img_c, float *out_am,
+                          const float *y_am, cudaStream_t st)
+{
+    const long long threads = p.nrays * 32;
+    k_dda_plan_radon<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+        (const DDARayRec *)p.rays, (const float *)p.steps, p.nrays, g.R, p.first, p.stride, img_c,
+        out_am, y_am);
+    RG_CK_LAUNCH("k_dda_plan_radon");
+    return RG_OK;
+}
+
+int launch_dda_plan_transpose(const DDAGeom &g, const DDAPlan &p, const float *s_am, float *img_c,
+                              cudaStream_t st)
+{
+    const long long threads = p.nrays * 32;
+    k_dda_plan_transpose<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
+        (const DDARayRec *)p.rays, (const float *)p.steps, p.nrays, g.R, p.first, p.stride, s_am,
+        img_c);
+    RG_CK_LAUNCH("k_dda_plan_transpose");
     return RG_OK;
 }
 

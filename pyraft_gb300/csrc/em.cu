@@ -20,7 +20,12 @@
 // zeroes pixels that no ray of the subset reaches).
 //
 // DDA path (pyraft's em() default): the same loop over the DDA Radon with
-// the fused ratio, the DDA transpose, and an elementwise update.
+// the fused ratio, the DDA transpose, and an elementwise update.  The walks
+// are FP64-bound, so with two or more iterations each subset's walks are
+// recorded once (DDAPlan, bresenham.cu) and replayed as streamed reads.
+#include <stdlib.h>
+#include <string.h>
+
 #include <algorithm>
 #include <vector>
 
@@ -42,6 +47,30 @@ size_t em_ss_ws(int N, int R, int A, int S)
 {
     const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)N * N * sizeof(float);
     return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S, img});
+}
+
+// The DDA EM's recorded walks (freed with the call).  RG_DDA_PLAN=0 walks
+// every time; RG_DDA_PLAN_MAX_GB caps a plan's step array (default 48).
+struct DDAPlans {
+    std::vector<DDAPlan> p;
+    explicit DDAPlans(int n) : p(n) {}
+    ~DDAPlans()
+    {
+        for (auto &q : p) dda_plan_free(q);
+    }
+};
+
+bool dda_plans_enabled()
+{
+    const char *e = getenv("RG_DDA_PLAN");
+    return !(e && !strcmp(e, "0"));
+}
+
+size_t dda_plan_max_bytes()
+{
+    const char *e = getenv("RG_DDA_PLAN_MAX_GB");
+    const double gb = e ? atof(e) : 48.0;
+    return (size_t)(std::max(gb, 0.0) * (double)(1ull << 30));
 }
 
 size_t em_dda_ws(int L, int C, int R, int A, int S)
@@ -134,16 +163,30 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
     rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, y, st);
     if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, C, 1, L, C, st);
     if (!rc) rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
+    // Record each subset's walks once when they will be replayed (two walks
+    // per sub-iteration), memory permitting (dda_plan_build).
+    DDAPlans plans(S);
+    if (!rc && niter >= 2 && dda_plans_enabled())
+        for (int k = 0; k < S && !rc; ++k)
+            rc = dda_plan_build(g, cs, k, S, dda_plan_max_bytes(), plans.p[k], st);
+    auto radon_k = [&](int k) {
+        if (plans.p[k].steps) return launch_dda_plan_radon(g, plans.p[k], x, ratio, y, st);
+        return launch_bres_radon(g, cs, x, C, 1, ratio, 1, R, y, k, S, st);
+    };
+    auto transpose_k = [&](int k) {
+        if (plans.p[k].steps) return launch_dda_plan_transpose(g, plans.p[k], ratio, bp, st);
+        return launch_bres_transpose(g, cs, ratio, bp, k, S, st);
+    };
     for (int k = 0; k < S && !rc; ++k) {
         if ((rc = launch_fill(bp, npix, 0.f, st))) break;
-        if ((rc = launch_bres_transpose(g, cs, ratio, bp, k, S, st))) break;
+        if ((rc = transpose_k(k))) break;
         rc = launch_invert(bp, inv + (size_t)k * npix, npix, st);
     }
     for (int it = 0; it < niter && !rc; ++it)
         for (int k = 0; k < S && !rc; ++k) {
-            if ((rc = launch_bres_radon(g, cs, x, C, 1, ratio, 1, R, y, k, S, st))) break;
+            if ((rc = radon_k(k))) break;
             if ((rc = launch_fill(bp, npix, 0.f, st))) break;
-            if ((rc = launch_bres_transpose(g, cs, ratio, bp, k, S, st))) break;
+            if ((rc = transpose_k(k))) break;
             rc = launch_em_update(x, bp, inv + (size_t)k * npix, npix, st);
         }
     if (!rc) rc = launch_copy2d(x, C, 1, image.data, image.column_stride, image.line_stride, L, C, st);

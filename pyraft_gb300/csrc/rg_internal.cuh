@@ -277,6 +277,22 @@ size_t ws_sum(std::initializer_list<size_t> pieces);
 // num, den: contiguous lines x columns FP64, pre-zeroed; out strided.
 int launch_bres_normalised(const DDAGeom &g, const double *d_cs, const float *s_am, double *num,
                            double *den, float *out, long long cs, long long ls, cudaStream_t st);
+// Recorded DDA walks of views first, first + stride, ... (bresenham.cu):
+// built once, replayed by the Radon and transpose of iterative methods.
+struct DDAPlan {
+    void *rays = nullptr;      // DDARayRec[nrays] (device)
+    void *steps = nullptr;     // FP32 per step (device); null: no plan
+    long long nrays = 0, total = 0;
+    int first = 0, stride = 1;
+};
+int dda_plan_build(const DDAGeom &g, const double *d_cs, int first, int stride,
+                   size_t max_bytes, DDAPlan &p, cudaStream_t st);
+void dda_plan_free(DDAPlan &p);
+// img_c contiguous lines x columns; out_am / s_am view-major (view row x R).
+int launch_dda_plan_radon(const DDAGeom &g, const DDAPlan &p, const float *img_c, float *out_am,
+                          const float *y_am, cudaStream_t st);
+int launch_dda_plan_transpose(const DDAGeom &g, const DDAPlan &p, const float *s_am, float *img_c,
+                              cudaStream_t st);
 int launch_dda_trace(int lines, int columns, const double *corners, const double *d_cst, int n,
                      int cap, int *oi, int *oj, double *os, int *ocount, cudaStream_t st);
 

@@ -140,3 +140,23 @@ def test_em_quarter_turn_pairs_match_one_view_kernels(orc, monkeypatch, S):
     ref = [rg.osem(s, (n, n), 4, S), rg.osem(s, (n, n), 4, S, reference=True)]
     for o, q in zip(out, ref):
         assert rel(o, q) <= 1e-5
+
+
+@pytest.mark.parametrize("S", [1, 3])
+def test_em_dda_recorded_walks_match_walking(orc, monkeypatch, S):
+    """The DDA EM replays each subset's walks from a plan recorded once
+    (same pixel sequences and sigmas as the walking kernels); with the plan
+    off (RG_DDA_PLAN=0), or too big for its cap (RG_DDA_PLAN_MAX_GB=0), it
+    walks every time.  All three agree to FP32 summation order."""
+    n, r, a = 48, 48, 40
+    rng = np.random.default_rng(20 + S)
+    x = orc.phantom_fromdesc((n, n), np.abs(rg.random_ellipses(6, rng)) * [1, .8, .8, .8, .8, 1])
+    y = orc.radon_bresenham(x, r, a)
+    s = rg.image(y, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
+    planned = rg.osem(s, (n, n), 6, S, method=BRES)
+    monkeypatch.setenv("RG_DDA_PLAN", "0")
+    walked = rg.osem(s, (n, n), 6, S, method=BRES)
+    monkeypatch.delenv("RG_DDA_PLAN")
+    monkeypatch.setenv("RG_DDA_PLAN_MAX_GB", "0")
+    capped = rg.osem(s, (n, n), 6, S, method=BRES)
+    assert rel(planned, walked) <= 1e-5 and rel(capped, walked) <= 1e-6
