@@ -37,6 +37,8 @@ __global__ __launch_bounds__(256) void k_to_am(const float *__restrict__ in, lon
 }
 
 // out[k * cs + j * ls] = am[j * R + k]
+// ADD: out += the transposed view-major array, instead of out =.
+template <bool ADD>
 __global__ __launch_bounds__(256) void k_from_am(const float *__restrict__ am, int R, int A,
                                                  float *__restrict__ out, long long cs,
                                                  long long ls, long long zi, long long zo)
@@ -53,7 +55,10 @@ __global__ __launch_bounds__(256) void k_from_am(const float *__restrict__ am, i
     __syncthreads();
     for (int y = w; y < 32; y += 8) {
         int k = k0 + y, j = j0 + lane;
-        if (k < R && j < A) out[(long long)k * cs + (long long)j * ls] = t[y][lane];
+        if (k < R && j < A) {
+            float *o = out + (long long)k * cs + (long long)j * ls;
+            *o = ADD ? *o + t[y][lane] : t[y][lane];
+        }
     }
 }
 
@@ -70,8 +75,17 @@ int launch_from_am(const float *am, int R, int A, float *out, long long cs, long
                    cudaStream_t st, int nz, long long zi, long long zo)
 {
     dim3 grid((A + 31) / 32, (R + 31) / 32, nz);
-    k_from_am<<<grid, 256, 0, st>>>(am, R, A, out, cs, ls, zi, zo);
+    k_from_am<false><<<grid, 256, 0, st>>>(am, R, A, out, cs, ls, zi, zo);
     RG_CK_LAUNCH("k_from_am");
+    return RG_OK;
+}
+
+int launch_add_from_am(const float *am, int R, int A, float *out, long long cs, long long ls,
+                       cudaStream_t st)
+{
+    dim3 grid((A + 31) / 32, (R + 31) / 32, 1);
+    k_from_am<true><<<grid, 256, 0, st>>>(am, R, A, out, cs, ls, 0, 0);
+    RG_CK_LAUNCH("k_from_am (add)");
     return RG_OK;
 }
 

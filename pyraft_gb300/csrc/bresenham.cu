@@ -418,8 +418,11 @@ int launch_dda_trace(int lines, int columns, const double *corners, const double
 struct DDARayRec {
     long long off;     // first step in the step array
     int count;         // steps (pixels) of the ray; 0 if it misses the image
-    int start;         // entry pixel, row-major index
+    int start;         // entry pixel index, in the ray's layout
     int dfast, dslow;  // pixel-index increment of a fast / slow move
+    int colmajor;      // layout: 1 column-major (rays whose fast axis runs
+                       // down the columns), 0 row-major; a warp's 32
+                       // consecutive steps then lie on one or two lines
 };
 
 // Walk (ray i of view first + y * stride) and count (W = false) or record
@@ -443,9 +446,12 @@ __global__ __launch_bounds__(128) void k_dda_plan(DDAGeom g, const double *__res
     const long long off = W ? rays[r].off : 0;
     int n = 0;
     if (!W) {
-        rays[r].start = it.i * g.columns + it.j;
-        rays[r].dfast = it.fast_is_i ? it.Delta_fast * g.columns : it.Delta_fast;
-        rays[r].dslow = it.fast_is_i ? it.Delta_slow : it.Delta_slow * g.columns;
+        // fast axis i (down the columns): column-major, index j * lines + i
+        const int cm = it.fast_is_i;
+        rays[r].colmajor = cm;
+        rays[r].start = cm ? it.j * g.lines + it.i : it.i * g.columns + it.j;
+        rays[r].dfast = it.Delta_fast;
+        rays[r].dslow = cm ? it.Delta_slow * g.lines : it.Delta_slow * g.columns;
     }
     int moved_slow = 0;
     for (; n < cap && !dda_end(it); ++n) {
@@ -457,25 +463,52 @@ __global__ __launch_bounds__(128) void k_dda_plan(DDAGeom g, const double *__res
 }
 
 // Replay: warp per ray.  Radon: out_am[view row][i] = sum img * sigma (the
-// EM ratio y / Ax if y_am); transpose: img_c += s * sigma (atomics).
+// EM ratio y / Ax if y_am); transpose: img += s * sigma (atomics).  Each
+// reads or adds to the image in its ray's layout: img_c / img_o row-major,
+// imgT_c / imgT_o the column-major copy.
+// Four 32-step chunks per round: their step words are loaded first, then
+// their pixels, so that a warp keeps several loads in flight (a ray has ~30
+// to ~140 chunks, and one chunk at a time leaves the replay latency-bound).
 template <int OP>
 __device__ __forceinline__ void dda_replay(const DDARayRec &rec, const float *__restrict__ steps,
                                            const float *__restrict__ img_c, float *__restrict__ img_o,
                                            float sv, float &sum)
 {
+    constexpr int kU = 4;
     const int lane = threadIdx.x & 31;
     const int dd = rec.dslow - rec.dfast;
-    int slows = 0;                     // slow moves before this chunk
-    for (int c = 0; c < rec.count; c += 32) {
-        const int s = c + lane;
-        const float w = s < rec.count ? __ldg(steps + rec.off + s) : 0.f;
-        const unsigned sb = __ballot_sync(0xffffffffu, __float_as_uint(w) & 1u);
-        const int mine = slows + __popc(sb & (0xffffffffu >> (31 - lane)));
-        slows += __popc(sb);
-        if (s < rec.count) {
-            const int pix = rec.start + s * rec.dfast + mine * dd;
-            if (OP == 0) sum = fmaf(__ldg(img_c + pix), w, sum);
-            else atomicAdd(img_o + pix, sv * w);
+    const unsigned le = 0xffffffffu >> (31 - lane);
+    int slows = 0;                     // slow moves before this round
+    for (int c = 0; c < rec.count; c += 32 * kU) {
+        float w[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int s = c + 32 * u + lane;
+            w[u] = s < rec.count ? __ldg(steps + rec.off + s) : 0.f;
+        }
+        int pix[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const unsigned sb = __ballot_sync(0xffffffffu, __float_as_uint(w[u]) & 1u);
+            const int s = c + 32 * u + lane;
+            pix[u] = rec.start + s * rec.dfast + (slows + __popc(sb & le)) * dd;
+            slows += __popc(sb);
+        }
+        if (OP == 0) {
+            float v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int s = c + 32 * u + lane;
+                v[u] = s < rec.count ? __ldg(img_c + pix[u]) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < kU; ++u) sum = fmaf(v[u], w[u], sum);
+        } else {
+#pragma unroll
+            for (int u = 0; u < kU; ++u) {
+                const int s = c + 32 * u + lane;
+                if (s < rec.count) atomicAdd(img_o + pix[u], sv * w[u]);
+            }
         }
     }
 }
@@ -484,6 +517,7 @@ __global__ __launch_bounds__(256) void k_dda_plan_radon(const DDARayRec *__restr
                                                         const float *__restrict__ steps,
                                                         long long nrays, int R, int first,
                                                         int stride, const float *__restrict__ img,
+                                                        const float *__restrict__ imgT,
                                                         float *__restrict__ out_am,
                                                         const float *__restrict__ y_am)
 {
@@ -491,7 +525,7 @@ __global__ __launch_bounds__(256) void k_dda_plan_radon(const DDARayRec *__restr
     if (r >= nrays) return;                        // warp-uniform
     const DDARayRec rec = rays[r];
     float sum = 0.f;
-    dda_replay<0>(rec, steps, img, nullptr, 0.f, sum);
+    dda_replay<0>(rec, steps, rec.colmajor ? imgT : img, nullptr, 0.f, sum);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if ((threadIdx.x & 31) == 0) {
@@ -508,7 +542,8 @@ __global__ __launch_bounds__(256) void k_dda_plan_transpose(const DDARayRec *__r
                                                             long long nrays, int R, int first,
                                                             int stride,
                                                             const float *__restrict__ s_am,
-                                                            float *__restrict__ img_c)
+                                                            float *__restrict__ img_c,
+                                                            float *__restrict__ imgT_c)
 {
     const long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (r >= nrays) return;                        // warp-uniform
@@ -516,7 +551,8 @@ __global__ __launch_bounds__(256) void k_dda_plan_transpose(const DDARayRec *__r
     const float sv = s_am[(size_t)j * R + i];
     if (sv == 0.f) return;                         // warp-uniform
     float unused = 0.f;
-    dda_replay<1>(rays[r], steps, nullptr, img_c, sv, unused);
+    const DDARayRec rec = rays[r];
+    dda_replay<1>(rec, steps, nullptr, rec.colmajor ? imgT_c : img_c, sv, unused);
 }
 
 void dda_plan_free(DDAPlan &p)
@@ -570,24 +606,24 @@ int dda_plan_build(const DDAGeom &g, const double *d_cs, int first, int stride,
     return RG_OK;
 }
 
-int launch_dda_plan_radon(const DDAGeom &g, const DDAPlan &p, const float *img_c, float *out_am,
-                          const float *y_am, cudaStream_t st)
+int launch_dda_plan_radon(const DDAGeom &g, const DDAPlan &p, const float *img_c,
+                          const float *imgT_c, float *out_am, const float *y_am, cudaStream_t st)
 {
     const long long threads = p.nrays * 32;
     k_dda_plan_radon<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
         (const DDARayRec *)p.rays, (const float *)p.steps, p.nrays, g.R, p.first, p.stride, img_c,
-        out_am, y_am);
+        imgT_c, out_am, y_am);
     RG_CK_LAUNCH("k_dda_plan_radon");
     return RG_OK;
 }
 
 int launch_dda_plan_transpose(const DDAGeom &g, const DDAPlan &p, const float *s_am, float *img_c,
-                              cudaStream_t st)
+                              float *imgT_c, cudaStream_t st)
 {
     const long long threads = p.nrays * 32;
     k_dda_plan_transpose<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(
         (const DDARayRec *)p.rays, (const float *)p.steps, p.nrays, g.R, p.first, p.stride, s_am,
-        img_c);
+        img_c, imgT_c);
     RG_CK_LAUNCH("k_dda_plan_transpose");
     return RG_OK;
 }

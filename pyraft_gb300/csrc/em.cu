@@ -76,7 +76,9 @@ size_t dda_plan_max_bytes()
 size_t em_dda_ws(int L, int C, int R, int A, int S)
 {
     const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)L * C * sizeof(float);
-    return ws_sum({sino, sino, img, img, img * S});
+    // y, ratio, x, bp, sensitivities, and the column-major copies of x and
+    // bp that the replayed walks use
+    return ws_sum({sino, sino, img, img, img * S, img, img});
 }
 
 }  // namespace
@@ -160,6 +162,8 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
     float *x = (float *)s.take(npix * sizeof(float));
     float *bp = (float *)s.take(npix * sizeof(float));
     float *inv = (float *)s.take(npix * sizeof(float) * S);
+    float *xT = (float *)s.take(npix * sizeof(float));
+    float *bpT = (float *)s.take(npix * sizeof(float));
     rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, y, st);
     if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, C, 1, L, C, st);
     if (!rc) rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
@@ -169,13 +173,17 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
     if (!rc && niter >= 2 && dda_plans_enabled())
         for (int k = 0; k < S && !rc; ++k)
             rc = dda_plan_build(g, cs, k, S, dda_plan_max_bytes(), plans.p[k], st);
+    // bp must be zero on entry to transpose_k
     auto radon_k = [&](int k) {
-        if (plans.p[k].steps) return launch_dda_plan_radon(g, plans.p[k], x, ratio, y, st);
-        return launch_bres_radon(g, cs, x, C, 1, ratio, 1, R, y, k, S, st);
+        if (!plans.p[k].steps) return launch_bres_radon(g, cs, x, C, 1, ratio, 1, R, y, k, S, st);
+        int rc2 = launch_to_am(x, C, 1, L, C, xT, st);          // xT[c * L + r] = x[r][c]
+        return rc2 ? rc2 : launch_dda_plan_radon(g, plans.p[k], x, xT, ratio, y, st);
     };
     auto transpose_k = [&](int k) {
-        if (plans.p[k].steps) return launch_dda_plan_transpose(g, plans.p[k], ratio, bp, st);
-        return launch_bres_transpose(g, cs, ratio, bp, k, S, st);
+        if (!plans.p[k].steps) return launch_bres_transpose(g, cs, ratio, bp, k, S, st);
+        int rc2 = launch_fill(bpT, npix, 0.f, st);
+        if (!rc2) rc2 = launch_dda_plan_transpose(g, plans.p[k], ratio, bp, bpT, st);
+        return rc2 ? rc2 : launch_add_from_am(bpT, L, C, bp, C, 1, st);
     };
     for (int k = 0; k < S && !rc; ++k) {
         if ((rc = launch_fill(bp, npix, 0.f, st))) break;

@@ -222,6 +222,9 @@ int launch_to_am(const float *in, long long cs, long long ls, int R, int A, floa
                  cudaStream_t st, int nz = 1, long long zi = 0, long long zo = 0);
 int launch_from_am(const float *am, int R, int A, float *out, long long cs, long long ls,
                    cudaStream_t st, int nz = 1, long long zi = 0, long long zo = 0);
+// out(k, j) += am[j * R + k] (k < R, j < A)
+int launch_add_from_am(const float *am, int R, int A, float *out, long long cs, long long ls,
+                       cudaStream_t st);
 int launch_copy2d(const float *in, long long ics, long long ils, float *out, long long ocs,
                   long long ols, int rows, int cols, cudaStream_t st);
 int launch_fill(float *p, size_t n, float v, cudaStream_t st);
@@ -288,11 +291,13 @@ struct DDAPlan {
 int dda_plan_build(const DDAGeom &g, const double *d_cs, int first, int stride,
                    size_t max_bytes, DDAPlan &p, cudaStream_t st);
 void dda_plan_free(DDAPlan &p);
-// img_c contiguous lines x columns; out_am / s_am view-major (view row x R).
-int launch_dda_plan_radon(const DDAGeom &g, const DDAPlan &p, const float *img_c, float *out_am,
-                          const float *y_am, cudaStream_t st);
+// img_c contiguous lines x columns and imgT_c its column-major copy (the
+// Radon reads both; the transpose adds to both, to be summed by the
+// caller); out_am / s_am view-major (view row x R).
+int launch_dda_plan_radon(const DDAGeom &g, const DDAPlan &p, const float *img_c,
+                          const float *imgT_c, float *out_am, const float *y_am, cudaStream_t st);
 int launch_dda_plan_transpose(const DDAGeom &g, const DDAPlan &p, const float *s_am, float *img_c,
-                              cudaStream_t st);
+                              float *imgT_c, cudaStream_t st);
 int launch_dda_trace(int lines, int columns, const double *corners, const double *d_cst, int n,
                      int cap, int *oi, int *oj, double *os, int *ocount, cudaStream_t st);
 
