@@ -235,7 +235,12 @@ int rg_fbp(rg_image sino, rg_image image, int kind,
  * nsubsets == 1 is plain EM; > 1 is OSEM over interleaved view subsets
  * (subset s = views s, s+S, s+2S, ...).  Guards: y/0 -> 0, and pixels with
  * zero sensitivity are set to 0 (the reference divides by zero).
- * The sensitivity A^T 1 is accumulated in FP64.                             */
+ * The sensitivity A^T 1 is accumulated in FP64.
+ * RG_BRESENHAM with niter >= 2 also allocates, outside the workspace, device
+ * memory for the rays' walks recorded once and replayed each sub-iteration
+ * (4 bytes per traversal step: 3.2 GB at 1024^2 x 720), within a third of
+ * the free device memory and RG_DDA_PLAN_MAX_GB (48 by default), freed
+ * before return; RG_DDA_PLAN=0 walks every time instead.                   */
 size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets);
 int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets,
           void *workspace, size_t workspace_bytes, void *stream);
