@@ -129,7 +129,8 @@ constexpr int kBtPad = 32;                               // checked per plan (tt
 constexpr int kTtRowB = kTtWin + 2 * kBtPad + 1;
 
 __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restrict__ d, int n,
-                                                     int total, int *counter, int *err)
+                                                     int total, int *counter, int *err,
+                                                     unsigned pb)
 {
     extern __shared__ __align__(128) float2 tile[];   // [kBtLines][kTtRowB]
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(tile);
@@ -161,7 +162,7 @@ __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restric
         }
         __syncthreads();
         tt_views<kTtRowB, kBtLines, kBtPad>(sbase, p0, i0, b.views, b.ovid + (o ? b.n_rows : 0), nvo, b.R,
-                          b.ratio_am, b.R, err);
+                          b.ratio_am, b.R, err, pb);
     }
 }
 
@@ -285,7 +286,8 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
             RG_CK_LAUNCH("k_batch_rows (zero)");
             RG_CK(cudaMemsetAsync(br.counter, 0, sizeof(int), st));
             k_batch_tiles<<<br.grid[4][0], 256, (size_t)kBtLines * kTtRowB * 8, st>>>(
-                d, br.n, br.total[kTiles][0], br.counter, device_error_word());
+                d, br.n, br.total[kTiles][0], br.counter, device_error_word(),
+                (unsigned)sizeof(float2));
             RG_CK_LAUNCH("k_batch_tiles");
             k_batch_rows<false><<<br.total[kRows][s], 256, 0, st>>>(d, br.n);
             RG_CK_LAUNCH("k_batch_rows (ratio)");

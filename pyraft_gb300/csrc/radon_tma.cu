@@ -105,15 +105,19 @@ __device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *tm,
 }
 
 // One full strip of a (ray, view): 16 lines, line r of the strip buffer at
-// byte offset r * BW * 8 (an immediate of the load).
+// byte offset r * BW * 8 (an immediate of the load).  pb (== 8, the bytes
+// of a pair) arrives as a kernel argument, so the sample's address is one
+// integer multiply-add on the FMA pipe instead of a shift and an add on the
+// integer pipe, which the position and weight bits keep busy.
 template <int BW, int R0>
-__device__ __forceinline__ void strip16(unsigned sb, unsigned &L, unsigned dq, float &part)
+__device__ __forceinline__ void strip16(unsigned sb, unsigned &L, unsigned dq, unsigned pb,
+                                        float &part)
 {
     if constexpr (R0 < kTmLines) {
-        const float2 pr = lds_pair_at<R0 * BW * 8>(sb + ((L >> 23) << 3));
+        const float2 pr = lds_pair_at<R0 * BW * 8>((L >> 23) * pb + sb);
         part += fmaf(frac_plus_one(L), pr.y, pr.x);
         L += dq;
-        strip16<BW, R0 + 1>(sb, L, dq, part);
+        strip16<BW, R0 + 1>(sb, L, dq, pb, part);
     }
 }
 
@@ -131,7 +135,8 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
                                                    const StBlock *__restrict__ blocks, int R,
                                                    float *__restrict__ out_am, int out_ld,
                                                    const float *__restrict__ y_am, int y_ld,
-                                                   long long zo, int *__restrict__ err)
+                                                   long long zo, int *__restrict__ err,
+                                                   unsigned pb)
 {
     extern __shared__ __align__(128) float2 sbuf[];   // [2][kTmLines][BW]
     __shared__ __align__(8) unsigned long long full[2];
@@ -265,11 +270,11 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
                     const unsigned dq = (unsigned)((q[v] + 256) >> 9);
                     float part = 0.f;
                     if (a == i0 && e == i0 + kTmLines - 1) {
-                        strip16<BW, 0>(sb, L, dq, part);
+                        strip16<BW, 0>(sb, L, dq, pb, part);
                     } else {
                         unsigned lb = sb + (unsigned)(a - i0) * (BW * 8);
                         for (int i = a; i <= e; ++i) {
-                            const float2 pr = lds_pair_at<0>(lb + ((L >> 23) << 3));
+                            const float2 pr = lds_pair_at<0>((L >> 23) * pb + lb);
                             part += fmaf(frac_plus_one(L), pr.y, pr.x);
                             L += dq;
                             lb += BW * 8;
@@ -454,7 +459,7 @@ static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensor
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((p.g.R + kTmRays - 1) / kTmRays, p.nblocks, nz);
     k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
-                               out_am, out_ld, y_am, y_ld, zo, d_err);
+                               out_am, out_ld, y_am, y_ld, zo, d_err, (unsigned)sizeof(float2));
     RG_CK_LAUNCH("k_radon_tma");
     return RG_OK;
 }
@@ -528,7 +533,8 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
                                                      const int *__restrict__ ovid, int n_rows,
                                                      int n_cols, int R,
                                                      float *__restrict__ out_am, int out_ld,
-                                                     long long zo, int *__restrict__ err)
+                                                     long long zo, int *__restrict__ err,
+                                                     unsigned pb)
 {
     extern __shared__ __align__(128) float2 tile[];   // [kTtLines][kTtRow]
     __shared__ __align__(8) unsigned long long full;
@@ -566,7 +572,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
         return;
     }
 
-    tt_views<kTtRow>(sbase, p0, i0, views, vid, nvo, R, out_am, out_ld, err);
+    tt_views<kTtRow>(sbase, p0, i0, views, vid, nvo, R, out_am, out_ld, err, pb);
 }
 
 // out[view][k] = 0 (zeroing pass) or the epilogue of the summed rays, for
@@ -645,7 +651,7 @@ int launch_radon_tiles(const SSPlan &p, const float2 *prow, const float2 *pcol, 
                     2 * nz);
     k_radon_tiles<<<grid, 256, smem, st>>>(tr, tc, N, p.d_views, (const int *)p.d_ovid,
                                            p.n_ovid[0], p.n_ovid[1], R, out_am, out_ld, zo,
-                                           device_error_word());
+                                           device_error_word(), (unsigned)sizeof(float2));
     RG_CK_LAUNCH("k_radon_tiles");
     if (epi == kEpiRatio)
         k_views_rows<kEpiRatio, false><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am, out_ld,

@@ -382,13 +382,16 @@ constexpr int kTtRow = kTtWin + 2 * kTtPad;   // smem row stride (entries): 2 KB
 // ROW: smem row stride of the staged tile in entries (>= WIN + 2 PAD);
 // LINES: lines of the tile.
 template <int ROW, int LINES, int R0>
-__device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, float &part)
+__device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, unsigned pb,
+                                        float &part)
 {
+    // pb (== 8) is a runtime value: the address is one multiply-add on the
+    // FMA pipe (the integer pipe carries the position and weight bits)
     if constexpr (R0 < LINES) {
-        const float2 pr = lds_pair_at<R0 * ROW * 8>(sb + ((L >> 23) << 3));
+        const float2 pr = lds_pair_at<R0 * ROW * 8>((L >> 23) * pb + sb);
         part += fmaf(frac_plus_one(L), pr.y, pr.x);
         L += dq;
-        tt_walk<ROW, LINES, R0 + 1>(sb, L, dq, part);
+        tt_walk<ROW, LINES, R0 + 1>(sb, L, dq, pb, part);
     }
 }
 
@@ -410,7 +413,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                                          const View *__restrict__ views,
                                          const int *__restrict__ vid, int nvo, int R,
                                          float *__restrict__ out_am, int out_ld,
-                                         int *__restrict__ err)
+                                         int *__restrict__ err, unsigned pb)
 {
     __shared__ int s_klo[kTtBatch], s_off[kTtBatch + 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -464,7 +467,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             unsigned L = (unsigned)(u >> 9);
             const unsigned dq = (unsigned)((v.ri + 256) >> 9);
             float part = 0.f;
-            tt_walk<ROW, LINES, 0>(sbase, L, dq, part);
+            tt_walk<ROW, LINES, 0>(sbase, L, dq, pb, part);
             if (part != 0.f) atomicAdd(out_am + (size_t)v.view * out_ld + k, part * v.delta);
         }
         __syncthreads();                                // s_klo / s_off reused
