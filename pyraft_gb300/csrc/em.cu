@@ -169,8 +169,15 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
     if (!rc) rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
     // Record each subset's walks once when they will be replayed (two walks
     // per sub-iteration), memory permitting (dda_plan_build).
+    // (not while the stream is captured into a graph: building a plan
+    // allocates and synchronises)
     DDAPlans plans(S);
-    if (!rc && niter >= 2 && dda_plans_enabled())
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!rc) {
+        const cudaError_t ce = cudaStreamIsCapturing(st, &cap);
+        if (ce != cudaSuccess) rc = cuda_error(ce, "rg_em");
+    }
+    if (!rc && niter >= 2 && dda_plans_enabled() && cap == cudaStreamCaptureStatusNone)
         for (int k = 0; k < S && !rc; ++k)
             rc = dda_plan_build(g, cs, k, S, dda_plan_max_bytes(), plans.p[k], st);
     // bp must be zero on entry to transpose_k
