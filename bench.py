@@ -48,16 +48,17 @@ LAUNCHES_PER_FBP = 4
 
 def smem_ceiling(updates, ms, sms, sm_mhz):
     """The gathers' shared-memory roofline: each update reads one 8-byte
-    pair from shared memory, and a warp's 64-bit load takes two 128-byte
-    wavefronts, at one wavefront per SM per clock: 16 updates per SM per
-    clock."""
+    sample pair from shared memory, and the SM serves one 128-byte
+    wavefront per clock: 16 updates per SM per clock.  (The paired kernel
+    reads a view's pair and its partner's with one 128-bit load, four
+    wavefronts for 64 updates.)"""
     mhz = sm_mhz or 2070.0
     peak = 16.0 * sms * mhz * 1e6 / 1e9
     got = updates / (ms * 1e-3) / 1e9
     return {"unit": "GUPS", "achieved": round(got, 1), "peak": round(peak, 1),
             "frac": round(got / peak, 3), "sms": sms, "sm_mhz": mhz,
-            "model": "8 B of shared memory per update; 2 wavefronts per warp-wide 64-bit "
-                     "load; 1 wavefront per SM per clock"}
+            "model": "8 B of shared memory per update; 128-byte wavefronts, 1 per SM "
+                     "per clock"}
 
 
 def env_rank():

@@ -18,11 +18,14 @@
 // c, row r), (c, r + 4), ... of its tile for view theta reads the partner
 // view's staged window at the same entries and accumulates the pixels (col
 // N-1-r, row c), (N-5-r, c), ... of the quarter-turned tile for view
-// theta + pi/2.  The partner's window covers the same
-// sample indices, so its load is the same shared address plus a constant
-// offset.  Per update this leaves a shared load and two FP32 adds of the
-// seven instructions of the one-view inner loop (gather_tile<0>), and the
-// per-view set-up is shared too.
+// theta + pi/2.  The partner's window covers the same sample indices, so
+// the staging area interleaves the two: entry e holds the view's sample
+// pair and the partner's, 16 bytes, and one 128-bit shared load serves both
+// updates.  Per update this leaves a shared load, the position arithmetic
+// and two FP32 adds of the seven instructions of the one-view inner loop
+// (gather_tile<0>), and the per-view set-up is shared too.  The 128-bit load
+// takes as many shared-memory wavefronts per update as the 64-bit one (8
+// lanes of 16 bytes, against 16 of 8), but half the load instructions.
 //
 // Each pixel then gets two partial sums: views [theta0, theta0 + pi/2) from
 // the CTA whose tile holds it, views [theta0 + pi/2, theta0 + pi) from the
@@ -64,10 +67,9 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
                                                 float *__restrict__ out, long long cs,
                                                 long long ls, int *__restrict__ err, int tx,
                                                 int ty, float2 *__restrict__ pairs,
-                                                unsigned pair_bytes, int split, int rank)
+                                                unsigned quad_bytes, int split, int rank)
 {
     constexpr int TH = kWarps * ROWS;                     // tile height
-    constexpr unsigned kPartner = kPairSlots * WMAX * 8;  // byte offset of the partner windows
     __shared__ SlotInfo slot[kPairSlots];
     __shared__ int slotW[kPairSlots];
     __shared__ int slotView[kPairSlots];
@@ -76,10 +78,9 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
 
     // Warp w covers columns 8 (w & 3) .. + 8 and rows 4 ROWS (w >> 2) .. +
     // 4 ROWS of the tile; lane l takes column l & 7 and rows l >> 3, + 4,
-    // + 8, ...  So the 32 lanes of one load read 8 columns x 4 adjacent rows,
-    // whose positions lie within about 9 entries of the window: about one
-    // shared-memory wavefront per load, where 32 columns of one row span up
-    // to 32 entries (two wavefronts).
+    // + 8, ...  So the 32 lanes of one load read 8 columns x 4 adjacent
+    // rows.  A quarter-warp (the 8 columns of one row) spans about 8 entries
+    // of the window: one shared-memory wavefront for its 128-bit loads.
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int row0 = ty * TH, col0 = tx * kTile;
     const int cofs = 8 * (warp & 3) + (lane & 7);
@@ -134,26 +135,30 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
         }
         __syncthreads();
 
-        // Stage the windows: q < kPairSlots the view of slot q, else the
-        // partner view of slot q - kPairSlots, over the same entries.
-        for (int q = warp; q < 2 * kPairSlots; q += kWarps) {
-            const int s = q < kPairSlots ? q : q - kPairSlots;
-            if (s >= nslot) continue;
+        // Stage the windows: entry e of slot s holds the view's pair and its
+        // partner's, side by side (one 16-byte load serves both).
+        float4 *quads = reinterpret_cast<float4 *>(pairs);
+        for (int s = warp; s < nslot; s += kWarps) {
             const int nlo = slot[s].nlo, W = slotW[s];
-            const float *__restrict__ row =
-                s_am + (size_t)(slotView[s] + (q < kPairSlots ? 0 : roff)) * s_ld;
-            const float d = slotDelta[q];
+            const float *__restrict__ rv = s_am + (size_t)slotView[s] * s_ld;
+            const float *__restrict__ rp = s_am + (size_t)(slotView[s] + roff) * s_ld;
+            const float dv = slotDelta[s], dp = slotDelta[kPairSlots + s];
             for (int e = lane; e < W; e += 32) {
                 const int n = nlo + e;
-                float2 pr = make_float2(0.f, 0.f);
+                float4 qd = make_float4(0.f, 0.f, 0.f, 0.f);
                 if (MODE == 0) {
-                    if (n >= 0 && n <= R - 2) pr = make_pair(__ldg(row + n), __ldg(row + n + 1), true);
+                    if (n >= 0 && n <= R - 2) {
+                        const float2 a = make_pair(__ldg(rv + n), __ldg(rv + n + 1), true);
+                        const float2 b = make_pair(__ldg(rp + n), __ldg(rp + n + 1), true);
+                        qd = make_float4(a.x, a.y, b.x, b.y);
+                    }
                 } else {
-                    const float s0 = (n >= 0 && n < R) ? __ldg(row + n) : 0.f;
-                    const float s1 = (n + 1 >= 0 && n + 1 < R) ? __ldg(row + n + 1) : 0.f;
-                    pr = make_float2(s0 * d, s1 * d);
+                    const bool in0 = n >= 0 && n < R, in1 = n + 1 >= 0 && n + 1 < R;
+                    const float v0 = in0 ? __ldg(rv + n) : 0.f, v1 = in1 ? __ldg(rv + n + 1) : 0.f;
+                    const float p0 = in0 ? __ldg(rp + n) : 0.f, p1 = in1 ? __ldg(rp + n + 1) : 0.f;
+                    qd = make_float4(v0 * dv, v1 * dv, p0 * dp, p1 * dp);
                 }
-                pairs[q * WMAX + e] = pr;
+                quads[s * WMAX + e] = qd;
             }
         }
         __syncthreads();
@@ -164,7 +169,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
         for (int s = 0; s < nslot; ++s) {
             const SlotInfo si = slot[s];
             if (si.nlo == INT_MIN) continue;
-            const unsigned pw = sbase + (unsigned)(s * WMAX) * pair_bytes;
+            const unsigned pw = sbase + (unsigned)(s * WMAX) * quad_bytes;
             unsigned vpos = si.base + (unsigned)(cofs * si.a) + (unsigned)(rofs * si.b);
             const unsigned step = 4u * (unsigned)si.b;
             // adjoint hat weights (gather_tile): sat(-P w1 + 1 + P), sat(P w1 + 1 - 2P);
@@ -173,12 +178,10 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             const float c0 = 1.f + P, c1 = 1.f - 2.f * P;
 #pragma unroll
             for (int r = 0; r < ROWS; ++r) {
-                const unsigned addr = (vpos >> 23) * pair_bytes + pw;
+                const unsigned addr = (vpos >> 23) * quad_bytes + pw;
                 float2 pb, pa;
-                asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];"
-                             : "=f"(pb.x), "=f"(pb.y) : "r"(addr));
-                asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];"
-                             : "=f"(pa.x), "=f"(pa.y) : "r"(addr), "n"(kPartner));
+                asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                             : "=f"(pb.x), "=f"(pb.y), "=f"(pa.x), "=f"(pa.y) : "r"(addr));
                 const float w1 = frac_plus_one(vpos);
                 if (MODE == 0) {
                     partB[r] += fmaf(w1, pb.y, pb.x);
@@ -244,12 +247,12 @@ __global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_
                                                     float *__restrict__ out,
                                                     long long cs, long long ls,
                                                     int *__restrict__ err, long long zs,
-                                                    long long zo, unsigned pair_bytes, int split)
+                                                    long long zo, unsigned quad_bytes, int split)
 {
-    extern __shared__ float2 pairs[];          // [kSlots][WMAX]: views, then partners
+    extern __shared__ __align__(16) float2 pairs[];  // [kPairSlots][WMAX] x {view, partner}
     gather_tile_rot<MODE, WMAX, ROWS>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
                                 out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
-                                blockIdx.y, pairs, pair_bytes, split, blockIdx.x % split);
+                                blockIdx.y, pairs, quad_bytes, split, blockIdx.x % split);
 }
 
 template <int MODE, int WMAX, int ROWS>
@@ -259,13 +262,13 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     // half: view pairs; roff: sinogram rows between a view and its partner
     const int N = p.g.N, half = p.nv / 2, roff = p.g.A / 2;
     // the staging area, which also holds the cluster reduction's partials
-    const size_t smem = std::max((size_t)kSlots * WMAX * sizeof(float2),
+    const size_t smem = std::max((size_t)kPairSlots * WMAX * sizeof(float4),
                                  (size_t)2 * ROWS * 256 * sizeof(float));
     dim3 grid((N + kTile - 1) / kTile, (N + kWarps * ROWS - 1) / (kWarps * ROWS), z.n);
     auto k = k_gather_rot<MODE, WMAX, ROWS>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
-    const unsigned pb = (unsigned)sizeof(float2);
+    const unsigned pb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
     if (split == 1) {
         k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, half, roff, N, scale, out, cs, ls,
