@@ -39,11 +39,14 @@ METRIC = "FBP GUPS (2048^2 image, 1800 views, 2048 rays; Ram-Lak + slant-stack B
 UNIT = "GUPS"
 UPDATES = N * N * A
 # ncu (dram__bytes_read.sum + dram__bytes_write.sum) of one backprojection
-# launch at this size (profiles/bp_rot_2048x1800_ncu.md): the sinogram and
-# the zeroed image that the two partial sums per pixel are added to.
-BP_TRAFFIC_BYTES = 31642880
-# kernels of one FBP step: k_to_am, k_filter_fft, k_zero_image, k_gather_rot
-LAUNCHES_PER_FBP = 4
+# call at this size (profiles/bp_rot_2048x1800_ncu.md): k_pair_quads reads
+# the sinogram (14.9 MB); k_gather_rot_tma reads the quads (29.5 MB, which
+# ncu's cache flush between kernels sends to DRAM) and the zeroed image that
+# the two partial sums per pixel are added to (16.8 MB).
+BP_TRAFFIC_BYTES = 14850560 + 46416640
+# kernels of one FBP step: k_to_am, k_filter_fft, k_zero_image, k_pair_quads,
+# k_gather_rot_tma
+LAUNCHES_PER_FBP = 5
 
 
 def smem_ceiling(updates, ms, sms, sm_mhz):
@@ -472,13 +475,15 @@ def main():
     fws = L.rg_filter_workspace(FS, _native.RG_FILTER_RAMLAK)
     fwsb = torch.empty(fws, dtype=torch.uint8, device="cuda")
     _native.check(L.rg_filter(FS, FA, _native.RG_FILTER_RAMLAK, fwsb.data_ptr(), fws, sp))
-    assert L.rg_backprojection_slantstack_workspace(FA, I) == 0
+    # a view-major sinogram needs no layout copy, only the paired gathers' quads
+    bws = L.rg_backprojection_slantstack_workspace(FA, I)
+    bwsb = torch.empty(bws, dtype=torch.uint8, device="cuda")
     bp_ms = []
     for k in range(warm + args.steps):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        _native.check(L.rg_backprojection_slantstack(FA, I, None, 0, sp))
+        _native.check(L.rg_backprojection_slantstack(FA, I, bwsb.data_ptr(), bws, sp))
         b.record(stream)
         b.synchronize()
         if k >= warm:
@@ -511,7 +516,10 @@ def main():
     rwsb = torch.empty(rws, dtype=torch.uint8, device="cuda")
     radon_ms = timed(lambda: _native.check(L.rg_radon_slantstack(RI, SO, rwsb.data_ptr(), rws,
                                                                  sp)))
-    adj_ms = timed(lambda: _native.check(L.rg_radon_transpose_slantstack(FA, I, None, 0, sp)))
+    aws = L.rg_radon_transpose_slantstack_workspace(FA, I)
+    awsb = torch.empty(aws, dtype=torch.uint8, device="cuda")
+    adj_ms = timed(lambda: _native.check(L.rg_radon_transpose_slantstack(FA, I, awsb.data_ptr(),
+                                                                         aws, sp)))
 
     # ---- end to end: pinned host sinogram in, image out, through rg_fbp
     h_in = torch.empty((R, A), dtype=torch.float32).pin_memory()
@@ -631,8 +639,9 @@ def main():
                                    "per-step CUDA events"},
                 "finite_and_equal": ok},
         "roofline": {"bound": "hbm",
-                     "kernel": "k_gather_rot<0> (backprojection, views paired a quarter turn "
-                               "apart; timed as the call, with its k_zero_image)",
+                     "kernel": "k_gather_rot_tma<0> (backprojection, views paired a quarter "
+                               "turn apart, windows staged by TMA; timed as the call, with its "
+                               "k_zero_image and k_pair_quads)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "traffic": BP_TRAFFIC_BYTES,
                      "algorithmic_bytes": alg_bytes, "kernel_ms": round(bp_ms, 4),

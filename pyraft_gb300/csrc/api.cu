@@ -92,6 +92,13 @@ static size_t ws_total(std::initializer_list<size_t> pieces)
     return t ? Scratch::align(t) : 0;
 }
 
+// Quad scratch of the paired gathers for nz sinograms of this shape (an
+// even view count; whether the geometry pairs is known only to its plan).
+static size_t quads_ws(const rg_image &sino, int nz = 1)
+{
+    return sino.columns % 2 == 0 ? gather_quads_bytes(sino.columns, sino.lines, nz) : 0;
+}
+
 // ----------------------------------------------------------------------------
 // Caches (per device, keyed by the raw bytes of the geometry).
 
@@ -329,7 +336,7 @@ int tuned_rows(const SSPlan &p, int mode)
 }
 
 static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
-                           long long cs, long long ls, cudaStream_t st)
+                           long long cs, long long ls, cudaStream_t st, void *quads = nullptr)
 {
     if (env_rows()) return RG_OK;
     const std::string key = tune_key(p, mode);
@@ -349,7 +356,8 @@ static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_l
         float tsum = 0.f;
         for (int rep = 0; rep < 3 && !rc; ++rep) {
             cudaEventRecord(a, st);
-            rc = launch_gather(p, mode, s_am, s_ld, out, cs, ls, nullptr, nullptr, nullptr, st, rows);
+            rc = launch_gather(p, mode, s_am, s_ld, out, cs, ls, nullptr, nullptr, nullptr, st, rows,
+                               Stack(), quads);
             cudaEventRecord(b, st);
             cudaError_t e = cudaEventSynchronize(b);
             if (!rc && e != cudaSuccess) rc = cuda_error(e, "autotune");
@@ -485,8 +493,8 @@ int rg_radon_slantstack_stack(rg_image phantom, long long phantom_stride, rg_ima
 size_t rg_radon_transpose_slantstack_stack_workspace(rg_image sino, rg_image image, int nstack)
 {
     (void)image;
-    return is_view_major(sino) ? 0
-                               : ws_total({(size_t)sino.lines * sino.columns * sizeof(float) * nstack});
+    return ws_total({is_view_major(sino) ? 0 : (size_t)sino.lines * sino.columns * sizeof(float) * nstack,
+                     quads_ws(sino, nstack)});
 }
 
 int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg_image image,
@@ -513,6 +521,8 @@ int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg
         s_am = t;
         zs = (long long)R * A;
     }
+    const size_t qb = quads_ws(sino, nstack);
+    void *quads = qb ? s.take(qb) : nullptr;
     Stack zz;
     zz.n = nstack;
     zz.in = zs;
@@ -520,10 +530,10 @@ int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg
     // tile height tuned on the first slice (its output is rewritten below)
     if (!rc)
         rc = autotune_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
-                             st);
+                             st, quads);
     if (!rc)
         rc = launch_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
-                           nullptr, nullptr, nullptr, st, 0, zz);
+                           nullptr, nullptr, nullptr, st, 0, zz, quads);
     scratch_end(s);
     return rc;
 }
@@ -569,7 +579,8 @@ int rg_radon_transpose_slantstack_f64(rg_image_f64 sino, rg_image_f64 image, voi
 // ---------------------------------------------------------------- gathers
 static size_t gather_ws(const rg_image &sino)
 {
-    return is_view_major(sino) ? 0 : ws_total({(size_t)sino.lines * sino.columns * sizeof(float)});
+    return ws_total({is_view_major(sino) ? 0 : (size_t)sino.lines * sino.columns * sizeof(float),
+                     quads_ws(sino)});
 }
 
 static int run_gather(int mode, rg_image sino, rg_image img, void *ws, size_t wsb, void *stream)
@@ -589,11 +600,14 @@ static int run_gather(int mode, rg_image sino, rg_image img, void *ws, size_t ws
         rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, t, st);
         s_am = t;
     }
+    const size_t qb = quads_ws(sino);
+    void *quads = qb ? s.take(qb) : nullptr;
     if (!rc)
-        rc = autotune_gather(ph->p, mode, s_am, R, img.data, img.column_stride, img.line_stride, st);
+        rc = autotune_gather(ph->p, mode, s_am, R, img.data, img.column_stride, img.line_stride, st,
+                             quads);
     if (!rc)
         rc = launch_gather(ph->p, mode, s_am, R, img.data, img.column_stride, img.line_stride,
-                           nullptr, nullptr, nullptr, st);
+                           nullptr, nullptr, nullptr, st, 0, Stack(), quads);
     scratch_end(s);
     return rc;
 }
@@ -812,7 +826,9 @@ int rg_filter(rg_image in, rg_image out, int kind, void *ws, size_t wsb, void *s
 size_t rg_fbp_workspace(rg_image sino, rg_image image, int kind)
 {
     (void)image;
-    return rg_filter_workspace(sino, kind);
+    (void)kind;
+    const size_t b = (size_t)sino.lines * sino.columns * sizeof(float);
+    return ws_total({b, b, quads_ws(sino)});
 }
 
 int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *stream)
@@ -830,15 +846,18 @@ int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *
     if ((rc = scratch_begin(s, ws, wsb, rg_fbp_workspace(sino, image, kind), st))) return rc;
     float *a = (float *)s.take((size_t)R * A * sizeof(float));
     float *b = (float *)s.take((size_t)R * A * sizeof(float));
+    const size_t qb = quads_ws(sino);
+    void *quads = qb ? s.take(qb) : nullptr;
     const float *src = sino.data;
     if (!is_view_major(sino)) {
         rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, a, st);
         src = a;
     }
     if (!rc && !(rc = filter_rows(kind, src, b, R, A, taps, st)) &&
-        !(rc = autotune_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride, st)))
+        !(rc = autotune_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
+                               st, quads)))
         rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
-                           nullptr, nullptr, nullptr, st);
+                           nullptr, nullptr, nullptr, st, 0, Stack(), quads);
     scratch_end(s);
     return rc;
 }

@@ -43,10 +43,17 @@ struct Holders {
     }
 };
 
+// Quad scratch of the paired gathers for the largest of S subsets of A views.
+static size_t em_quads_bytes(int R, int A, int S)
+{
+    return gather_quads_bytes((A + S - 1) / S, R, 1);
+}
+
 size_t em_ss_ws(int N, int R, int A, int S)
 {
     const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)N * N * sizeof(float);
-    return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S, img});
+    return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S, img,
+                   em_quads_bytes(R, A, S)});
 }
 
 // The DDA EM's recorded walks (freed with the call).  RG_DDA_PLAN=0 walks
@@ -111,6 +118,8 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
     // gather output of the paired kernels, whose two partial sums per pixel
     // rule out the fused update: x <- x * g * inv follows as its own pass
     float *gsum = (float *)s.take((size_t)N * N * sizeof(float));
+    const size_t qb = em_quads_bytes(R, A, S);
+    void *quads = qb ? s.take(qb) : nullptr;
     int rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
     for (int k = 0; k < S && !rc; ++k) {
         float *ik = inv + (size_t)k * N * N;
@@ -127,7 +136,7 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
             if ((rc = launch_radon(*plans[k], prow, pcol, ratio, R, y_am, R, st))) break;
             if (plans[k]->rot_ok && gather_rot_enabled()) {
                 rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, gsum, N, 1, nullptr, nullptr,
-                                   nullptr, st);
+                                   nullptr, st, 0, Stack(), quads);
                 if (!rc) rc = launch_em_update(x, gsum, inv + (size_t)k * N * N, (size_t)N * N, st);
             } else {
                 rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, nullptr, 0, 0, x,

@@ -33,18 +33,36 @@
 // both partials are added atomically: two adds onto zero give the same
 // float in either order, so the result does not depend on timing.
 //
+// Staging.  When the caller supplies scratch for it, a prepass
+// (k_pair_quads) writes every quad of the plan to global memory once, [view
+// pair][sample entry], and the gather (k_gather_rot_tma) loads each view
+// pair's window as one TMA box into shared memory, double-buffered on two
+// mbarriers, so the next chunk of 16 pairs streams in while the current one
+// is summed and no thread spends issue slots on staging.  Without that
+// scratch (or for windows wider than a TMA box) k_gather_rot stages the
+// quads itself with loads from the sinogram.
+//
 // Precision: FP32 partial sums over a chunk of 16 view pairs, added across
 // chunks in FP32 (no compensation: the two-level sum keeps the error near
 // 1e-7 of the pixel values).
+#include <string.h>
+
 #include <algorithm>
 
 #include "ss_tiles.cuh"
+#include "tma.cuh"
 
 namespace rg {
 
 namespace {
 
 constexpr int kPairSlots = kSlots / 2;    // view pairs per staged chunk
+constexpr int kQuadBox = 256;             // widest TMA box (entries)
+constexpr int kStages = 2;                // TMA window buffers (double buffering)
+// Fewest view pairs for the TMA-staged form: with fewer, its prepass launch
+// and pipeline fill cost more than staging by loads (measured on OSEM
+// subsets of 36 pairs and 64-slice stacks of 180 pairs).
+constexpr int kTmaMinPairs = 256;
 
 __global__ void k_zero_image(float *__restrict__ out, int N, long long cs, long long ls,
                              long long zo)
@@ -58,8 +76,125 @@ __global__ void k_zero_image(float *__restrict__ out, int N, long long cs, long 
     }
 }
 
+// Window of view v over the tile whose first pixel is (row0, col0), TH rows
+// x kTile columns: si gets the Q9.23 origin and steps and the first sample
+// index nlo; the return value is the window's width in entries.
+template <int MODE, int TH>
+__device__ __forceinline__ int rot_window(const View &v, int row0, int col0, SlotInfo &si)
+{
+    long long cr, cc, c0;
+    if (MODE == 0) { cr = v.brow; cc = v.bcol; c0 = v.b0; }
+    else           { cr = v.krow; cc = v.kcol; c0 = v.k0; }
+    const long long origin = c0 + (long long)row0 * cr + (long long)col0 * cc;
+    const long long dr = (long long)(TH - 1) * cr, dc = (long long)(kTile - 1) * cc;
+    const long long mn = origin + min(0LL, dr) + min(0LL, dc);
+    const long long mx = origin + max(0LL, dr) + max(0LL, dc);
+    const int nlo = (int)(mn >> 32) - 1;
+    const int nhi = (int)(mx >> 32) + 1;
+    si.nlo = nlo;
+    si.base = (unsigned)((origin - ((long long)nlo << 32)) >> 9);
+    si.a = (int)((cc + 256) >> 9);
+    si.b = (int)((cr + 256) >> 9);
+    return nhi - nlo + 1;
+}
+
+// One slot: the thread's ROWS positions for a view, each read as one
+// 16-byte quad {view pair, partner pair} at shared address pw + entry *
+// quad_bytes (quad_bytes == 16 arrives as an argument, so the address is an
+// integer multiply-add on the FMA pipe).
+template <int MODE, int ROWS>
+__device__ __forceinline__ void rot_slot(const SlotInfo &si, float P, unsigned pw,
+                                         unsigned quad_bytes, int cofs, int rofs,
+                                         float (&partB)[ROWS], float (&partA)[ROWS])
+{
+    unsigned vpos = si.base + (unsigned)(cofs * si.a) + (unsigned)(rofs * si.b);
+    const unsigned step = 4u * (unsigned)si.b;
+    // adjoint hat weights (gather_tile): sat(-P w1 + 1 + P), sat(P w1 + 1 - 2P);
+    // P is the same for a view and its partner
+    const float c0 = 1.f + P, c1 = 1.f - 2.f * P;
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const unsigned addr = (vpos >> 23) * quad_bytes + pw;
+        float2 pb, pa;
+        asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                     : "=f"(pb.x), "=f"(pb.y), "=f"(pa.x), "=f"(pa.y) : "r"(addr));
+        const float w1 = frac_plus_one(vpos);
+        if (MODE == 0) {
+            partB[r] += fmaf(w1, pb.y, pb.x);
+            partA[r] += fmaf(w1, pa.y, pa.x);
+        } else {
+            const float wa = fma_sat(-P, w1, c0), wb = fma_sat(P, w1, c1);
+            partB[r] = fmaf(pb.y, wb, fmaf(pb.x, wa, partB[r]));
+            partA[r] = fmaf(pa.y, wb, fmaf(pa.x, wa, partA[r]));
+        }
+        vpos += step;
+    }
+}
+
+// Add the tile's two partial sums to the output (through the cluster's
+// distributed shared memory first when the views are split over `split`
+// CTAs).  `red` is at least 2 ROWS x 256 floats of shared memory that no
+// copy writes any more; every thread of the CTA calls this.
+template <int MODE, int ROWS>
+__device__ __forceinline__ void rot_finish(const float (&accB)[ROWS], const float (&accA)[ROWS],
+                                           float *red, int split, int rank, int myrow, int col,
+                                           int N, float *__restrict__ out, long long cs,
+                                           long long ls, float scale)
+{
+    if (split > 1) {
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            red[r * 256 + threadIdx.x] = accB[r];
+            red[(ROWS + r) * 256 + threadIdx.x] = accA[r];
+        }
+        cl.sync();
+        const int per = ROWS / split;
+        for (int q = 0; q < per; ++q) {
+            const int r = rank * per + q;
+            float sb = 0.f, sa = 0.f;
+            for (int src = 0; src < split; ++src) {
+                const float *peer = cl.map_shared_rank(red, src);
+                sb += peer[r * 256 + threadIdx.x];
+                sa += peer[(ROWS + r) * 256 + threadIdx.x];
+            }
+            const int row = myrow + 4 * r;
+            const bool edge = MODE != 0 && (row == 0 || col == 0 || row == N - 1 || col == N - 1);
+            if (row < N && col < N && !edge) {
+                atomicAdd(out + (long long)row * cs + (long long)col * ls, sb * scale);
+                atomicAdd(out + (long long)col * cs + (long long)(N - 1 - row) * ls, sa * scale);
+            }
+        }
+        cl.sync();    // no CTA leaves while a peer still reads its partials
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const int row = myrow + 4 * r;
+        if (row >= N || col >= N) break;
+        // a quarter turn maps edge pixels onto edge pixels
+        if (MODE != 0 && (row == 0 || col == 0 || row == N - 1 || col == N - 1)) continue;
+        atomicAdd(out + (long long)row * cs + (long long)col * ls, accB[r] * scale);
+        atomicAdd(out + (long long)col * cs + (long long)(N - 1 - row) * ls, accA[r] * scale);
+    }
+}
+
+// Warp w covers columns 8 (w & 3) .. + 8 and rows 4 ROWS (w >> 2) .. + 4
+// ROWS of the tile; lane l takes column l & 7 and rows l >> 3, + 4, + 8, ...
+// So the 32 lanes of one load read 8 columns x 4 adjacent rows.  A
+// quarter-warp (the 8 columns of one row) spans about 8 entries of the
+// window: one shared-memory wavefront for its 128-bit loads.
+__device__ __forceinline__ int rot_cofs() { return 8 * ((threadIdx.x >> 5) & 3) + (threadIdx.x & 7); }
+template <int ROWS>
+__device__ __forceinline__ int rot_rofs()
+{
+    return 4 * ROWS * (threadIdx.x >> 7) + ((threadIdx.x & 31) >> 3);
+}
+
 // MODE 0: backprojection; MODE 1: matched adjoint (edge pixels left to
-// k_adjoint_edges, as in gather_tile with edge_fixup).
+// k_adjoint_edges, as in gather_tile with edge_fixup).  Stages each chunk's
+// quads with loads from the sinogram.
 template <int MODE, int WMAX, int ROWS>
 __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, int s_ld, int R,
                                                 const View *__restrict__ views, int half,
@@ -76,15 +211,9 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
     __shared__ float slotP[kPairSlots];
     __shared__ float slotDelta[2 * kPairSlots];           // views, then partners
 
-    // Warp w covers columns 8 (w & 3) .. + 8 and rows 4 ROWS (w >> 2) .. +
-    // 4 ROWS of the tile; lane l takes column l & 7 and rows l >> 3, + 4,
-    // + 8, ...  So the 32 lanes of one load read 8 columns x 4 adjacent
-    // rows.  A quarter-warp (the 8 columns of one row) spans about 8 entries
-    // of the window: one shared-memory wavefront for its 128-bit loads.
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int row0 = ty * TH, col0 = tx * kTile;
-    const int cofs = 8 * (warp & 3) + (lane & 7);
-    const int rofs = 4 * ROWS * (warp >> 2) + (lane >> 3);
+    const int cofs = rot_cofs(), rofs = rot_rofs<ROWS>();
     const int col = col0 + cofs;
     const int myrow = row0 + rofs;             // rows myrow + 4 r
 
@@ -94,7 +223,7 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
 
     const int vbeg = (int)((long long)half * rank / split);
     const int vend = (int)((long long)half * (rank + 1) / split);
-    const unsigned sbase = (unsigned)__cvta_generic_to_shared(pairs);
+    const unsigned sbase = smem_addr(pairs);
     for (int chunk = vbeg; chunk < vend; chunk += kPairSlots) {
         const int nslot = min(kPairSlots, vend - chunk);
         if (warp == 0 && lane < kPairSlots) {
@@ -103,21 +232,11 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             float P = 0.f, d0 = 0.f, d1 = 0.f;
             if (lane < nslot) {
                 const View &v = views[chunk + lane];
-                long long cr, cc, c0;
-                if (MODE == 0) { cr = v.brow; cc = v.bcol; c0 = v.b0; }
-                else           { cr = v.krow; cc = v.kcol; c0 = v.k0; }
-                const long long origin = c0 + (long long)row0 * cr + (long long)col0 * cc;
-                const long long dr = (long long)(TH - 1) * cr, dc = (long long)(kTile - 1) * cc;
-                const long long mn = origin + min(0LL, dr) + min(0LL, dc);
-                const long long mx = origin + max(0LL, dr) + max(0LL, dc);
-                const int nlo = (int)(mn >> 32) - 1;
-                const int nhi = (int)(mx >> 32) + 1;
-                if (nhi - nlo + 1 <= WMAX) {
-                    si.nlo = nlo;
-                    si.base = (unsigned)((origin - ((long long)nlo << 32)) >> 9);
-                    si.a = (int)((cc + 256) >> 9);
-                    si.b = (int)((cr + 256) >> 9);
-                    W = nhi - nlo + 1;
+                SlotInfo w;
+                const int width = rot_window<MODE, TH>(v, row0, col0, w);
+                if (width <= WMAX) {
+                    si = w;
+                    W = width;
                 } else if (err) {
                     atomicOr(err, 1);
                 }
@@ -170,74 +289,16 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
             const SlotInfo si = slot[s];
             if (si.nlo == INT_MIN) continue;
             const unsigned pw = sbase + (unsigned)(s * WMAX) * quad_bytes;
-            unsigned vpos = si.base + (unsigned)(cofs * si.a) + (unsigned)(rofs * si.b);
-            const unsigned step = 4u * (unsigned)si.b;
-            // adjoint hat weights (gather_tile): sat(-P w1 + 1 + P), sat(P w1 + 1 - 2P);
-            // P is the same for a view and its partner
-            const float P = MODE == 0 ? 0.f : slotP[s];
-            const float c0 = 1.f + P, c1 = 1.f - 2.f * P;
-#pragma unroll
-            for (int r = 0; r < ROWS; ++r) {
-                const unsigned addr = (vpos >> 23) * quad_bytes + pw;
-                float2 pb, pa;
-                asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
-                             : "=f"(pb.x), "=f"(pb.y), "=f"(pa.x), "=f"(pa.y) : "r"(addr));
-                const float w1 = frac_plus_one(vpos);
-                if (MODE == 0) {
-                    partB[r] += fmaf(w1, pb.y, pb.x);
-                    partA[r] += fmaf(w1, pa.y, pa.x);
-                } else {
-                    const float wa = fma_sat(-P, w1, c0), wb = fma_sat(P, w1, c1);
-                    partB[r] = fmaf(pb.y, wb, fmaf(pb.x, wa, partB[r]));
-                    partA[r] = fmaf(pa.y, wb, fmaf(pa.x, wa, partA[r]));
-                }
-                vpos += step;
-            }
+            rot_slot<MODE, ROWS>(si, MODE == 0 ? 0.f : slotP[s], pw, quad_bytes, cofs, rofs,
+                                 partB, partA);
         }
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) { accB[r] += partB[r]; accA[r] += partA[r]; }
         __syncthreads();
     }
-
-    if (split > 1) {
-        // The last chunk ended with a barrier: the staging area is free.
-        namespace cg = cooperative_groups;
-        cg::cluster_group cl = cg::this_cluster();
-        float *red = reinterpret_cast<float *>(pairs);    // [2 ROWS][256]
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            red[r * 256 + threadIdx.x] = accB[r];
-            red[(ROWS + r) * 256 + threadIdx.x] = accA[r];
-        }
-        cl.sync();
-        const int per = ROWS / split;
-        for (int q = 0; q < per; ++q) {
-            const int r = rank * per + q;
-            float sb = 0.f, sa = 0.f;
-            for (int src = 0; src < split; ++src) {
-                const float *peer = cl.map_shared_rank(red, src);
-                sb += peer[r * 256 + threadIdx.x];
-                sa += peer[(ROWS + r) * 256 + threadIdx.x];
-            }
-            const int row = myrow + 4 * r;
-            const bool edge = MODE != 0 && (row == 0 || col == 0 || row == N - 1 || col == N - 1);
-            if (row < N && col < N && !edge) {
-                atomicAdd(out + (long long)row * cs + (long long)col * ls, sb * scale);
-                atomicAdd(out + (long long)col * cs + (long long)(N - 1 - row) * ls, sa * scale);
-            }
-        }
-        cl.sync();    // no CTA leaves while a peer still reads its partials
-        return;
-    }
-#pragma unroll
-    for (int r = 0; r < ROWS; ++r) {
-        const int row = myrow + 4 * r;
-        if (row >= N || col >= N) break;
-        // a quarter turn maps edge pixels onto edge pixels
-        if (MODE != 0 && (row == 0 || col == 0 || row == N - 1 || col == N - 1)) continue;
-        atomicAdd(out + (long long)row * cs + (long long)col * ls, accB[r] * scale);
-        atomicAdd(out + (long long)col * cs + (long long)(N - 1 - row) * ls, accA[r] * scale);
-    }
+    // the last chunk ended with a barrier: the staging area is free
+    rot_finish<MODE, ROWS>(accB, accA, reinterpret_cast<float *>(pairs), split, rank, myrow, col,
+                           N, out, cs, ls, scale);
 }
 
 template <int MODE, int WMAX, int ROWS>
@@ -253,6 +314,166 @@ __global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_
     gather_tile_rot<MODE, WMAX, ROWS>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
                                 out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
                                 blockIdx.y, pairs, quad_bytes, split, blockIdx.x % split);
+}
+
+// ---------------------------------------------------------------------------
+// TMA-staged form.
+
+// Entries per view pair in the quad array: the backprojection's quads are
+// samples n, n + 1 for n = 0 .. R - 2 (entry n); the adjoint's are n = -1 ..
+// R - 1 (entry n + 1), zero outside the row.
+__host__ __device__ constexpr int quad_entries(int mode, int R) { return mode == 0 ? R - 1 : R + 1; }
+
+// quads[z][j][e] for view pair j (view views[j], partner views[j + half],
+// sinogram rows views[j].view and views[j].view + roff): the quad that
+// k_gather_rot stages for entry e.
+template <int MODE>
+__global__ void k_pair_quads(const float *__restrict__ s_am, int s_ld, long long zs, int R,
+                             const View *__restrict__ views, int half, int roff,
+                             float4 *__restrict__ quads)
+{
+    const int Rq = quad_entries(MODE, R);
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (e >= Rq) return;
+    const View &v = views[j];
+    const float *__restrict__ rv = s_am + blockIdx.z * zs + (size_t)v.view * s_ld;
+    const float *__restrict__ rp = rv + (size_t)roff * s_ld;
+    float4 qd;
+    if (MODE == 0) {
+        const float2 a = make_pair(__ldg(rv + e), __ldg(rv + e + 1), true);
+        const float2 b = make_pair(__ldg(rp + e), __ldg(rp + e + 1), true);
+        qd = make_float4(a.x, a.y, b.x, b.y);
+    } else {
+        const int n = e - 1;
+        const float dv = v.delta, dp = views[j + half].delta;
+        const bool in0 = n >= 0, in1 = n + 1 < R;
+        const float v0 = in0 ? __ldg(rv + n) : 0.f, v1 = in1 ? __ldg(rv + n + 1) : 0.f;
+        const float p0 = in0 ? __ldg(rp + n) : 0.f, p1 = in1 ? __ldg(rp + n + 1) : 0.f;
+        qd = make_float4(v0 * dv, v1 * dv, p0 * dp, p1 * dp);
+    }
+    quads[((size_t)blockIdx.z * half + j) * Rq + e] = qd;
+}
+
+// The paired gather on TMA-staged windows.  tm is a 3-D map over the quad
+// array, (float of the quad, entry, z * half + pair), with a box of 4 x wb
+// x 1 (wb a multiple of 8, so every slot's buffer starts on 128 bytes).
+// There are two buffers of 16 windows.  Warp 0 sets up chunk c + 1 (its
+// windows and one TMA load per view pair onto the buffer's mbarrier) while
+// all warps sum chunk c; the buffer it fills was last read in chunk c - 1,
+// which every thread finished before the barrier that closed it.  (Three
+// buffers cost a resident CTA per SM at 8 rows and measured slower.)  A
+// window wider than wb is skipped with error bit 1; a wait that runs out
+// sets bit 2, waits (bounded) for the CTA's copies still in flight and ends
+// the view loop, and the CTA still takes part in its cluster's reduction.
+template <int MODE, int ROWS>
+__global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ CUtensorMap tm,
+                                                        const View *__restrict__ views, int half,
+                                                        int N, float scale,
+                                                        float *__restrict__ out, long long cs,
+                                                        long long ls, int *__restrict__ err,
+                                                        long long zo, int wb,
+                                                        unsigned quad_bytes, int split)
+{
+    extern __shared__ __align__(128) float4 qbuf[];   // [kStages][kPairSlots][wb]
+    __shared__ __align__(8) unsigned long long full[kStages];
+    __shared__ SlotInfo slot[kStages][kPairSlots];
+    __shared__ float slotP[kStages][kPairSlots];
+    constexpr int TH = kWarps * ROWS;
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int rank = blockIdx.x % split, tx = blockIdx.x / split, ty = blockIdx.y;
+    const int z = blockIdx.z;
+    out += (long long)z * zo;
+    const int row0 = ty * TH, col0 = tx * kTile;
+    const int cofs = rot_cofs(), rofs = rot_rofs<ROWS>();
+    const int col = col0 + cofs;
+    const int myrow = row0 + rofs;
+
+    float accB[ROWS], accA[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) { accB[r] = 0.f; accA[r] = 0.f; }
+
+    const int vbeg = (int)((long long)half * rank / split);
+    const int vend = (int)((long long)half * (rank + 1) / split);
+    const int nchunks = (vend - vbeg + kPairSlots - 1) / kPairSlots;
+    const unsigned qbase = smem_addr(qbuf);
+    const unsigned slot_bytes = (unsigned)wb * 16u;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < kStages; ++b) mbar_init(smem_addr(&full[b]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // Warp 0: windows of chunk c into slot[c % kStages], then the loads.
+    auto issue = [&](int c) {
+        const int chunk = vbeg + c * kPairSlots;
+        const int nslot = min(kPairSlots, vend - chunk);
+        const int b = c % kStages;
+        SlotInfo si = {0u, 0, 0, INT_MIN};
+        float P = 0.f;
+        bool ok = false;
+        if (lane < nslot) {
+            const View &v = views[chunk + lane];
+            SlotInfo w;
+            if (rot_window<MODE, TH>(v, row0, col0, w) <= wb) {
+                si = w;
+                ok = true;
+            } else if (err) {
+                atomicOr(err, 1);
+            }
+            P = v.P;
+        }
+        if (lane < kPairSlots) {
+            slot[b][lane] = si;
+            slotP[b][lane] = P;
+        }
+        const unsigned valid = __ballot_sync(0xffffffffu, ok);
+        const unsigned bar = smem_addr(&full[b]);
+        if (lane == 0) mbar_expect_tx(bar, (unsigned)__popc(valid) * slot_bytes);
+        __syncwarp();
+        if (ok)
+            tma_load_3d(qbase + (unsigned)(b * kPairSlots + lane) * slot_bytes, &tm, 0,
+                        si.nlo + (MODE == 0 ? 0 : 1), z * half + chunk + lane, bar);
+    };
+
+    if (warp == 0 && nchunks > 0) issue(0);
+    int c = 0;
+    bool failed = false;
+    for (; c < nchunks; ++c) {
+        const int b = c % kStages;
+        if (warp == 0 && c + 1 < nchunks) issue(c + 1);
+        const bool ok = mbar_wait(smem_addr(&full[b]), (c / kStages) & 1);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        const int nslot = min(kPairSlots, vend - (vbeg + c * kPairSlots));
+        float partB[ROWS], partA[ROWS];
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) { partB[r] = 0.f; partA[r] = 0.f; }
+        for (int s = 0; s < nslot; ++s) {
+            const SlotInfo si = slot[b][s];
+            if (si.nlo == INT_MIN) continue;
+            const unsigned pw = qbase + (unsigned)(b * kPairSlots + s) * slot_bytes;
+            rot_slot<MODE, ROWS>(si, MODE == 0 ? 0.f : slotP[b][s], pw, quad_bytes, cofs, rofs,
+                                 partB, partA);
+        }
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) { accB[r] += partB[r]; accA[r] += partA[r]; }
+        __syncthreads();
+    }
+    if (failed) {
+        if (threadIdx.x == 0) {
+            if (err) atomicOr(err, 2);
+            // copies still in flight: chunk c and, if issued, chunk c + 1
+            for (int q = c; q < min(c + kStages, nchunks); ++q)
+                mbar_wait(smem_addr(&full[q % kStages]), (q / kStages) & 1);
+        }
+        __syncthreads();
+    }
+    rot_finish<MODE, ROWS>(accB, accA, reinterpret_cast<float *>(qbuf), split, rank, myrow, col,
+                           N, out, cs, ls, scale);
 }
 
 template <int MODE, int WMAX, int ROWS>
@@ -294,12 +515,88 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     return RG_OK;
 }
 
+// TMA box width for a window bound w: a multiple of 8 entries (128 bytes).
+int quad_box(int w) { return (w + 7) & ~7; }
+
+template <int MODE, int ROWS>
+int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
+                   long long ls, int *d_err, cudaStream_t st, const Stack &z, float4 *quads,
+                   int w)
+{
+    const int N = p.g.N, R = p.g.R, half = p.nv / 2, roff = p.g.A / 2;
+    const int Rq = quad_entries(MODE, R);
+    {
+        dim3 g((Rq + 255) / 256, half, z.n);
+        k_pair_quads<MODE><<<g, 256, 0, st>>>(s_am, s_ld, z.in, R, p.d_views, half, roff, quads);
+        RG_CK_LAUNCH("k_pair_quads");
+    }
+    const int wb = quad_box(w);
+    CUtensorMap tm;
+    {
+        EncodeTiledFn fn = tensor_map_encoder();
+        if (!fn) return set_error(RG_ECUDA, "cuTensorMapEncodeTiled is not available");
+        cuuint64_t dims[3] = {4, (cuuint64_t)Rq, (cuuint64_t)half * z.n};
+        cuuint64_t strides[2] = {16, (cuuint64_t)Rq * 16};
+        cuuint32_t box[3] = {4, (cuuint32_t)wb, 1};
+        cuuint32_t estr[3] = {1, 1, 1};
+        CUresult r = fn(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)quads, dims, strides,
+                        box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS)
+            return set_error(RG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    }
+    auto k = k_gather_rot_tma<MODE, ROWS>;
+    // two buffers of 16 windows, which also hold the cluster reduction's partials
+    const size_t smem = std::max((size_t)kStages * kPairSlots * wb * sizeof(float4),
+                                 (size_t)2 * ROWS * 256 * sizeof(float));
+    dim3 grid((N + kTile - 1) / kTile, (N + kWarps * ROWS - 1) / (kWarps * ROWS), z.n);
+    RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
+    const unsigned qb = (unsigned)sizeof(float4);
+    const float scale = MODE == 0 ? p.dth : 1.f;
+    if (split == 1) {
+        k<<<grid, 256, smem, st>>>(tm, p.d_views, half, N, scale, out, cs, ls, d_err, z.out, wb,
+                                   qb, 1);
+        RG_CK_LAUNCH("k_gather_rot_tma");
+        return RG_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RG_CK(cudaLaunchKernelEx(&cfg, k, tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
+                             d_err, z.out, wb, qb, split));
+    RG_CK_LAUNCH("k_gather_rot_tma (cluster)");
+    return RG_OK;
+}
+
+// RG_GATHER_ROT_TMA: 0 stages by loads, 1 by TMA whenever the call brings
+// the quad scratch; unset: by TMA from kTmaMinPairs view pairs.
+bool gather_rot_use_tma(int pairs)
+{
+    const char *e = getenv("RG_GATHER_ROT_TMA");
+    if (e && !strcmp(e, "0")) return false;
+    if (e && !strcmp(e, "1")) return true;
+    return pairs >= kTmaMinPairs;
+}
+
 template <int MODE, int ROWS>
 int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
-                    long long ls, int *d_err, cudaStream_t st, const Stack &z)
+                    long long ls, int *d_err, cudaStream_t st, const Stack &z, void *quads)
 {
     const int t = ROWS == 16 ? 2 : ROWS == 8 ? 1 : 0;
     const int w = MODE == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
+    if (quads && quad_box(w) <= kQuadBox && p.nv / 2 <= 65535 && gather_rot_use_tma(p.nv / 2))
+        return gather_rot_tma<MODE, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z,
+                                          (float4 *)quads, w);
     if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
     if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
     if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
@@ -321,18 +618,24 @@ int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_
     return RG_OK;
 }
 
+size_t gather_quads_bytes(int nv, int R, int nz)
+{
+    if (nv < 2 || R < 2 || nz < 1) return 0;
+    return (size_t)nz * (size_t)(nv / 2) * (size_t)quad_entries(1, R) * sizeof(float4);
+}
+
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z)
+                      const Stack &z, void *quads)
 {
     if (mode == 0) {
-        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
+        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
+        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
     }
-    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
+    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
+    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
 }
 
 }  // namespace rg

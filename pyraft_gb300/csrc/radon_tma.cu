@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "ss_tiles.cuh"
+#include "tma.cuh"
 
 namespace rg {
 
@@ -42,68 +43,6 @@ constexpr int kTmRays = 64;     // rays per CTA (two warps of 32)
 constexpr int kTmViews = 16;    // views per block (max)
 constexpr int kTmVpt = 4;       // views per thread
 constexpr int kTmLines = 16;    // lines per strip
-constexpr int kTmWaitLimit = 1 << 24;                    // polls (backstop)
-constexpr unsigned long long kTmWaitNs = 200000000ull;    // 0.2 s per wait
-
-__device__ __forceinline__ unsigned smem_addr(const void *p)
-{
-    return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
-{
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Wait on phase `parity` of an mbarrier for at most kTmWaitNs (strips
-// normally arrive within microseconds); false if the time ran out.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const unsigned long long t0 = global_ns();
-    for (int it = 0; it < kTmWaitLimit; ++it) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 63) == 63 && global_ns() - t0 > kTmWaitNs) return false;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(unsigned dst, const CUtensorMap *tm, int x, int y,
-                                            int z, unsigned bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-        "l"(reinterpret_cast<unsigned long long>(tm)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
-
 // One full strip of a (ray, view): 16 lines, line r of the strip buffer at
 // byte offset r * BW * 8 (an immediate of the load).  pb (== 8, the bytes
 // of a pair) arrives as a kernel argument, so the sample's address is one
@@ -238,7 +177,7 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
                 const int b = n & 1;
                 xs[b] = x0;
                 bad[b] = (emax + 1 - x0 >= BW) ? 1 : 0;
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                fence_proxy_async_smem();
                 mbar_expect_tx(smem_addr(&full[b]), kBufBytes);
                 tma_load_3d(sbase + b * kBufBytes, tm, x0, i0, z, smem_addr(&full[b]));
             }
@@ -393,12 +332,7 @@ int st_blocks_build(SSPlan &p, const View *hv)
     return RG_OK;
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_fn()
+EncodeTiledFn tensor_map_encoder()
 {
     static std::once_flag once;
     static EncodeTiledFn fn = nullptr;
@@ -420,7 +354,7 @@ static EncodeTiledFn encode_fn()
 static int encode_pairs_map(CUtensorMap *tm, const float2 *pairs, int N, int nz, long long zp,
                             int bw, int box_lines = kTmLines)
 {
-    EncodeTiledFn fn = encode_fn();
+    EncodeTiledFn fn = tensor_map_encoder();
     if (!fn) return set_error(RG_ECUDA, "cuTensorMapEncodeTiled is not available");
     const int pitch = pairs_pitch(N);
     cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)N, (cuuint64_t)nz};
@@ -558,7 +492,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        fence_proxy_async_smem();
         mbar_expect_tx(smem_addr(&full), kTtLines * kTtWin * 8);
         for (int r = 0; r < kTtLines; ++r)
             tma_load_3d(sbase + (r * kTtRow + kTtPad) * 8, tm, p0, i0 + r, z, smem_addr(&full));

@@ -187,10 +187,16 @@ struct Stack {
     long long in = 0, out = 0;
 };
 // rows: rows per thread (4, 8 or 16; 0 = the tuned choice for this geometry).
+// quads: device scratch of gather_quads_bytes(p.nv, p.g.R, z.n) bytes
+// (16-byte aligned) through which the paired path (p.rot_ok, modes 0 and 1)
+// stages its windows by TMA; null makes it stage them with loads.
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
                   float *out, long long cs, long long ls,
                   float *em_x, const float *inv_sens, int *d_err, cudaStream_t st,
-                  int rows = 0, Stack z = Stack());
+                  int rows = 0, Stack z = Stack(), void *quads = nullptr);
+// Bytes of the paired gathers' quad scratch for nz problems of nv views over
+// R rays: a 16-byte quad per (view pair, sample entry), R + 1 entries.
+size_t gather_quads_bytes(int nv, int R, int nz);
 // Rows per thread picked for (geometry, mode) by the autotuner (api.cu).
 int tuned_rows(const SSPlan &p, int mode);
 // Cluster size (1, 2 or 4) for the view split of a gather kernel k launched
@@ -202,7 +208,7 @@ int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, c
 // added to each pixel.
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z);
+                      const Stack &z, void *quads);
 // Whether launch_gather takes the paired path where a plan allows it
 // (RG_GATHER_ROT=0 turns it off).
 bool gather_rot_enabled();

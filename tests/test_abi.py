@@ -50,6 +50,10 @@ def test_rejects_bad_arguments_on_host(lib):
     assert lib.rg_filter(sino, sino, 99, None, 0, None) == -1
 
 
+def _align256(n):
+    return (n + 255) // 256 * 256
+
+
 def test_workspace_queries_are_host_arithmetic(lib):
     img = _img(4096, 256, 256)
     sino = _img(8192, 256, 180, (0.0, 1.0), (math.pi, -1.0))
@@ -57,7 +61,11 @@ def test_workspace_queries_are_host_arithmetic(lib):
     assert n >= 2 * 256 * 258 * 8 + 256 * 180 * 4
     assert lib.rg_em_workspace(sino, img, 2, 10) > lib.rg_em_workspace(sino, img, 2, 1)
     vm = _native.RG_IMAGE(8192, 256, 256, 180, 1, 0.0, 1.0, math.pi, -1.0)   # view-major
-    assert lib.rg_backprojection_slantstack_workspace(vm, img) == 0
+    # a view-major sinogram needs no transposed copy, only the paired
+    # gathers' quads: 16 bytes per (view pair, entry), 90 pairs x 257 entries
+    assert lib.rg_backprojection_slantstack_workspace(vm, img) == _align256(90 * 257 * 16)
+    vm_odd = _native.RG_IMAGE(8192, 256, 256, 179, 1, 0.0, 1.0, math.pi, -1.0)
+    assert lib.rg_backprojection_slantstack_workspace(vm_odd, img) == 0
 
 
 def test_unaligned_workspace_rejected(lib):

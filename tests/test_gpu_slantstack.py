@@ -334,6 +334,61 @@ def test_gathers_quarter_turn_pairs(orc, monkeypatch, n, r, a, rows, split):
         assert rel(adj, adj1) <= 1e-6
 
 
+@pytest.mark.parametrize("n,r,a", [(64, 64, 48), (255, 256, 180), (130, 300, 64), (96, 120, 40)])
+@pytest.mark.parametrize("rows,split", [("4", "1"), ("8", "2"), ("16", "4")])
+def test_gathers_quarter_turn_tma_vs_staged(orc, monkeypatch, n, r, a, rows, split):
+    """The paired gathers with their windows loaded by TMA from the quad
+    prepass (RG_GATHER_ROT_TMA=1: any number of view pairs) against the same
+    gathers staging the windows with loads (RG_GATHER_ROT_TMA=0) and the
+    oracle.  At (130, 300) the 16-row windows are wider than a TMA box and
+    that launch stages with loads; the 4- and 8-row ones take TMA."""
+    rng = np.random.default_rng(5 * n + a)
+    s = inner_sino(rng, r, a)
+    sf = rng.random((r, a))
+    sf[-1, 0] = 0.0
+    monkeypatch.setenv("RG_GATHER_ROWS", rows)
+    monkeypatch.setenv("RG_GATHER_SPLIT", split)
+    monkeypatch.setenv("RG_GATHER_ROT_TMA", "1")
+    adjoint = r <= n
+    bp = np.asarray(rg.backprojection(sino_img(s), (SLANT, (n, n), 0)))
+    if adjoint:
+        adj = np.asarray(rg.radon_transpose(sino_img(sf), (n, n), SLANT))
+    monkeypatch.setenv("RG_GATHER_ROT_TMA", "0")
+    bp1 = np.asarray(rg.backprojection(sino_img(s), (SLANT, (n, n), 0)))
+    assert rel(bp, orc.backprojection_slantstack(s, n)) <= 1e-5
+    assert rel(bp, bp1) <= 1e-6
+    if adjoint:
+        adj1 = np.asarray(rg.radon_transpose(sino_img(sf), (n, n), SLANT))
+        assert rel(adj, orc.radon_slantstack_transpose(sf, n)) <= 1e-5
+        assert rel(adj, adj1) <= 1e-6
+
+
+@pytest.mark.parametrize("a,tma", [(120, "1"), (600, None)])
+def test_em_and_fbp_quarter_turn_tma_vs_staged(orc, monkeypatch, a, tma):
+    """EM with the matched adjoint and with the backprojection, OSEM (6
+    subsets: the count divides A / 2, so each subset pairs), all through
+    rg_em's quad scratch, and the FBP through rg_fbp's, against the same
+    calls with the windows staged by loads.  With 600 views the full-plan
+    calls (300 view pairs) take TMA by default; the OSEM subsets (50 pairs)
+    stage by loads either way."""
+    rng = np.random.default_rng(77)
+    n, r = 128, 128
+    x = interior_image(rng, n) + 0.1
+    y = orc.radon_slantstack(x, r, a)
+    out = {}
+    for mode in (tma, "0"):
+        if mode is None:
+            monkeypatch.delenv("RG_GATHER_ROT_TMA", raising=False)
+        else:
+            monkeypatch.setenv("RG_GATHER_ROT_TMA", mode)
+        out[mode] = (np.asarray(rg.em(sino_img(y), (n, n), 4, method=SLANT)),
+                     np.asarray(rg.em(sino_img(y), (n, n), 4, method=SLANT, reference=True)),
+                     np.asarray(rg.osem(sino_img(y), (n, n), 2, nblocks=6, method=SLANT)),
+                     np.asarray(rg.fbp(sino_img(y), filter="ramlak")))
+    for got, ref in zip(out[tma], out["0"]):
+        assert rel(got, ref) <= 1e-5
+
+
 @pytest.mark.parametrize("n,r,a", [(2, 2, 2), (5, 5, 4), (17, 17, 10), (33, 20, 30), (40, 40, 2)])
 def test_gathers_quarter_turn_small_geometries(orc, monkeypatch, n, r, a):
     """Paired gathers on images much smaller than a tile, and with a single
