@@ -361,8 +361,9 @@ __global__ void k_pair_quads(const float *__restrict__ s_am, int s_ld, long long
 // There are two buffers of 16 windows.  Warp 0 sets up chunk c + 1 (its
 // windows and one TMA load per view pair onto the buffer's mbarrier) while
 // all warps sum chunk c; the buffer it fills was last read in chunk c - 1,
-// which every thread finished before the barrier that closed it.  (Three
-// buffers cost a resident CTA per SM at 8 rows and measured slower.)  A
+// which every thread finished before the barrier that closed it.  That
+// barrier, one per chunk, also orders the slot tables.  (Three buffers cost
+// a resident CTA per SM at 8 rows and measured slower.)  A
 // window wider than wb is skipped with error bit 1; a wait that runs out
 // sets bit 2, waits (bounded) for the CTA's copies still in flight and ends
 // the view loop, and the CTA still takes part in its cluster's reduction.
@@ -438,16 +439,18 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
     };
 
     if (warp == 0 && nchunks > 0) issue(0);
+    // chunk 0's slot tables; those of chunk c + 1, written during chunk c,
+    // are ordered by chunk c's closing barrier
+    __syncthreads();
     int c = 0;
     bool failed = false;
     for (; c < nchunks; ++c) {
         const int b = c % kStages;
         if (warp == 0 && c + 1 < nchunks) issue(c + 1);
+        // A wait that runs out is acted on at the chunk's closing barrier:
+        // until then the thread sums whatever the buffer holds (its reads
+        // stay inside it), and the call reports the error.
         const bool ok = mbar_wait(smem_addr(&full[b]), (c / kStages) & 1);
-        if (__syncthreads_or(!ok)) {
-            failed = true;
-            break;
-        }
         const int nslot = min(kPairSlots, vend - (vbeg + c * kPairSlots));
         float partB[ROWS], partA[ROWS];
 #pragma unroll
@@ -461,7 +464,11 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
         }
 #pragma unroll
         for (int r = 0; r < ROWS; ++r) { accB[r] += partB[r]; accA[r] += partA[r]; }
-        __syncthreads();
+        // closes chunk c: every thread is done with its buffer and slots
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
     }
     if (failed) {
         if (threadIdx.x == 0) {
