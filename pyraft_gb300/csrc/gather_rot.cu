@@ -42,9 +42,14 @@
 // scratch (or for windows wider than a TMA box) k_gather_rot stages the
 // quads itself with loads from the sinogram.
 //
-// Precision: FP32 partial sums over a chunk of 16 view pairs, added across
-// chunks in FP32 (no compensation: the two-level sum keeps the error near
-// 1e-7 of the pixel values).
+// Precision: k_gather_rot keeps FP32 partial sums over each chunk of 16 view
+// pairs and adds them across chunks in FP32.  k_gather_rot_tma sums straight
+// into its accumulators, which frees 2 ROWS registers (40 at 4 rows: 6
+// resident CTAs per SM instead of 5).  An FP32 emulation of that order on a
+// Ram-Lak-filtered phantom sinogram with 1800 views (450-term sums per
+// pixel, cluster ranks and halves added after) is within 2.9e-7 (rel-L2) of
+// the FP64 sum, against 9.0e-8 for the partial sums; the error grows as the
+// square root of the view count.
 #include <string.h>
 
 #include <algorithm>
@@ -452,18 +457,13 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
         // stay inside it), and the call reports the error.
         const bool ok = mbar_wait(smem_addr(&full[b]), (c / kStages) & 1);
         const int nslot = min(kPairSlots, vend - (vbeg + c * kPairSlots));
-        float partB[ROWS], partA[ROWS];
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) { partB[r] = 0.f; partA[r] = 0.f; }
         for (int s = 0; s < nslot; ++s) {
             const SlotInfo si = slot[b][s];
             if (si.nlo == INT_MIN) continue;
             const unsigned pw = qbase + (unsigned)(b * kPairSlots + s) * slot_bytes;
             rot_slot<MODE, ROWS>(si, MODE == 0 ? 0.f : slotP[b][s], pw, quad_bytes, cofs, rofs,
-                                 partB, partA);
+                                 accB, accA);
         }
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) { accB[r] += partB[r]; accA[r] += partA[r]; }
         // closes chunk c: every thread is done with its buffer and slots
         if (__syncthreads_or(!ok)) {
             failed = true;
