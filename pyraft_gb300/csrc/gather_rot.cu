@@ -42,14 +42,13 @@
 // scratch (or for windows wider than a TMA box) k_gather_rot stages the
 // quads itself with loads from the sinogram.
 //
-// Precision: k_gather_rot keeps FP32 partial sums over each chunk of 16 view
-// pairs and adds them across chunks in FP32.  k_gather_rot_tma sums straight
-// into its accumulators, which frees 2 ROWS registers (40 at 4 rows: 6
-// resident CTAs per SM instead of 5).  An FP32 emulation of that order on a
+// Precision: both kernels sum straight into FP32 accumulators (per-chunk
+// partial sums cost 2 ROWS registers: 48 instead of 40 at 4 rows, 5
+// resident CTAs per SM instead of 6).  An FP32 emulation of that order on a
 // Ram-Lak-filtered phantom sinogram with 1800 views (450-term sums per
 // pixel, cluster ranks and halves added after) is within 2.9e-7 (rel-L2) of
-// the FP64 sum, against 9.0e-8 for the partial sums; the error grows as the
-// square root of the view count.
+// the FP64 sum, against 9.0e-8 with partial sums over chunks of 16 pairs;
+// the error grows as the square root of the view count.
 #include <string.h>
 
 #include <algorithm>
@@ -287,18 +286,13 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
         }
         __syncthreads();
 
-        float partB[ROWS], partA[ROWS];
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) { partB[r] = 0.f; partA[r] = 0.f; }
         for (int s = 0; s < nslot; ++s) {
             const SlotInfo si = slot[s];
             if (si.nlo == INT_MIN) continue;
             const unsigned pw = sbase + (unsigned)(s * WMAX) * quad_bytes;
             rot_slot<MODE, ROWS>(si, MODE == 0 ? 0.f : slotP[s], pw, quad_bytes, cofs, rofs,
-                                 partB, partA);
+                                 accB, accA);
         }
-#pragma unroll
-        for (int r = 0; r < ROWS; ++r) { accB[r] += partB[r]; accA[r] += partA[r]; }
         __syncthreads();
     }
     // the last chunk ended with a barrier: the staging area is free
