@@ -42,9 +42,9 @@
 // scratch (or for windows wider than a TMA box) k_gather_rot stages the
 // quads itself with loads from the sinogram.
 //
-// Precision: both kernels sum straight into FP32 accumulators (per-chunk
-// partial sums cost 2 ROWS registers: 48 instead of 40 at 4 rows, 5
-// resident CTAs per SM instead of 6).  An FP32 emulation of that order on a
+// Precision: both kernels sum straight into FP32 accumulators (in
+// k_gather_rot_tma, per-chunk partial sums would cost 2 ROWS registers: 48
+// instead of 40 at 4 rows, 5 resident CTAs per SM instead of 6).  An FP32 emulation of that order on a
 // Ram-Lak-filtered phantom sinogram with 1800 views (450-term sums per
 // pixel, cluster ranks and halves added after) is within 2.9e-7 (rel-L2) of
 // the FP64 sum, against 9.0e-8 with partial sums over chunks of 16 pairs;
