@@ -43,7 +43,7 @@ UPDATES = N * N * A
 # the sinogram (14.9 MB); k_gather_rot_tma reads the quads (29.5 MB, which
 # ncu's cache flush between kernels sends to DRAM) and the zeroed image that
 # the two partial sums per pixel are added to (16.8 MB).
-BP_TRAFFIC_BYTES = 14850560 + 46416640
+BP_TRAFFIC_BYTES = 14850304 + 46378496
 # kernels of one FBP step: k_to_am, k_filter_fft, k_zero_image, k_pair_quads,
 # k_gather_rot_tma
 LAUNCHES_PER_FBP = 5
