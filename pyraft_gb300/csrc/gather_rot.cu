@@ -39,16 +39,18 @@
 // pair's window as one TMA box into shared memory, double-buffered on two
 // mbarriers, so the next chunk of 16 pairs streams in while the current one
 // is summed and no thread spends issue slots on staging.  Without that
-// scratch (or for windows wider than a TMA box) k_gather_rot stages the
-// quads itself with loads from the sinogram.
+// scratch, below kTmaMinPairs view pairs (where the prepass launch and the
+// pipeline fill cost more) or for windows wider than a TMA box,
+// k_gather_rot stages the quads itself with loads from the sinogram.
 //
 // Precision: both kernels sum straight into FP32 accumulators (in
 // k_gather_rot_tma, per-chunk partial sums would cost 2 ROWS registers: 48
-// instead of 40 at 4 rows, 5 resident CTAs per SM instead of 6).  An FP32 emulation of that order on a
-// Ram-Lak-filtered phantom sinogram with 1800 views (450-term sums per
-// pixel, cluster ranks and halves added after) is within 2.9e-7 (rel-L2) of
-// the FP64 sum, against 9.0e-8 with partial sums over chunks of 16 pairs;
-// the error grows as the square root of the view count.
+// instead of 40 at 4 rows, 5 resident CTAs per SM instead of 6).  An FP32
+// emulation of that order on a Ram-Lak-filtered phantom sinogram with 1800
+// views (450-term sums per pixel, cluster ranks and halves added after) is
+// within 2.9e-7 (rel-L2) of the FP64 sum, against 9.0e-8 with partial sums
+// over chunks of 16 pairs; the error grows as the square root of the view
+// count.
 #include <string.h>
 
 #include <algorithm>
