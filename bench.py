@@ -44,9 +44,9 @@ UPDATES = N * N * A
 # ncu's cache flush between kernels sends to DRAM) and the zeroed image that
 # the two partial sums per pixel are added to (16.8 MB).
 BP_TRAFFIC_BYTES = 14850304 + 46378496
-# kernels of one FBP step: k_to_am, k_filter_fft, k_zero_image, k_pair_quads,
-# k_gather_rot_tma
-LAUNCHES_PER_FBP = 5
+# kernels of one FBP step: k_to_am, k_filter_fft, k_pair_quads (which also
+# zeroes the output), k_gather_rot_tma
+LAUNCHES_PER_FBP = 4
 
 
 def smem_ceiling(updates, ms, sms, sm_mhz):
@@ -641,7 +641,7 @@ def main():
         "roofline": {"bound": "hbm",
                      "kernel": "k_gather_rot_tma<0> (backprojection, views paired a quarter "
                                "turn apart, windows staged by TMA; timed as the call, with its "
-                               "k_zero_image and k_pair_quads)",
+                               "k_pair_quads prepass, which also zeroes the output)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 3), "traffic": BP_TRAFFIC_BYTES,
                      "algorithmic_bytes": alg_bytes, "kernel_ms": round(bp_ms, 4),

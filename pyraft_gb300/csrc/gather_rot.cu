@@ -327,12 +327,26 @@ __host__ __device__ constexpr int quad_entries(int mode, int R) { return mode ==
 
 // quads[z][j][e] for view pair j (view views[j], partner views[j + half],
 // sinogram rows views[j].view and views[j].view + roff): the quad that
-// k_gather_rot stages for entry e.
+// k_gather_rot stages for entry e.  zout != nullptr: also zero the N x N
+// output of slice z (strides cs, ls; slices zo apart), which the gather then
+// adds its partial sums to, in place of a launch of its own.
 template <int MODE>
 __global__ void k_pair_quads(const float *__restrict__ s_am, int s_ld, long long zs, int R,
                              const View *__restrict__ views, int half, int roff,
-                             float4 *__restrict__ quads)
+                             float4 *__restrict__ quads, float *__restrict__ zout, int N,
+                             long long cs, long long ls, long long zo)
 {
+    if (zout) {
+        const long long n = (long long)N * N;
+        const long long nt = (long long)gridDim.x * gridDim.y * blockDim.x;
+        float *o = zout + blockIdx.z * zo;
+        for (long long i = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x +
+                           threadIdx.x;
+             i < n; i += nt) {
+            const int r = (int)(i / N), c = (int)(i - (long long)r * N);
+            o[(long long)r * cs + (long long)c * ls] = 0.f;
+        }
+    }
     const int Rq = quad_entries(MODE, R);
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
@@ -524,13 +538,14 @@ int quad_box(int w) { return (w + 7) & ~7; }
 template <int MODE, int ROWS>
 int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                    long long ls, int *d_err, cudaStream_t st, const Stack &z, float4 *quads,
-                   int w)
+                   int w, bool zero_out)
 {
     const int N = p.g.N, R = p.g.R, half = p.nv / 2, roff = p.g.A / 2;
     const int Rq = quad_entries(MODE, R);
     {
         dim3 g((Rq + 255) / 256, half, z.n);
-        k_pair_quads<MODE><<<g, 256, 0, st>>>(s_am, s_ld, z.in, R, p.d_views, half, roff, quads);
+        k_pair_quads<MODE><<<g, 256, 0, st>>>(s_am, s_ld, z.in, R, p.d_views, half, roff, quads,
+                                              zero_out ? out : nullptr, N, cs, ls, z.out);
         RG_CK_LAUNCH("k_pair_quads");
     }
     const int wb = quad_box(w);
@@ -593,13 +608,16 @@ bool gather_rot_use_tma(int pairs)
 
 template <int MODE, int ROWS>
 int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
-                    long long ls, int *d_err, cudaStream_t st, const Stack &z, void *quads)
+                    long long ls, int *d_err, cudaStream_t st, const Stack &z, void *quads,
+                    bool zero_out)
 {
     const int t = ROWS == 16 ? 2 : ROWS == 8 ? 1 : 0;
     const int w = MODE == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
     if (quads && quad_box(w) <= kQuadBox && p.nv / 2 <= 65535 && gather_rot_use_tma(p.nv / 2))
         return gather_rot_tma<MODE, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z,
-                                          (float4 *)quads, w);
+                                          (float4 *)quads, w, zero_out);
+    if (zero_out)
+        if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
     if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
     if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
     if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
@@ -629,16 +647,17 @@ size_t gather_quads_bytes(int nv, int R, int nz)
 
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z, void *quads)
+                      const Stack &z, void *quads, bool zero_out)
 {
+    const bool zo = zero_out;
     if (mode == 0) {
-        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
-        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
-        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
+        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
+        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
+        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
     }
-    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
-    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
-    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads);
+    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
+    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
+    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
 }
 
 }  // namespace rg

@@ -204,11 +204,12 @@ int tuned_rows(const SSPlan &p, int mode);
 int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st);
 // Backprojection (mode 0) or matched adjoint (mode 1, interior pixels: the
 // edge pixels are left to the caller) with views paired a quarter turn
-// apart (p.rot_ok).  The output must be zeroed first; two partial sums are
-// added to each pixel.
+// apart (p.rot_ok).  Two partial sums are added to each pixel of an output
+// that is zeroed first: by this call when zero_out (in the quad prepass
+// where it runs), else by the caller.
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z, void *quads);
+                      const Stack &z, void *quads, bool zero_out);
 // Whether launch_gather takes the paired path where a plan allows it
 // (RG_GATHER_ROT=0 turns it off).
 bool gather_rot_enabled();

@@ -569,10 +569,9 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
 {
     if (rows == 0) rows = tuned_rows(p, mode);
     if (mode == 0) {
-        if (!em_x && p.rot_ok && gather_rot_enabled()) {
-            if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
-            return launch_gather_rot(p, 0, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads);
-        }
+        if (!em_x && p.rot_ok && gather_rot_enabled())
+            return launch_gather_rot(p, 0, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads,
+                                     true);
         if (em_x)
             return gather_rows<0, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
         return gather_rows<0, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
@@ -586,7 +585,8 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
             if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
             if (int rc = adjoint_edges<1, false>(p, s_am, s_ld, out, cs, ls, nullptr, nullptr, st, z))
                 return rc;
-            return launch_gather_rot(p, 1, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads);
+            return launch_gather_rot(p, 1, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads,
+                                     false);
         }
         if (em_x)
             return gather_rows<1, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
