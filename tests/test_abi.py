@@ -68,6 +68,29 @@ def test_workspace_queries_are_host_arithmetic(lib):
     assert lib.rg_backprojection_slantstack_workspace(vm_odd, img) == 0
 
 
+def test_workspaces_hold_the_paired_gathers_quads(lib):
+    """Every query whose call can run the TMA-staged paired gathers reserves
+    their sample quads: 16 bytes per (view pair, entry), R + 1 entries, per
+    slice, in 256-byte-aligned pieces after the call's other scratch."""
+    R, A, n, S = 256, 180, 256, 4
+    img = _img(4096, n, n)
+    sino = _img(8192, R, A, (0.0, 1.0), (math.pi, -1.0))             # ray-major
+    vm = _native.RG_IMAGE(8192, R, R, A, 1, 0.0, 1.0, math.pi, -1.0)   # view-major
+    al = _align256
+    quads = (A // 2) * (R + 1) * 16
+    sino_b = R * A * 4
+    assert lib.rg_backprojection_slantstack_workspace(sino, img) == al(sino_b) + al(quads)
+    assert lib.rg_radon_transpose_slantstack_workspace(vm, img) == al(quads)
+    assert lib.rg_radon_transpose_slantstack_stack_workspace(vm, img, S) == al(S * quads)
+    assert (lib.rg_radon_transpose_slantstack_stack_workspace(sino, img, S) ==
+            al(S * sino_b) + al(S * quads))
+    assert lib.rg_fbp_workspace(sino, img, 1) == 2 * al(sino_b) + al(quads)
+    # EM: the quads of the largest subset (ceil(A / nsubsets) views)
+    em1, em10 = lib.rg_em_workspace(sino, img, 2, 1), lib.rg_em_workspace(sino, img, 2, 10)
+    # (the subsets also carry one sensitivity image each: 9 more for 10)
+    assert em1 - em10 == al(quads) - al((18 // 2) * (R + 1) * 16) - 9 * al(n * n * 4)
+
+
 def test_unaligned_workspace_rejected(lib):
     img = _img(4096, 16, 16)
     sino = _img(8192, 16, 12, (0.0, 1.0), (math.pi, -1.0))
