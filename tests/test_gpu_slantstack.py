@@ -389,6 +389,31 @@ def test_em_and_fbp_quarter_turn_tma_vs_staged(orc, monkeypatch, a, tma):
         assert rel(got, ref) <= 1e-5
 
 
+def test_paired_gathers_overwrite_the_output(orc, monkeypatch):
+    """The paired gathers add two partial sums per pixel onto an output that
+    the call zeroes first (for the TMA-staged backprojection, inside the quad
+    prepass): an output buffer full of NaN must come back equal to the oracle,
+    with the windows staged by TMA and by loads."""
+    from pyraft_gb300.raftypes import rg_image
+    rng = np.random.default_rng(21)
+    n, r, a = 96, 96, 600                       # 300 view pairs: TMA by default
+    s = inner_sino(rng, r, a)
+    s[-1, 0] = 0.0                              # the adjoint's one exact grid tie
+    L = _native.load()
+    st = torch.cuda.current_stream().cuda_stream
+    s_dev = torch.from_numpy(s.astype(np.float32)).cuda()   # rg_image keeps only its pointer
+    S = rg_image(rg.gpu_image(s_dev, *SINO_C))
+    cases = ((L.rg_backprojection_slantstack, orc.backprojection_slantstack(s, n)),
+             (L.rg_radon_transpose_slantstack, orc.radon_slantstack_transpose(s, n)))
+    for tma in ("1", "0"):
+        monkeypatch.setenv("RG_GATHER_ROT_TMA", tma)
+        for fn, ref in cases:
+            out = torch.full((n, n), float("nan"), device="cuda")
+            _native.check(fn(S, rg_image(rg.gpu_image(out)), None, 0, st))
+            torch.cuda.synchronize()
+            assert rel(out.cpu().numpy(), ref) <= 1e-5
+
+
 @pytest.mark.parametrize("n,r,a", [(2, 2, 2), (5, 5, 4), (17, 17, 10), (33, 20, 30), (40, 40, 2)])
 def test_gathers_quarter_turn_small_geometries(orc, monkeypatch, n, r, a):
     """Paired gathers on images much smaller than a tile, and with a single
