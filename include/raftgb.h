@@ -94,18 +94,19 @@ int rg_radon_slantstack(rg_image phantom, rg_image radon,
                         void *workspace, size_t workspace_bytes, void *stream);
 
 /* Same Radon transform for callers that cannot allocate device memory (no
- * counterpart in the reference): code running inside a stream capture,
- * where allocation calls are not allowed, or a process whose device memory
- * is already committed to another pool.  All scratch (per-view table, line
- * pairs, result staging) lives in one static 32 MiB device array that every
- * GPU loading the library holds until exit; the call makes no cudaMalloc,
- * cudaFree or other allocation.  Geometries needing more scratch (about
- * size 1200 with 1800 views and as many rays) or more than 4096 views are
- * rejected with RG_EINVAL.  The first call on a device resolves the array's
- * device address (cudaGetSymbolAddress): make it before any stream capture.
- * Calls share the array, so calls that overlap on the GPU race; each call
- * rewrites all the scratch it reads, so nothing needs clearing between
- * calls.                                                                     */
+ * counterpart in the reference): a process whose device memory is already
+ * committed to another framework's pool, or an acquisition loop that must
+ * not allocate once it runs (cudaMalloc/cudaFree may synchronise the whole
+ * device).  All scratch (per-view table, line pairs, result staging) lives
+ * in one static 32 MiB device array that every GPU loading the library
+ * holds until exit; the call makes no cudaMalloc, cudaFree or other
+ * allocation.  Geometries needing more scratch (about size 1200 with 1800
+ * views and as many rays) or more than 4096 views are rejected with
+ * RG_EINVAL.  The first call on a device (and the first after its context
+ * was replaced) resolves the array's device address with
+ * cudaGetSymbolAddress.  Calls share the array, so calls that overlap on
+ * the GPU race; each call rewrites all the scratch it reads, so nothing
+ * needs clearing between calls.                                             */
 int rg_radon_slantstack_noalloc(rg_image phantom, rg_image radon, void *stream);
 
 /* Pixel-driven backprojection with linear interpolation in t, scaled by

@@ -1,5 +1,5 @@
 """ctypes bindings to the reference's own hot-path C/C++ compiled in place
-(``make -C oracle ref`` -> ``oracle/_ref/libraft_ref.so``).
+(``make -C oracle ref REF_SRC=<checkout>/raft`` -> ``oracle/_ref/libraft_ref.so``).
 
 TEST INFRASTRUCTURE: used only to pin the oracle restatement
 (tests/test_oracle_golden.py, when the library exists) and to generate the

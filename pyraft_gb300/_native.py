@@ -15,6 +15,11 @@ LIB_PATH = os.path.join(HERE, "lib", "libraftgb.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "raftgb.h")
 
 RG_OK = 0
+RG_EINVAL = -1
+RG_ECUDA = -2
+RG_ENOMEM = -3
+RG_EUNSUPPORTED = -4
+RG_EWORKSPACE = -5
 RG_BRESENHAM = 1
 RG_SLANTSTACK = 2
 RG_SLANTSTACK_BP = 3

@@ -5,21 +5,24 @@
 // two line-pair copies of the image and, unless the sinogram is view-major,
 // a view-major result buffer.  It takes them from the caller's workspace or
 // from the stream-ordered pool, and it caches plans in cudaMalloc'd memory.
-// Some callers cannot do any of that: code that runs while a stream is being
-// captured (allocation calls are not allowed there), or a process that has
-// handed all device memory to another framework's pool or to a
-// data-acquisition loop and must not allocate after start-up.  For them,
-// rg_radon_slantstack_noalloc keeps all its scratch in one file-scope
-// __device__ array of kNoAllocBytes (32 MiB), which every GPU that loads the
-// library holds until the process exits.  The call itself runs the same
-// kernels as rg_radon_slantstack and calls no cudaMalloc, cudaFree or other
-// allocating routine; the per-view table is built in a static host array
-// (under a mutex) and copied into the scratch on the caller's stream.
+// Some callers cannot do any of that: a process that has handed all of its
+// device memory to another framework's pool at start-up, or a
+// data-acquisition loop that must not allocate once it runs (cudaMalloc and
+// cudaFree may synchronise the whole device and stall the streams that move
+// detector frames).  For them, rg_radon_slantstack_noalloc keeps all its
+// scratch in one file-scope __device__ array of kNoAllocBytes (32 MiB), which
+// every GPU that loads the library holds until the process exits.  The call
+// runs the same kernels as rg_radon_slantstack and calls no cudaMalloc,
+// cudaFree or other allocating routine; the per-view table is built in a
+// static host array (under a mutex) and copied into the scratch on the
+// caller's stream.
 //
 // Host code cannot use the array's name as a device address (it names a
-// host-side shadow), so the first call on each device looks up the device
-// address with cudaGetSymbolAddress while that device is current and caches
-// it; make that first call before any stream capture.
+// host-side shadow), so the first call on each device, with that device
+// current, looks up the device address with cudaGetSymbolAddress and caches
+// it together with the identity of the device's current context.  A call
+// that finds another context there (the old one was destroyed, e.g. by
+// cudaDeviceReset, and the module loaded again) looks the address up anew.
 //
 // All calls on a device share the one array, and each call overwrites every
 // byte it later reads (the view table, both line-pair copies with their zero
@@ -40,23 +43,69 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 std::mutex g_mu;
-void *g_dev_ptr[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (looked up once
-// per device).  Caller holds g_mu.
+// Per device: the scratch's device address and the id of the context it
+// was resolved in.
+struct ScratchAddr {
+    void *ptr = nullptr;
+    unsigned long long ctx_id = 0;
+};
+ScratchAddr g_addr[kMaxDevices];
+
+// Identity of the calling thread's current context (the device's primary
+// context under the runtime API), from the driver through the runtime's
+// entry-point query, so the library does not link libcuda itself.
+int current_context_id(unsigned long long *id)
+{
+    typedef int (*GetCurrent)(void **);
+    typedef int (*GetId)(void *, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    if (!get_current || !get_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        RG_CK(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000,
+                                               cudaEnableDefault, &q1));
+        RG_CK(cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault,
+                                               &q2));
+        if (q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return set_error(RG_EUNSUPPORTED, "driver lacks cuCtxGetCurrent/cuCtxGetId");
+        get_current = (GetCurrent)f1;
+        get_id = (GetId)f2;
+    }
+    void *ctx = nullptr;
+    *id = 0;
+    if (get_current(&ctx) != 0)
+        return set_error(RG_ECUDA, "cuCtxGetCurrent failed for the no-alloc scratch");
+    if (ctx && get_id(ctx, id) != 0)
+        return set_error(RG_ECUDA, "cuCtxGetId failed for the no-alloc scratch");
+    return RG_OK;      // *id stays 0 while the thread has no current context
+}
+
+// Device address of g_noalloc_scratch on the current device: looked up once
+// per device (and again if the device's context was replaced).  Caller holds
+// g_mu.
 int scratch_address(void **out)
 {
     int dev = 0;
     RG_CK(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kMaxDevices)
         return set_error(RG_EUNSUPPORTED, "device ordinal %d beyond %d", dev, kMaxDevices);
-    if (!g_dev_ptr[dev]) {
+    unsigned long long ctx = 0;
+    int rc = current_context_id(&ctx);
+    if (rc) return rc;
+    ScratchAddr &a = g_addr[dev];
+    if (!a.ptr || ctx == 0 || a.ctx_id != ctx) {
+        // cudaGetSymbolAddress also makes the device's primary context
+        // current when the thread has none yet; read its id after it.
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(no-alloc scratch)");
-        g_dev_ptr[dev] = p;
+        if ((rc = current_context_id(&ctx))) return rc;
+        a.ptr = p;
+        a.ctx_id = ctx;
     }
-    *out = g_dev_ptr[dev];
+    *out = a.ptr;
     return RG_OK;
 }
 

@@ -1,12 +1,16 @@
-"""FBP filter step as a row-wise spatial convolution on the GPU.
+"""FBP filter step on the GPU, one view at a time along t.
 
 * ``lowpassino_fbp(sino)``: pyraft's filter (pyraft/filters/filters.py:13-68,
-  a cosine-windowed ramp applied by circular FFT along t).  Here the same
-  linear operator is applied as a circular convolution with its spatial
-  kernel Re(ifft(G)), computed once per geometry in FP64.
-* ``ramlak(sino)``: the discrete Ram-Lak filter, linear convolution,
+  a cosine-windowed ramp applied by circular FFT along t).  Here it is a
+  circular FFT of length R (k_filter_fft) when R is a power of two up to
+  16384, else a circular convolution with its spatial kernel Re(ifft(G)),
+  computed once per geometry in FP64 (k_conv_rows).
+* ``ramlak(sino)``: the discrete Ram-Lak filter as a linear convolution,
   q[n] = dt * sum_k h[n-k] p[k], h[0] = 1/(4 dt^2),
-  h[odd m] = -1/(pi^2 m^2 dt^2), h[even m != 0] = 0.
+  h[odd m] = -1/(pi^2 m^2 dt^2), h[even m != 0] = 0.  Up to 8192 rays it is
+  evaluated by a zero-padded FFT of the first difference (k_filter_fft),
+  above that by direct sums (k_ramlak_rows); both give the same linear
+  convolution.
 Both keep the sinogram's corners and return the input's kind (host image or
 gpu_image).
 """

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the reference itself.
 
 Runs the reference's own hot-path C/C++ (compiled in place by
-``make -C oracle ref`` into oracle/_ref/libraft_ref.so) on small seeded
+``make -C oracle ref REF_SRC=<checkout>/raft`` into oracle/_ref/libraft_ref.so) on small seeded
 inputs and saves inputs and outputs as compressed .npz files.  The tests then
 pin the oracle restatement (and through it the CUDA path) to these outputs
 without needing the reference tree.
@@ -36,7 +36,7 @@ DDA_RAYS = [(th, t) for th in (0.0, 1e-3, 0.3, math.pi / 4, 1.0, math.pi / 2,
 
 def main() -> None:
     if not R.available():
-        raise SystemExit("oracle/_ref/libraft_ref.so missing: run `make -C oracle ref`")
+        raise SystemExit("oracle/_ref/libraft_ref.so missing: run `make -C oracle ref REF_SRC=<checkout>/raft`")
     rng = np.random.default_rng(20261203)
     out = {}
 

@@ -1,14 +1,16 @@
 """The allocation-free Radon entry point, rg_radon_slantstack_noalloc.
 
-It exists for callers that cannot allocate device memory: code running
-while a stream is captured, or a process whose device memory already belongs
-to another pool.  Its scratch lives in a static device array instead of a
-workspace or the stream-ordered pool.  This test calls it through the C ABI
-twice in a row, on different inputs, and checks each result against the
-regular entry point rg_radon_slantstack within the rel-L2 1e-5 tolerance
-of the other Radon tests (both run the same kernels, so they agree to the
-last bit in practice).  A leftover from the first call would show up in the
-second.  It is collected last so that a failure here cannot hide others.
+It exists for callers that cannot allocate device memory: a process whose
+device memory already belongs to another framework's pool, or an
+acquisition loop that must not allocate once it runs (cudaMalloc and
+cudaFree may synchronise the whole device).  Its scratch lives in a static
+device array instead of a workspace or the stream-ordered pool.  This test
+calls it through the C ABI twice in a row, on different inputs, and checks
+each result against the regular entry point rg_radon_slantstack within the
+rel-L2 1e-5 tolerance of the other Radon tests (both run the same kernels,
+so they agree to the last bit in practice).  A leftover from the first call
+would show up in the second.  It is collected last so that a failure here
+cannot hide others.
 """
 import math
 
@@ -57,5 +59,10 @@ def test_noalloc_rejects_oversized_geometry():
     big = torch.zeros((8, 8), dtype=torch.float32, device="cuda")
     img = _native.RG_IMAGE(big.data_ptr(), 2048, 1, 2048, 2048, -1.0, 1.0, 1.0, -1.0)
     sino = _native.RG_IMAGE(big.data_ptr(), 2048, 1, 1800, 1800, 0.0, 1.0, math.pi, -1.0)
-    assert lib.rg_radon_slantstack_noalloc(img, sino, None) == -1
+    assert lib.rg_radon_slantstack_noalloc(img, sino, None) == _native.RG_EINVAL
     assert b"static scratch" in lib.rg_last_error()
+    # more views than the per-view table holds (4096)
+    img = _native.RG_IMAGE(big.data_ptr(), 64, 1, 64, 64, -1.0, 1.0, 1.0, -1.0)
+    sino = _native.RG_IMAGE(big.data_ptr(), 64, 1, 4097, 4097, 0.0, 1.0, math.pi, -1.0)
+    assert lib.rg_radon_slantstack_noalloc(img, sino, None) == _native.RG_EINVAL
+    assert b"4096" in lib.rg_last_error()
