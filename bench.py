@@ -11,11 +11,18 @@ resident sinogram.  The sinogram (14.7 MB) fits in L2, so L2 is flushed
 (160 MiB write, above the 129 MB L2) before every timed step and the step
 time is the sum of per-step CUDA-event intervals.
 
-Also reported: the backprojection kernel alone against the HBM roofline of
-the gather-byte model (8 B per interpolated update + compulsory image and
-sinogram bytes), the end-to-end time of the same call with pinned host
-buffers and both copies inside the timed region, and the reference
-algorithm on the host cores (oracle port, bounded sample).
+Also reported on the same line:
+- the backprojection call alone against its shared-memory roofline (8 B of
+  shared memory per interpolated update, one 128-byte wavefront per SM per
+  clock), with its measured DRAM traffic against the HBM peak;
+- the end-to-end time of the same call with pinned host buffers and both
+  copies inside the timed region;
+- `osem`: the EM/OSEM half of the metric -- plain EM 100 iterations and OSEM
+  10 x 10 on a 1024^2, 720-view emission slice, and the batched uneven OSEM
+  (256 slices, 10 subsets x 20 iterations, one persistent batch per
+  sub-iteration, graph-captured) against the plain one-slice-per-call form;
+- the reference algorithm on the host cores (oracle port, a bounded sample
+  of 1/32 of the step spread over the image and the views).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -49,19 +56,40 @@ BP_TRAFFIC_BYTES = 14850304 + 46378496
 LAUNCHES_PER_FBP = 4
 
 
-def smem_ceiling(updates, ms, sms, sm_mhz):
-    """The gathers' shared-memory roofline: each update reads one 8-byte
-    sample pair from shared memory, and the SM serves one 128-byte
-    wavefront per clock: 16 updates per SM per clock.  (The paired kernel
-    reads a view's pair and its partner's with one 128-bit load, four
-    wavefronts for 64 updates.)"""
+def smem_roofline(updates, ms, sms, sm_mhz, traffic, compulsory, hbm_peak, hbm_kind):
+    """Roofline of the paired backprojection gather.
+
+    Its bound is shared-memory bandwidth, not HBM: every update reads one
+    8-byte sample pair (the view's; the partner view's pair arrives in the
+    same 128-bit load) from shared memory, and an SM serves one 128-byte
+    wavefront per clock, so at most 16 updates per SM per clock.  The
+    8 B/update "gather-byte" figure therefore counts shared-memory bytes; a
+    staged sample serves ~1000 updates, and DRAM carries only the sinogram,
+    the sample quads and the output.  `hbm` reports the measured DRAM
+    traffic of the call (ncu) over its CUDA-event time against the HBM peak.
+    """
     mhz = sm_mhz or 2070.0
-    peak = 16.0 * sms * mhz * 1e6 / 1e9
-    got = updates / (ms * 1e-3) / 1e9
-    return {"unit": "GUPS", "achieved": round(got, 1), "peak": round(peak, 1),
-            "frac": round(got / peak, 3), "sms": sms, "sm_mhz": mhz,
-            "model": "8 B of shared memory per update; 128-byte wavefronts, 1 per SM "
-                     "per clock"}
+    peak = 128.0 * sms * mhz * 1e6 / 1e9               # GB/s of shared-memory wavefronts
+    got = 8.0 * updates / (ms * 1e-3) / 1e9
+    dram = traffic / (ms * 1e-3) / 1e9
+    return {"bound": "smem", "achieved": round(got, 1), "peak": round(peak, 1), "unit": "GB/s",
+            "frac": round(got / peak, 3), "traffic": traffic,
+            "algorithmic_bytes": 8 * updates,
+            "model": "8 B of shared memory per (pixel, view) update (one sample pair); "
+                     "one 128-byte shared-memory wavefront per SM per clock = 16 updates per "
+                     "SM per clock",
+            "peak_source": f"derived: 128 B x {sms} SMs x {mhz:.0f} MHz (SM clock sampled "
+                           f"during the run); MEASURED_PEAKS.json has no shared-memory figure",
+            "gups": {"achieved": round(updates / (ms * 1e-3) / 1e9, 1),
+                     "peak": round(16.0 * sms * mhz * 1e6 / 1e9, 1)},
+            "hbm": {"achieved_gbs": round(dram, 1), "peak": hbm_peak,
+                    "peak_source": f"{hbm_kind} (MEASURED_PEAKS.json hbm_gbs)",
+                    "frac": round(dram / hbm_peak, 4),
+                    "traffic_bytes": traffic, "compulsory_bytes": compulsory,
+                    "traffic_over_compulsory": round(traffic / compulsory, 2),
+                    "note": "DRAM bytes of one call (ncu dram__bytes_read.sum + "
+                            "dram__bytes_write.sum of k_pair_quads + k_gather_rot_tma); "
+                            "compulsory = sinogram read + image written once"}}
 
 
 def env_rank():
@@ -144,27 +172,47 @@ class Clocks:
 # ----------------------------------------------------------------------------
 # CPU baseline (bounded sample of the same workload on the host cores)
 
-def cpu_fbp_sample(sino_np, kind_ref):
-    """Time the filter on a subset of views and the backprojection on a
-    subset of image rows; scale to the full step.  Returns (est_step_s,
-    sample description, cores, kind)."""
+CPU_SAMPLE = 32          # the CPU legs process 1/32 of a step
+
+
+def cpu_fbp_sample(sino_np):
+    """One bounded sample of the FBP step on the host cores: 1/32 of the
+    step's work in both of its legs, spread over the whole input.
+    - filter: every 32nd view, Ram-Lak by numpy FFT (zero-padded linear
+      convolution; pyraft filters by numpy FFT, pyraft/filters/filters.py:13-68);
+    - backprojection: every 32nd image row (64 of 2048), the FP64 oracle port
+      of raft_backprojection_slantstack (raft/raft_backprojection_slantstack.c:
+      121-180) on all host cores.
+    Returns (seconds, updates, description, cores, kind); updates = the
+    backprojection updates of the sampled rows (pixels x views)."""
     import numpy as np
     from oracle import oracle as O
     cores = os.cpu_count() or 1
-    rows, views = 64, 96
+    rows = N // CPU_SAMPLE
     dt = 2.0 / (R - 1)
     t0 = time.perf_counter()
-    O.ramlak_views(np.ascontiguousarray(sino_np.T), dt, views, threads=cores)
+    O.ramlak_fft(sino_np[:, ::CPU_SAMPLE], dt)
     s_filter = time.perf_counter() - t0
     t0 = time.perf_counter()
-    O.backprojection_rows(sino_np, N, N // 2 - rows // 2, N // 2 + rows // 2, threads=cores)
+    O.backprojection_rowstep(sino_np, N, CPU_SAMPLE // 2, CPU_SAMPLE, rows, threads=cores)
     s_bp = time.perf_counter() - t0
-    cpu_fbp_sample.last_sample_s = s_filter + s_bp
-    sample = (f"FP64 oracle port of raft_backprojection_slantstack on {rows} of {N} image "
-              f"rows and the Ram-Lak convolution on {views} of {A} views, each scaled to the "
-              f"full 2048^2 x 1800 step (the sample itself runs "
-              f"{1e3 * (s_filter + s_bp):.0f} ms; ms_per_step is the scaled full step)")
-    return s_filter * (A / views) + s_bp * (N / rows), sample, cores, "port"
+    sample = (f"1/{CPU_SAMPLE} of the FBP step, spread over the input: Ram-Lak by numpy FFT of "
+              f"one view in {CPU_SAMPLE} ({len(range(0, A, CPU_SAMPLE))} of {A}, one thread) and "
+              f"the FP64 oracle port of raft_backprojection_slantstack on one image row in "
+              f"{CPU_SAMPLE} ({rows} of {N}, {cores} threads); GUPS = the sampled rows' pixel x view "
+              f"updates / sample time (filter {1e3 * s_filter:.0f} ms + backprojection "
+              f"{1e3 * s_bp:.0f} ms)")
+    return s_filter + s_bp, rows * N * A, sample, cores, "port"
+
+
+def bench_config(world):
+    """The `config` object of both arms (identical, so the two lines compare)."""
+    return {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
+                        "slant-stack backprojection, one slice per GPU",
+            "image": N, "views": A, "rays": R, "filter": "ramlak",
+            "l2": "flushed (160 MiB write) before every timed step; step time = sum "
+                  "of per-step CUDA-event intervals",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}
 
 
 # ----------------------------------------------------------------------------
@@ -215,12 +263,15 @@ def make_osem_batch(torch, rg, idx, sizes, seed):
     return sinos
 
 
-def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7, rank=0, world=1):
+def osem_compare(torch, rg, nslices, niter, nsubsets, plain_stride, seed=7, rank=0, world=1,
+                 runs=3):
     """Batched graph-captured OSEM vs the plain one-slice-per-call form on
     the same slices.  With several ranks (one per GPU) the slices are
     partitioned by cost (pyraft_gb300.shard) and the batched time is the max
-    over ranks; the plain form runs on rank 0 only, on its first
-    `plain_slices` slices (all, if None), and is reported per slice."""
+    over ranks (median of `runs` full runs).  The plain form runs on rank 0
+    only, on every `plain_stride`-th of its slices (all of them for stride
+    1), and its time is scaled to the whole batch by the sampled slices'
+    share of sum(N^2 x views)."""
     import numpy as np
     from pyraft_gb300 import _native, shard
     from pyraft_gb300.raftypes import rg_image
@@ -245,7 +296,7 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7, rank
     run_batch(1)                                     # warm-up (plans, graph path)
     torch.cuda.synchronize()
     times = []
-    for _ in range(3):                               # median of three full runs
+    for _ in range(runs):
         if world > 1:
             torch.distributed.barrier()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -260,28 +311,31 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_slices, seed=7, rank
         "slices": nslices, "iterations": niter, "subsets": nsubsets, "n_gpus": world,
         "batched_slices_per_s": round(nslices / t_batch, 3),
         "batched_s": round(t_batch, 3),
+        "batched_runs": runs,
         "batched_gups": round(upd / t_batch / 1e9, 1),
     }
     if rank != 0:
         return res
-    m = ns if plain_slices is None else min(plain_slices, ns)
-    host = [s.cpu().numpy() for s in sinos[:m]]
+    pick = list(range(0, ns, max(1, plain_stride)))
+    host = {k: sinos[k].cpu().numpy() for k in pick}
     out = np.zeros((2048, 2048), dtype=np.float32)
     t0 = time.perf_counter()
-    for k in range(m):
+    for k in pick:
         n, v = sizes[k]
         _native.check(L.rg_em_plain_host(out.ctypes.data, host[k].ctypes.data, n, n, v, niter,
                                          nsubsets))
     t_plain = time.perf_counter() - t0
-    frac = sum(sizes[k][0] ** 2 * sizes[k][1] for k in range(m)) / \
+    frac = sum(sizes[k][0] ** 2 * sizes[k][1] for k in pick) / \
         sum(n * n * v for n, v in sizes_all)
     t_plain_all = t_plain / frac
     res.update({
         "plain_slices_per_s": round(nslices / t_plain_all, 3),
         "plain_s": round(t_plain_all, 3),
-        "plain_timed_slices": m,
-        "plain_note": (f"one GPU, first {m} slices of rank 0 timed, scaled by their share of "
-                       f"N^2*views of the whole batch"),
+        "plain_timed_slices": len(pick),
+        "plain_timed_s": round(t_plain, 3),
+        "plain_note": (f"one GPU, every {max(1, plain_stride)}th slice of rank 0 timed "
+                       f"({len(pick)} slices, {100 * frac:.1f} % of the batch's N^2 x views), "
+                       f"scaled by that share"),
         "speedup_per_gpu": round(t_plain_all / t_batch / world, 2),
     })
     return res
@@ -374,7 +428,12 @@ def main():
                          "(256 slices, 10 subsets x 20 iterations) vs the plain form")
     ap.add_argument("--slices", type=int, default=256)
     ap.add_argument("--iters", type=int, default=20)
-    ap.add_argument("--plain-slices", type=int, default=None)
+    ap.add_argument("--plain-stride", type=int, default=4,
+                    help="the plain per-call form times every k-th slice of the batch")
+    ap.add_argument("--batch-runs", type=int, default=2,
+                    help="timed runs of the whole batched OSEM (median)")
+    ap.add_argument("--no-osem", action="store_true",
+                    help="FBP line without its osem object (quick runs)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warm = max(3, args.warmup)
@@ -401,8 +460,8 @@ def main():
         torch.cuda.set_device(local)
         if world > 1:
             torch.distributed.init_process_group("nccl")
-        res = osem_compare(torch, rg, args.slices, args.iters, 10, args.plain_slices,
-                           rank=rank, world=world)
+        res = osem_compare(torch, rg, args.slices, args.iters, 10, args.plain_stride,
+                           rank=rank, world=world, runs=args.batch_runs)
         if rank == 0:
             print(json.dumps({"workload": "batched uneven OSEM vs plain per-call form",
                               "scaling": "strong (slices partitioned over GPUs by cost)",
@@ -490,9 +549,7 @@ def main():
             bp_ms.append(a.elapsed_time(b))
     bp_ms = statistics.mean(bp_ms)
     compulsory = N * N * 4 + R * A * 4
-    alg_bytes = 8 * UPDATES + compulsory
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (bp_ms * 1e-3) / 1e9
     sms = torch.cuda.get_device_properties(0).multi_processor_count
 
     # ---- the other operators of the path at the same size (one call each)
@@ -620,12 +677,7 @@ def main():
         "steps": args.steps, "warmup": warm, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded random-ellipse transmission sinogram, Poisson I0=1e4)",
-        "config": {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
-                               "slant-stack backprojection, one slice per GPU",
-                   "image": N, "views": A, "rays": R, "filter": "ramlak",
-                   "l2": "flushed (160 MiB write) before every timed step; step time = sum "
-                         "of per-step CUDA-event intervals",
-                   "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+        "config": bench_config(world),
         "e2e": {"value": round(world * UPDATES / (p_ms * 1e-3) / 1e9, 3), "unit": UNIT,
                 "h2d_bytes_per_step": R * A * 4, "d2h_bytes_per_step": N * N * 4,
                 "ms_per_step": round(p_ms, 4), "api": "rg_fbp (C ABI), pinned host buffers",
@@ -638,19 +690,12 @@ def main():
                            "mode": "upload, FBP, download back to back on one stream, "
                                    "per-step CUDA events"},
                 "finite_and_equal": ok},
-        "roofline": {"bound": "hbm",
-                     "kernel": "k_gather_rot_tma<0> (backprojection, views paired a quarter "
+        "roofline": {"kernel": "k_gather_rot_tma<0> (backprojection, views paired a quarter "
                                "turn apart, windows staged by TMA; timed as the call, with its "
                                "k_pair_quads prepass, which also zeroes the output)",
-                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 3), "traffic": BP_TRAFFIC_BYTES,
-                     "algorithmic_bytes": alg_bytes, "kernel_ms": round(bp_ms, 4),
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
-                     "model": "8 B per (pixel, view) update + image and sinogram bytes once",
-                     "note": "frac > 1 because every staged sinogram sample serves ~1000 "
-                             "updates from shared memory, so DRAM carries only the compulsory "
-                             "bytes; the bound is shared-memory bandwidth (smem_ceiling)",
-                     "smem_ceiling": smem_ceiling(UPDATES, bp_ms, sms, clk["sm_mhz"])},
+                     "kernel_ms": round(bp_ms, 4),
+                     **smem_roofline(UPDATES, bp_ms, sms, clk["sm_mhz"], BP_TRAFFIC_BYTES,
+                                     compulsory, peak, peak_kind)},
         "ops": {"radon_gups": round(R * A * N / (radon_ms * 1e-3) / 1e9, 1),
                 "radon_ms": round(radon_ms, 4),
                 "adjoint_gups": round(UPDATES / (adj_ms * 1e-3) / 1e9, 1),
@@ -661,44 +706,62 @@ def main():
         "clocks": clk,
         "wall_s_timed_region": round(wall, 3),
     }
+    if not args.no_osem:
+        # The metric's EM/OSEM half, after the FBP measurements (it does not
+        # touch their timed region).
+        em = em_run(torch, rg)
+        batch = osem_compare(torch, rg, args.slices, args.iters, 10, args.plain_stride,
+                             rank=rank, world=world, runs=args.batch_runs)
+        line["osem"] = {
+            "unit": "slices/s",
+            "em_slice": {"workload": "EM 100 iterations and OSEM 10 subsets x 10 iterations, "
+                                     "1024^2 emission slice, 720 views, 1024 rays, Poisson "
+                                     "counts (mean 50 per bin), x0 = 1, one rg_em call each",
+                         **em},
+            "batch": {"workload": "batched uneven OSEM: 256 slices, N in {256,512,1024,2048}, "
+                                  "views in [180,1800], rays = N, 10 subsets x 20 iterations; "
+                                  "batched = rg_osem_batch (persistent grids, graph-captured "
+                                  "sub-iterations, resident sinograms); plain = rg_em_plain_host "
+                                  "per slice (host buffers, five launches per sub-iteration)",
+                      **batch},
+        }
     if rank == 0:
-        t_cpu, sample, cores, kind = cpu_fbp_sample(h_in.numpy().astype(np.float64), False)
-        line["cpu_baseline"] = {"value": round(UPDATES / t_cpu / 1e9, 4), "unit": UNIT,
+        t_cpu, upd_cpu, sample, cores, kind = cpu_fbp_sample(h_in.numpy().astype(np.float64))
+        line["cpu_baseline"] = {"value": round(upd_cpu / t_cpu / 1e9, 4), "unit": UNIT,
                                 "cores": cores, "kind": kind, "sample": sample,
-                                "est_s_per_step": round(t_cpu, 2)}
+                                "sample_ms": round(1e3 * t_cpu, 1)}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
 
 
 def reference_arm(args, rank, world, warm):
-    """The reference's CPU algorithm on the host cores (compiled reference if
-    present, else the oracle port), same metric and config, bounded sample
-    per step.  Under torchrun only rank 0 works."""
+    """The reference's CPU algorithm on the host cores (the oracle port; the
+    compiled reference does not travel to the GPU machine), same metric and
+    config as the GPU arm.  Each step is one bounded sample: 1/32 of the FBP
+    step spread over the input (cpu_fbp_sample), and the value is the
+    sample's updates over its measured time, so steps x ms_per_step is the
+    arm's real timed region.  Under torchrun only rank 0 works."""
     if rank != 0:
         return
     import numpy as np
-    from oracle import oracle as O
     rng = np.random.default_rng(1234)
     sino = rng.random((R, A))
-    steps, samples = [], []
+    steps, upd = [], 0
     for k in range(warm + args.steps):
-        t, sample, cores, kind = cpu_fbp_sample(sino, True)
+        t, upd, sample, cores, kind = cpu_fbp_sample(sino)
         if k >= warm:
             steps.append(t)
-            samples.append(cpu_fbp_sample.last_sample_s)
     t = statistics.mean(steps)
-    v = UPDATES / t / 1e9
+    v = upd / t / 1e9
     print(json.dumps({
         "metric": METRIC, "value": round(v, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": warm, "ms_per_step": round(t * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic", "impl": "reference",
-        "config": {"workload": "FBP 2048x2048, 1800 views in [0,pi), 2048 rays, Ram-Lak + "
-                               "slant-stack backprojection", "image": N, "views": A, "rays": R},
+        "data": "synthetic (uniform random sinogram of the FBP shape)", "impl": "reference",
+        "config": bench_config(world),
         "cpu_baseline": {"value": round(v, 4), "unit": UNIT, "cores": cores, "kind": kind,
-                         "sample": sample,
-                         "measured_sample_ms_per_step": round(1e3 * statistics.mean(samples), 1)},
+                         "sample": sample},
         "e2e": {"value": round(v, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }), flush=True)

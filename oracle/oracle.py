@@ -38,11 +38,12 @@ class OrcImg(ctypes.Structure):
                 ("br_x", ctypes.c_double), ("br_y", ctypes.c_double)]
 
 
-def build(ref: bool = False) -> None:
-    """Compile the oracle (and, if asked, the reference) with make."""
+def build(ref_src: str | None = None) -> None:
+    """Compile the oracle (and, given the reference's raft/ directory, the
+    reference's own sources) with make."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
+    if ref_src:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF_SRC={ref_src}"], check=True)
 
 
 _lib = None
@@ -114,6 +115,43 @@ def backprojection_rows(sino, size, row0, row1, img_corners=IMG_CORNERS,
                                              ctypes.c_int(row1),
                                              ctypes.c_int(threads or nthreads()))
     return out
+
+
+def backprojection_rowstep(sino, size, row0, step, count, img_corners=IMG_CORNERS,
+                           sino_corners=SINO_CORNERS, threads=None):
+    """Rows row0, row0 + step, ... (count of them) of backprojection_slantstack,
+    returned as a (count, size) array: a sample spread over the image."""
+    assert count >= 1 and step >= 1 and 0 <= row0 and row0 + (count - 1) * step < size
+    sino = np.ascontiguousarray(sino, dtype=np.float64)
+    out = np.zeros((size, size))
+    I, S = _img(out, img_corners), _img(sino, sino_corners)
+    lib().orc_backprojection_slantstack_rowstep(ctypes.byref(S), ctypes.byref(I),
+                                                ctypes.c_int(row0), ctypes.c_int(step),
+                                                ctypes.c_int(count),
+                                                ctypes.c_int(threads or nthreads()))
+    return out[row0:row0 + (count - 1) * step + 1:step].copy()
+
+
+def ramlak_fft(sino, dt):
+    """The discrete Ram-Lak filter of `ramlak` (linear convolution along axis
+    0, q[n] = dt * sum_k h[n-k] p[k]) evaluated the way pyraft filters, by
+    numpy FFT (pyraft/filters/filters.py:13-68 applies its ramp by np.fft
+    along t): the kernel's 2R-1 taps and each view are zero-padded to a
+    power of two M >= 2R-1, multiplied in frequency and cut back to R."""
+    sino = np.asarray(sino, dtype=np.float64)
+    R = sino.shape[0]
+    M = 1 << (2 * R - 2).bit_length()
+    m = np.arange(-(R - 1), R).astype(np.float64)
+    h = np.zeros(2 * R - 1)
+    h[m == 0] = 1.0 / (4.0 * dt * dt)
+    odd = np.abs(m) % 2 == 1
+    h[odd] = -1.0 / (np.pi ** 2 * m[odd] ** 2 * dt * dt)
+    hp = np.zeros(M)
+    hp[:R] = h[R - 1:]                  # lags 0 .. R-1
+    hp[M - (R - 1):] = h[:R - 1]        # lags -(R-1) .. -1, wrapped
+    Hf = np.fft.rfft(hp)
+    Sf = np.fft.rfft(sino, n=M, axis=0)
+    return dt * np.fft.irfft(Sf * Hf[:, None], n=M, axis=0)[:R]
 
 
 def ramlak_views(sino, dt, nv, threads=None):

@@ -280,6 +280,27 @@ void orc_backprojection_slantstack_rows(const orc_img *sino, orc_img *img, int r
     orc_parallel((row1 - row0) * img->lines, nthreads, ss_bp_rows_body, &r);
 }
 
+/* Rows row0, row0 + step, ... (count rows): a sample spread over the whole
+ * image, for CPU timing and for parity checks of full-size GPU results. */
+typedef struct { bp_ctx c; int row0, step; } bp_rowstep_ctx;
+
+static void ss_bp_rowstep_body(void *vctx, int lo, int hi, int worker)
+{
+    bp_rowstep_ctx *r = (bp_rowstep_ctx *)vctx;
+    int size = r->c.img->lines;
+    for (int w = lo; w < hi; ++w) {
+        int idx = (r->row0 + (w / size) * r->step) * size + w % size;
+        ss_bp_body(&r->c, idx, idx + 1, worker);
+    }
+}
+
+void orc_backprojection_slantstack_rowstep(const orc_img *sino, orc_img *img, int row0,
+                                           int step, int count, int nthreads)
+{
+    bp_rowstep_ctx r = {{sino, img}, row0, step};
+    orc_parallel(count * img->lines, nthreads, ss_bp_rowstep_body, &r);
+}
+
 /* ------------------------------------------------------------------------ */
 /* DDA (Bresenham-like) pixel walk.  Restates raft_ddaiterator
  * (raft/raft_ddaiterator.c:16-257, struct raft/raft_ddaiterator.h:10-47):

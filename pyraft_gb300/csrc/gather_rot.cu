@@ -382,6 +382,8 @@ __global__ void k_pair_quads(const float *__restrict__ s_am, int s_ld, long long
 // window wider than wb is skipped with error bit 1; a wait that runs out
 // sets bit 2, waits (bounded) for the CTA's copies still in flight and ends
 // the view loop, and the CTA still takes part in its cluster's reduction.
+// expire_first (a test switch, 0 in normal use) makes the first wait give up
+// at once, so that tests can see that path run and report.
 template <int MODE, int ROWS>
 __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ CUtensorMap tm,
                                                         const View *__restrict__ views, int half,
@@ -389,7 +391,8 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
                                                         float *__restrict__ out, long long cs,
                                                         long long ls, int *__restrict__ err,
                                                         long long zo, int wb,
-                                                        unsigned quad_bytes, int split)
+                                                        unsigned quad_bytes, int split,
+                                                        int expire_first)
 {
     extern __shared__ __align__(128) float4 qbuf[];   // [kStages][kPairSlots][wb]
     __shared__ __align__(8) unsigned long long full[kStages];
@@ -465,7 +468,8 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
         // A wait that runs out is acted on at the chunk's closing barrier:
         // until then the thread sums whatever the buffer holds (its reads
         // stay inside it), and the call reports the error.
-        const bool ok = mbar_wait(smem_addr(&full[b]), (c / kStages) & 1);
+        const bool ok = (expire_first && c == 0) ? false
+                                                 : mbar_wait(smem_addr(&full[b]), (c / kStages) & 1);
         const int nslot = min(kPairSlots, vend - (vbeg + c * kPairSlots));
         for (int s = 0; s < nslot; ++s) {
             const SlotInfo si = slot[b][s];
@@ -548,7 +552,11 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
                                               zero_out ? out : nullptr, N, cs, ls, z.out);
         RG_CK_LAUNCH("k_pair_quads");
     }
-    const int wb = quad_box(w);
+    // RG_TEST_WINDOW_CUT=1 (a test switch) under-reports the window bound by
+    // one step of 8: the box and the buffers shrink with it, and the slots
+    // whose windows no longer fit are skipped with error bit 1.
+    const int wb = quad_box(w) - (test_switch("RG_TEST_WINDOW_CUT") && quad_box(w) > 8 ? 8 : 0);
+    const int expire = test_switch("RG_TEST_EXPIRE_WAIT") ? 1 : 0;
     CUtensorMap tm;
     {
         EncodeTiledFn fn = tensor_map_encoder();
@@ -574,7 +582,7 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const float scale = MODE == 0 ? p.dth : 1.f;
     if (split == 1) {
         k<<<grid, 256, smem, st>>>(tm, p.d_views, half, N, scale, out, cs, ls, d_err, z.out, wb,
-                                   qb, 1);
+                                   qb, 1, expire);
         RG_CK_LAUNCH("k_gather_rot_tma");
         return RG_OK;
     }
@@ -591,7 +599,7 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     cfg.attrs = at;
     cfg.numAttrs = 1;
     RG_CK(cudaLaunchKernelEx(&cfg, k, tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
-                             d_err, z.out, wb, qb, split));
+                             d_err, z.out, wb, qb, split, expire));
     RG_CK_LAUNCH("k_gather_rot_tma (cluster)");
     return RG_OK;
 }

@@ -27,6 +27,8 @@
 // a strip that would not fit is skipped with an error flag, never read out
 // of bounds.  Every mbarrier wait is bounded; a CTA whose wait runs out sets
 // the error flag, waits (bounded) for its own copies and leaves.
+// expire_first (a test switch, 0 in normal use) makes each CTA's first strip
+// wait give up at once, so that tests can see that path run and report.
 #include <cuda.h>
 #include <string.h>
 
@@ -75,7 +77,7 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
                                                    float *__restrict__ out_am, int out_ld,
                                                    const float *__restrict__ y_am, int y_ld,
                                                    long long zo, int *__restrict__ err,
-                                                   unsigned pb)
+                                                   unsigned pb, int expire_first)
 {
     extern __shared__ __align__(128) float2 sbuf[];   // [2][kTmLines][BW]
     __shared__ __align__(8) unsigned long long full[2];
@@ -191,7 +193,8 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
             // buffer b ^ 1 was last read in strip n - 1, which every thread
             // finished before the barrier that closed it
             if (warp == 0 && n + 1 < nstrips) issue(n + 1);
-            const bool ok = mbar_wait(smem_addr(&full[b]), (n >> 1) & 1);
+            const bool ok = (expire_first && n == 0) ? false
+                                                     : mbar_wait(smem_addr(&full[b]), (n >> 1) & 1);
             if (__syncthreads_or(!ok)) {
                 failed = true;
                 break;
@@ -393,7 +396,8 @@ static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensor
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((p.g.R + kTmRays - 1) / kTmRays, p.nblocks, nz);
     k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
-                               out_am, out_ld, y_am, y_ld, zo, d_err, (unsigned)sizeof(float2));
+                               out_am, out_ld, y_am, y_ld, zo, d_err, (unsigned)sizeof(float2),
+                               test_switch("RG_TEST_EXPIRE_WAIT") ? 1 : 0);
     RG_CK_LAUNCH("k_radon_tma");
     return RG_OK;
 }

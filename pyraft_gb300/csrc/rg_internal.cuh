@@ -15,6 +15,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include <initializer_list>
 #include <string>
@@ -51,6 +52,15 @@ enum { kLinesAreRows = 1, kRkNegative = 2 };
 // Host-side helpers (api.cu).
 int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
+// True when environment variable `name` is "1" (read per call).  Used for the
+// failure-path test switches RG_TEST_EXPIRE_WAIT (the first mbarrier wait of
+// every CTA of the TMA kernels gives up at once) and RG_TEST_WINDOW_CUT (the
+// TMA gather under-reports its window bound); neither is set in normal use.
+inline bool test_switch(const char *name)
+{
+    const char *e = getenv(name);
+    return e && e[0] == '1' && e[1] == 0;
+}
 
 #define RG_CK(call)                                                     \
     do {                                                                \

@@ -568,6 +568,9 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                   cudaStream_t st, int rows, Stack z, void *quads)
 {
     if (rows == 0) rows = tuned_rows(p, mode);
+    // the kernels OR their error bits (window checks, bounded waits) into the
+    // device's status word, which rg_device_status() reads and clears
+    if (!d_err) d_err = device_error_word();
     if (mode == 0) {
         if (!em_x && p.rot_ok && gather_rot_enabled())
             return launch_gather_rot(p, 0, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads,
