@@ -12,9 +12,11 @@
 //      epilogue: r = y / (A x), 0 where A x == 0;
 //   3. matched-adjoint gather of r over the subset's views with the update
 //      fused into the epilogue: x <- x * (A^T r) * (1 / A^T 1).  Where the
-//      subset's views pair up a quarter turn apart (gather_rot.cu), the
-//      paired gather writes A^T r to scratch and the update is its own
-//      elementwise pass.
+//      subset's views pair up a quarter turn apart (gather_rot.cu), each
+//      pixel gets two partial sums from two CTAs: they are added into a
+//      zeroed scratch image, and the last CTA to add to a 32 x 32 block
+//      applies the update to it (EmFuse; the edge pixels first, by their own
+//      kernel).  For N not a multiple of 32 the update is its own pass.
 // The sensitivities A_s^T 1 of each subset are accumulated in FP64 once per
 // call and stored as reciprocals (0 where the sensitivity is 0, which also
 // zeroes pixels that no ray of the subset reaches).
@@ -49,11 +51,17 @@ static size_t em_quads_bytes(int R, int A, int S)
     return gather_quads_bytes((A + S - 1) / S, R, 1);
 }
 
+// Block counters of the EM update fused into the paired gathers (EmFuse).
+static size_t em_cnt_bytes(int N)
+{
+    return em_fusable(N) ? (size_t)(N / 32) * (N / 32) * sizeof(int) : 0;
+}
+
 size_t em_ss_ws(int N, int R, int A, int S)
 {
     const size_t sino = (size_t)R * A * sizeof(float), img = (size_t)N * N * sizeof(float);
     return ws_sum({sino, sino, radon_pairs_bytes(N), radon_pairs_bytes(N), img, img * S, img,
-                   em_quads_bytes(R, A, S)});
+                   em_quads_bytes(R, A, S), em_cnt_bytes(N)});
 }
 
 // The DDA EM's recorded walks (freed with the call).  RG_DDA_PLAN=0 walks
@@ -66,6 +74,14 @@ struct DDAPlans {
         for (auto &q : p) dda_plan_free(q);
     }
 };
+
+// RG_EM_UNFUSED=1: the paired gathers write their sums to scratch and the EM
+// update runs as its own pass even where it could be fused (A/B timing).
+bool em_unfused()
+{
+    const char *e = getenv("RG_EM_UNFUSED");
+    return e && !strcmp(e, "1");
+}
 
 bool dda_plans_enabled()
 {
@@ -115,12 +131,23 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
     float2 *prow = (float2 *)s.take(radon_pairs_bytes(N));
     float2 *pcol = (float2 *)s.take(radon_pairs_bytes(N));
     float *inv = (float *)s.take((size_t)N * N * sizeof(float) * S);
-    // gather output of the paired kernels, whose two partial sums per pixel
-    // rule out the fused update: x <- x * g * inv follows as its own pass
+    // Partial sums of the paired gathers (two per pixel).  For N a multiple
+    // of 32 the gathers apply the update themselves (EmFuse: zeroed here
+    // once, left zero by every gather); otherwise x <- x * g * inv follows
+    // as its own pass.
     float *gsum = (float *)s.take((size_t)N * N * sizeof(float));
     const size_t qb = em_quads_bytes(R, A, S);
     void *quads = qb ? s.take(qb) : nullptr;
+    const size_t cb = em_cnt_bytes(N);
+    EmFuse fuse;
+    fuse.gsum = gsum;
+    fuse.cnt = cb ? (int *)s.take(cb) : nullptr;
+    bool any_rot = false;
+    for (int k = 0; k < S; ++k) any_rot = any_rot || plans[k]->rot_ok;
+    const bool fused = any_rot && gather_rot_enabled() && em_fusable(N) && !em_unfused();
     int rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
+    if (!rc && fused) rc = launch_fill(gsum, (size_t)N * N, 0.f, st);
+    if (!rc && fused) RG_CK(cudaMemsetAsync(fuse.cnt, 0, cb, st));
     for (int k = 0; k < S && !rc; ++k) {
         float *ik = inv + (size_t)k * N * N;
         if (bp) {
@@ -134,7 +161,11 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
         for (int k = 0; k < S && !rc; ++k) {
             if ((rc = launch_line_pairs(x, N, 1, N, prow, pcol, st))) break;
             if ((rc = launch_radon(*plans[k], prow, pcol, ratio, R, y_am, R, st))) break;
-            if (plans[k]->rot_ok && gather_rot_enabled()) {
+            if (plans[k]->rot_ok && fused) {
+                rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, nullptr, 0, 0, x,
+                                   inv + (size_t)k * N * N, nullptr, st, 0, Stack(), quads,
+                                   &fuse);
+            } else if (plans[k]->rot_ok && gather_rot_enabled()) {
                 rc = launch_gather(*plans[k], bp ? 0 : 1, ratio, R, gsum, N, 1, nullptr, nullptr,
                                    nullptr, st, 0, Stack(), quads);
                 if (!rc) rc = launch_em_update(x, gsum, inv + (size_t)k * N * N, (size_t)N * N, st);

@@ -186,6 +186,91 @@ __device__ __forceinline__ void rot_finish(const float (&accB)[ROWS], const floa
     }
 }
 
+// The fused EM update (EmFuse), after rot_finish.  The CTA whose tile
+// starts at (row0, col0) added partial sums to the 32 x 32 pixel blocks of
+// its tile (TH / 32 blocks in a column) and of the quarter-turned tile
+// (TH / 32 blocks in a row).  Every block receives partials from `arrivals`
+// CTAs (its tile's and its turned tile's, times the cluster split).  Each
+// CTA counts itself in on each block it added to, after all of its adds
+// (barrier, then a device-scope fence by the counting thread); the CTA that
+// arrives last fences again, resets the counter and applies
+// x <- x * gsum * inv to the block, zeroing gsum there for the next call.
+// The adjoint leaves edge pixels to the caller (k_adjoint_edges).  No
+// thread waits on another CTA.  Every thread of the CTA calls this.
+template <int MODE, int ROWS>
+__device__ __forceinline__ void rot_em_finish(int row0, int col0, int N, float *__restrict__ gsum,
+                                              float *__restrict__ x,
+                                              const float *__restrict__ inv, int *cnt,
+                                              int arrivals)
+{
+    constexpr int NB = kWarps * ROWS / 32;            // blocks per tile column
+    __shared__ int s_fin[2 * NB];
+    __syncthreads();                                  // this CTA's adds are issued
+    const int nb = N / 32;
+    if ((int)threadIdx.x < 2 * NB) {
+        int br, bc;
+        if ((int)threadIdx.x < NB) {                  // the tile's own blocks
+            br = row0 / 32 + (int)threadIdx.x;
+            bc = col0 / 32;
+        } else {                                      // the quarter-turned tile's
+            br = col0 / 32;
+            bc = (N - row0) / 32 - NB + ((int)threadIdx.x - NB);
+        }
+        int fin = -1;
+        if (br >= 0 && br < nb && bc >= 0 && bc < nb) {
+            __threadfence();
+            const int b = br * nb + bc;
+            if (atomicAdd(cnt + b, 1) == arrivals - 1) {
+                __threadfence();
+                cnt[b] = 0;
+                fin = b;
+            }
+        }
+        s_fin[threadIdx.x] = fin;
+    }
+    __syncthreads();
+    // 256 threads = one float4 each of a 32 x 32 block: row t / 8, columns
+    // 4 (t % 8) .. + 3 (rows of a block start on 128 bytes: N % 32 == 0 and
+    // 256-byte aligned buffers).  The loads of the next finished block are
+    // issued before the current one is used.
+    const int er = (int)threadIdx.x >> 3, ec = ((int)threadIdx.x & 7) * 4;
+    auto next = [&](int k) {
+        while (k < 2 * NB && s_fin[k] < 0) ++k;
+        return k;
+    };
+    auto at = [&](int b) { return (size_t)((b / nb) * 32 + er) * N + (b % nb) * 32 + ec; };
+    int k = next(0);
+    float4 g = make_float4(0.f, 0.f, 0.f, 0.f), xv = g, iv = g;
+    if (k < 2 * NB) {
+        const size_t i = at(s_fin[k]);
+        g = __ldcg(reinterpret_cast<const float4 *>(gsum + i));   // the partials' sum, from L2
+        xv = *reinterpret_cast<const float4 *>(x + i);
+        iv = *reinterpret_cast<const float4 *>(inv + i);
+    }
+    while (k < 2 * NB) {
+        const int b = s_fin[k];
+        const float4 cg = g, cx = xv, ci = iv;
+        k = next(k + 1);
+        if (k < 2 * NB) {
+            const size_t i = at(s_fin[k]);
+            g = __ldcg(reinterpret_cast<const float4 *>(gsum + i));
+            xv = *reinterpret_cast<const float4 *>(x + i);
+            iv = *reinterpret_cast<const float4 *>(inv + i);
+        }
+        const int r = (b / nb) * 32 + er, c = (b % nb) * 32 + ec;
+        const size_t i = (size_t)r * N + c;
+        float4 o = make_float4(cx.x * cg.x * ci.x, cx.y * cg.y * ci.y, cx.z * cg.z * ci.z,
+                               cx.w * cg.w * ci.w);
+        if (MODE != 0) {                              // edge pixels keep their value
+            if (r == 0 || r == N - 1) o = cx;
+            if (c == 0) o.x = cx.x;
+            if (c + 3 == N - 1) o.w = cx.w;
+        }
+        *reinterpret_cast<float4 *>(x + i) = o;
+        __stcg(reinterpret_cast<float4 *>(gsum + i), make_float4(0.f, 0.f, 0.f, 0.f));
+    }
+}
+
 // Warp w covers columns 8 (w & 3) .. + 8 and rows 4 ROWS (w >> 2) .. + 4
 // ROWS of the tile; lane l takes column l & 7 and rows l >> 3, + 4, + 8, ...
 // So the 32 lanes of one load read 8 columns x 4 adjacent rows.  A
@@ -201,14 +286,16 @@ __device__ __forceinline__ int rot_rofs()
 // MODE 0: backprojection; MODE 1: matched adjoint (edge pixels left to
 // k_adjoint_edges, as in gather_tile with edge_fixup).  Stages each chunk's
 // quads with loads from the sinogram.
-template <int MODE, int WMAX, int ROWS>
+template <int MODE, int WMAX, int ROWS, bool EMF>
 __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, int s_ld, int R,
                                                 const View *__restrict__ views, int half,
                                                 int roff, int N, float scale,
                                                 float *__restrict__ out, long long cs,
                                                 long long ls, int *__restrict__ err, int tx,
                                                 int ty, float2 *__restrict__ pairs,
-                                                unsigned quad_bytes, int split, int rank)
+                                                unsigned quad_bytes, int split, int rank,
+                                                float *__restrict__ em_x,
+                                                const float *__restrict__ em_inv, int *em_cnt)
 {
     constexpr int TH = kWarps * ROWS;                     // tile height
     __shared__ SlotInfo slot[kPairSlots];
@@ -300,21 +387,27 @@ __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, 
     // the last chunk ended with a barrier: the staging area is free
     rot_finish<MODE, ROWS>(accB, accA, reinterpret_cast<float *>(pairs), split, rank, myrow, col,
                            N, out, cs, ls, scale);
+    if (EMF) rot_em_finish<MODE, ROWS>(row0, col0, N, out, em_x, em_inv, em_cnt, 2 * split);
 }
 
-template <int MODE, int WMAX, int ROWS>
+// EMF: the EM update fused into the epilogue (EmFuse); a separate
+// instantiation, so that the plain gathers keep their registers.
+template <int MODE, int WMAX, int ROWS, bool EMF>
 __global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_am, int s_ld, int R,
                                                     const View *__restrict__ views, int half,
                                                     int roff, int N, float scale,
                                                     float *__restrict__ out,
                                                     long long cs, long long ls,
                                                     int *__restrict__ err, long long zs,
-                                                    long long zo, unsigned quad_bytes, int split)
+                                                    long long zo, unsigned quad_bytes, int split,
+                                                    float *__restrict__ em_x,
+                                                    const float *__restrict__ em_inv, int *em_cnt)
 {
     extern __shared__ __align__(16) float2 pairs[];  // [kPairSlots][WMAX] x {view, partner}
-    gather_tile_rot<MODE, WMAX, ROWS>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
+    gather_tile_rot<MODE, WMAX, ROWS, EMF>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
                                 out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
-                                blockIdx.y, pairs, quad_bytes, split, blockIdx.x % split);
+                                blockIdx.y, pairs, quad_bytes, split, blockIdx.x % split,
+                                em_x, em_inv, em_cnt);
 }
 
 // ---------------------------------------------------------------------------
@@ -384,7 +477,7 @@ __global__ void k_pair_quads(const float *__restrict__ s_am, int s_ld, long long
 // the view loop, and the CTA still takes part in its cluster's reduction.
 // expire_first (a test switch, 0 in normal use) makes the first wait give up
 // at once, so that tests can see that path run and report.
-template <int MODE, int ROWS>
+template <int MODE, int ROWS, bool EMF>
 __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ CUtensorMap tm,
                                                         const View *__restrict__ views, int half,
                                                         int N, float scale,
@@ -392,7 +485,10 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
                                                         long long ls, int *__restrict__ err,
                                                         long long zo, int wb,
                                                         unsigned quad_bytes, int split,
-                                                        int expire_first)
+                                                        int expire_first,
+                                                        float *__restrict__ em_x,
+                                                        const float *__restrict__ em_inv,
+                                                        int *em_cnt)
 {
     extern __shared__ __align__(128) float4 qbuf[];   // [kStages][kPairSlots][wb]
     __shared__ __align__(8) unsigned long long full[kStages];
@@ -495,26 +591,30 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
     }
     rot_finish<MODE, ROWS>(accB, accA, reinterpret_cast<float *>(qbuf), split, rank, myrow, col,
                            N, out, cs, ls, scale);
+    if (EMF) rot_em_finish<MODE, ROWS>(row0, col0, N, out, em_x, em_inv, em_cnt, 2 * split);
 }
 
 template <int MODE, int WMAX, int ROWS>
 int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
-                 long long ls, int *d_err, cudaStream_t st, const Stack &z)
+                 long long ls, int *d_err, cudaStream_t st, const Stack &z, const EmFuse *em)
 {
+    float *ex = em ? em->x : nullptr;
+    const float *ei = em ? em->inv : nullptr;
+    int *ec = em ? em->cnt : nullptr;
     // half: view pairs; roff: sinogram rows between a view and its partner
     const int N = p.g.N, half = p.nv / 2, roff = p.g.A / 2;
     // the staging area, which also holds the cluster reduction's partials
     const size_t smem = std::max((size_t)kPairSlots * WMAX * sizeof(float4),
                                  (size_t)2 * ROWS * 256 * sizeof(float));
     dim3 grid((N + kTile - 1) / kTile, (N + kWarps * ROWS - 1) / (kWarps * ROWS), z.n);
-    auto k = k_gather_rot<MODE, WMAX, ROWS>;
+    auto k = em ? k_gather_rot<MODE, WMAX, ROWS, true> : k_gather_rot<MODE, WMAX, ROWS, false>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
     const unsigned pb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
     if (split == 1) {
         k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, half, roff, N, scale, out, cs, ls,
-                                   d_err, z.in, z.out, pb, 1);
+                                   d_err, z.in, z.out, pb, 1, ex, ei, ec);
         RG_CK_LAUNCH("k_gather_rot");
         return RG_OK;
     }
@@ -531,7 +631,7 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     cfg.attrs = at;
     cfg.numAttrs = 1;
     RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, half, roff, N,
-                             scale, out, cs, ls, d_err, z.in, z.out, pb, split));
+                             scale, out, cs, ls, d_err, z.in, z.out, pb, split, ex, ei, ec));
     RG_CK_LAUNCH("k_gather_rot (cluster)");
     return RG_OK;
 }
@@ -542,8 +642,11 @@ int quad_box(int w) { return (w + 7) & ~7; }
 template <int MODE, int ROWS>
 int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                    long long ls, int *d_err, cudaStream_t st, const Stack &z, float4 *quads,
-                   int w, bool zero_out)
+                   int w, bool zero_out, const EmFuse *em)
 {
+    float *ex = em ? em->x : nullptr;
+    const float *ei = em ? em->inv : nullptr;
+    int *ec = em ? em->cnt : nullptr;
     const int N = p.g.N, R = p.g.R, half = p.nv / 2, roff = p.g.A / 2;
     const int Rq = quad_entries(MODE, R);
     {
@@ -571,7 +674,7 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
         if (r != CUDA_SUCCESS)
             return set_error(RG_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
     }
-    auto k = k_gather_rot_tma<MODE, ROWS>;
+    auto k = em ? k_gather_rot_tma<MODE, ROWS, true> : k_gather_rot_tma<MODE, ROWS, false>;
     // two buffers of 16 windows, which also hold the cluster reduction's partials
     const size_t smem = std::max((size_t)kStages * kPairSlots * wb * sizeof(float4),
                                  (size_t)2 * ROWS * 256 * sizeof(float));
@@ -582,7 +685,7 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const float scale = MODE == 0 ? p.dth : 1.f;
     if (split == 1) {
         k<<<grid, 256, smem, st>>>(tm, p.d_views, half, N, scale, out, cs, ls, d_err, z.out, wb,
-                                   qb, 1, expire);
+                                   qb, 1, expire, ex, ei, ec);
         RG_CK_LAUNCH("k_gather_rot_tma");
         return RG_OK;
     }
@@ -599,7 +702,7 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     cfg.attrs = at;
     cfg.numAttrs = 1;
     RG_CK(cudaLaunchKernelEx(&cfg, k, tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
-                             d_err, z.out, wb, qb, split, expire));
+                             d_err, z.out, wb, qb, split, expire, ex, ei, ec));
     RG_CK_LAUNCH("k_gather_rot_tma (cluster)");
     return RG_OK;
 }
@@ -617,19 +720,19 @@ bool gather_rot_use_tma(int pairs)
 template <int MODE, int ROWS>
 int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                     long long ls, int *d_err, cudaStream_t st, const Stack &z, void *quads,
-                    bool zero_out)
+                    bool zero_out, const EmFuse *em)
 {
     const int t = ROWS == 16 ? 2 : ROWS == 8 ? 1 : 0;
     const int w = MODE == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
     if (quads && quad_box(w) <= kQuadBox && p.nv / 2 <= 65535 && gather_rot_use_tma(p.nv / 2))
         return gather_rot_tma<MODE, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z,
-                                          (float4 *)quads, w, zero_out);
+                                          (float4 *)quads, w, zero_out, em);
     if (zero_out)
         if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
-    if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-    if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-    if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
-    if (w <= 512) return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z);
+    if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
+    if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
+    if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
+    if (w <= 512) return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
     return set_error(RG_EUNSUPPORTED,
                      "gather window of %d samples per tile exceeds 512 "
                      "(image much coarser than the ray spacing)", w);
@@ -655,17 +758,21 @@ size_t gather_quads_bytes(int nv, int R, int nz)
 
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z, void *quads, bool zero_out)
+                      const Stack &z, void *quads, bool zero_out, const EmFuse *em)
 {
     const bool zo = zero_out;
+    if (em && (!em_fusable(p.g.N) || z.n != 1 || out != em->gsum || cs != p.g.N || ls != 1 ||
+               zero_out))
+        return set_error(RG_EINVAL, "fused EM gather: one N x N slice, N a multiple of 32, "
+                                    "into its own zeroed partial-sum buffer");
     if (mode == 0) {
-        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
-        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
-        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
+        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
+        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
+        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
     }
-    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
-    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
-    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo);
+    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
+    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
+    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
 }
 
 }  // namespace rg

@@ -196,6 +196,21 @@ struct Stack {
     int n = 1;
     long long in = 0, out = 0;
 };
+// The EM update fused into the paired gathers (launch_gather_rot with `em`):
+// each pixel's two partial sums are added into gsum (N x N contiguous, zero
+// on entry and left zero on exit), and the last of the CTAs that add to a
+// 32 x 32 block of pixels (cnt: one counter per block, zero on entry and
+// left zero) applies x <- x * gsum * inv to the block's pixels -- the
+// adjoint's interior pixels, whose edge pixels the caller updates -- and
+// zeroes the block's gsum.  Needs N % 32 == 0 (blocks map onto blocks under
+// the quarter turn).
+struct EmFuse {
+    float *x = nullptr;
+    const float *inv = nullptr;
+    float *gsum = nullptr;
+    int *cnt = nullptr;
+};
+inline bool em_fusable(int N) { return N >= 32 && N % 32 == 0; }
 // rows: rows per thread (4, 8 or 16; 0 = the tuned choice for this geometry).
 // quads: device scratch of gather_quads_bytes(p.nv, p.g.R, z.n) bytes
 // (16-byte aligned) through which the paired path (p.rot_ok, modes 0 and 1)
@@ -203,7 +218,8 @@ struct Stack {
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
                   float *out, long long cs, long long ls,
                   float *em_x, const float *inv_sens, int *d_err, cudaStream_t st,
-                  int rows = 0, Stack z = Stack(), void *quads = nullptr);
+                  int rows = 0, Stack z = Stack(), void *quads = nullptr,
+                  const EmFuse *fuse = nullptr);
 // Bytes of the paired gathers' quad scratch for nz problems of nv views over
 // R rays: a 16-byte quad per (view pair, sample entry), R + 1 entries.
 size_t gather_quads_bytes(int nv, int R, int nz);
@@ -216,10 +232,11 @@ int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, c
 // edge pixels are left to the caller) with views paired a quarter turn
 // apart (p.rot_ok).  Two partial sums are added to each pixel of an output
 // that is zeroed first: by this call when zero_out (in the quad prepass
-// where it runs), else by the caller.
+// where it runs), else by the caller.  With `em` (one slice, out = em->gsum,
+// N x N contiguous) the EM update is fused as described at EmFuse.
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z, void *quads, bool zero_out);
+                      const Stack &z, void *quads, bool zero_out, const EmFuse *em = nullptr);
 // Whether launch_gather takes the paired path where a plan allows it
 // (RG_GATHER_ROT=0 turns it off).
 bool gather_rot_enabled();

@@ -565,16 +565,29 @@ bool gather_rot_enabled()
 
 int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                   long long cs, long long ls, float *em_x, const float *inv_sens, int *d_err,
-                  cudaStream_t st, int rows, Stack z, void *quads)
+                  cudaStream_t st, int rows, Stack z, void *quads, const EmFuse *fuse)
 {
     if (rows == 0) rows = tuned_rows(p, mode);
     // the kernels OR their error bits (window checks, bounded waits) into the
     // device's status word, which rg_device_status() reads and clears
     if (!d_err) d_err = device_error_word();
+    // EM update fused into the paired gathers (EmFuse): the adjoint's edge
+    // pixels are updated first by their own kernel, the rest by the gather
+    EmFuse ef;
+    const bool fused = em_x && fuse && mode != 2 && p.rot_ok && gather_rot_enabled() &&
+                       em_fusable(p.g.N) && z.n == 1;
+    if (fused) {
+        ef = *fuse;
+        ef.x = em_x;
+        ef.inv = inv_sens;
+    }
     if (mode == 0) {
         if (!em_x && p.rot_ok && gather_rot_enabled())
             return launch_gather_rot(p, 0, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads,
                                      true);
+        if (fused)
+            return launch_gather_rot(p, 0, s_am, s_ld, ef.gsum, p.g.N, 1, d_err, st, rows, z,
+                                     quads, false, &ef);
         if (em_x)
             return gather_rows<0, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
         return gather_rows<0, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
@@ -590,6 +603,12 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                 return rc;
             return launch_gather_rot(p, 1, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads,
                                      false);
+        }
+        if (fused) {
+            if (int rc = adjoint_edges<1, true>(p, s_am, s_ld, nullptr, 0, 0, em_x, inv_sens, st, z))
+                return rc;
+            return launch_gather_rot(p, 1, s_am, s_ld, ef.gsum, p.g.N, 1, d_err, st, rows, z,
+                                     quads, false, &ef);
         }
         if (em_x)
             return gather_rows<1, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);

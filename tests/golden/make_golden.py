@@ -34,6 +34,49 @@ DDA_RAYS = [(th, t) for th in (0.0, 1e-3, 0.3, math.pi / 4, 1.0, math.pi / 2,
             for t in (-1.0, -0.73, -0.25, 0.0, 0.31, 0.999, 1.0)]
 
 
+# Read-only checkout of the reference (pyraft v0.0.8); PYRAFT_REFERENCE
+# overrides the default location.
+REFERENCE = os.environ.get("PYRAFT_REFERENCE", "/root/reference")
+
+
+def reference_lowpassino_fbp():
+    """The reference's own pyraft.filters.filters.lowpassino_fbp, loaded from
+    its source file.  Its package imports the compiled libraft and pynfft,
+    which cannot load here, so the two modules it star-imports are stubbed:
+    ringfun (unused by this function) is empty, and raftypes provides only
+    `image`, an ndarray subclass that carries top_left / bottom_right like
+    pyraft's (pyraft/raftypes.py:254-358)."""
+    import importlib.util
+    import types
+
+    class image(np.ndarray):
+        def __new__(cls, a, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0)):
+            obj = np.asarray(a, dtype=np.float64).view(cls)
+            obj.top_left, obj.bottom_right = top_left, bottom_right
+            return obj
+
+        def __array_finalize__(self, obj):
+            self.top_left = getattr(obj, "top_left", (0.0, 1.0))
+            self.bottom_right = getattr(obj, "bottom_right", (math.pi, -1.0))
+
+    pkg = types.ModuleType("pyraft_ref")
+    pkg.__path__ = []
+    sub = types.ModuleType("pyraft_ref.filters")
+    sub.__path__ = []
+    raftypes = types.ModuleType("pyraft_ref.raftypes")
+    raftypes.image = image
+    raftypes.__all__ = ["image"]
+    ringfun = types.ModuleType("pyraft_ref.filters.ringfun")
+    ringfun.__all__ = []
+    for m in (pkg, sub, raftypes, ringfun):
+        sys.modules[m.__name__] = m
+    path = os.path.join(REFERENCE, "pyraft", "filters", "filters.py")
+    spec = importlib.util.spec_from_file_location("pyraft_ref.filters.filters", path)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.lowpassino_fbp, image
+
+
 def main() -> None:
     if not R.available():
         raise SystemExit("oracle/_ref/libraft_ref.so missing: run `make -C oracle ref REF_SRC=<checkout>/raft`")
@@ -108,6 +151,21 @@ def main() -> None:
     out["dda"] = dict(i=np.concatenate(ii), j=np.concatenate(jj),
                       sigma=np.concatenate(ss), offsets=np.array(off),
                       rays=np.array(meta), shape=np.array([32, 40]))
+
+    # pyraft's FBP filter, run from the reference's own Python source.
+    lowpass, ref_image = reference_lowpassino_fbp()
+    cases = {}
+    for k, (r, v, tl, br) in enumerate([(64, 48, (0.0, 1.0), (math.pi, -1.0)),
+                                        (97, 13, (0.0, 1.0), (math.pi, -1.0)),
+                                        (256, 5, (0.2, 1.3), (2.9, -0.7)),
+                                        (33, 7, (0.0, 0.5), (math.pi, -1.5))]):
+        s_lp = rng.random((r, v))
+        got = lowpass(ref_image(s_lp, tl, br))
+        cases[f"sino{k}"] = s_lp
+        cases[f"corners{k}"] = np.array([tl[0], tl[1], br[0], br[1]])
+        cases[f"out{k}"] = np.asarray(got, dtype=np.float64)
+    cases["count"] = np.array(4)
+    out["lowpass"] = cases
 
     for name, arrays in out.items():
         path = os.path.join(HERE, f"{name}.npz")

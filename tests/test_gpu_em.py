@@ -128,8 +128,9 @@ def test_em_reference_backprojector_vs_oracle(orc):
 @pytest.mark.parametrize("S", [1, 3, 4, 5])
 def test_em_quarter_turn_pairs_match_one_view_kernels(orc, monkeypatch, S):
     """EM and OSEM whose subsets pair up a quarter turn apart (S divides A/2
-    = 30: S = 1, 3, 5) take the paired gathers with a separate update pass;
-    S = 4 keeps the fused one-view gather.  Either way the result matches
+    = 30: S = 1, 3, 5) take the paired gathers with the update fused into
+    their epilogue (N = 64 is a multiple of 32); S = 4 keeps the fused
+    one-view gather.  Either way the result matches
     the one-view kernels (RG_GATHER_ROT=0) to FP32 rounding, for the matched
     adjoint and for the backprojection (reference=True)."""
     n, r, a = 64, 64, 60
@@ -160,3 +161,29 @@ def test_em_dda_recorded_walks_match_walking(orc, monkeypatch, S):
     monkeypatch.setenv("RG_DDA_PLAN_MAX_GB", "0")
     capped = rg.osem(s, (n, n), 6, S, method=BRES)
     assert rel(planned, walked) <= 1e-5 and rel(capped, walked) <= 1e-6
+
+
+@pytest.mark.parametrize("n,a,S,tma", [(128, 600, 1, None), (128, 600, 3, None),
+                                       (96, 60, 1, "0"), (64, 60, 5, "0"), (64, 48, 3, "1"),
+                                       (130, 64, 1, None)])
+def test_em_fused_update_matches_separate_pass(orc, monkeypatch, n, a, S, tma):
+    """The EM update fused into the paired gathers (the last CTA to add its
+    partial sum to a 32 x 32 pixel block updates the block) against the
+    same gathers writing their sums to scratch with the update as its own
+    pass (RG_EM_UNFUSED=1): both compute x * (a + b) * inv from two
+    partial sums added onto zero, so a full-plan EM agrees exactly; OSEM
+    subsets take the tile-driven Radon, whose atomic ray sums round in a
+    varying order, so they agree to 1e-5.  Checked for the matched adjoint
+    and for the backprojection (reference=True), staged by TMA and by loads.
+    N = 130 is not a multiple of 32 and keeps the separate pass."""
+    if tma is not None:
+        monkeypatch.setenv("RG_GATHER_ROT_TMA", tma)
+    y = _emission(orc, n, n, a, 40 + S)
+    s = rg.image(y, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
+    fused = [np.asarray(rg.osem(s, (n, n), 3, S)),
+             np.asarray(rg.osem(s, (n, n), 3, S, reference=True))]
+    monkeypatch.setenv("RG_EM_UNFUSED", "1")
+    sep = [np.asarray(rg.osem(s, (n, n), 3, S)),
+           np.asarray(rg.osem(s, (n, n), 3, S, reference=True))]
+    for f, q in zip(fused, sep):
+        assert rel(f, q) <= (1e-6 if S == 1 else 1e-5)

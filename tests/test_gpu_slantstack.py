@@ -246,6 +246,22 @@ def test_lowpass_vs_numpy_fft(orc, monkeypatch, path):
         assert rel(out, orc.lowpassino_fbp(s)) <= 1e-5
 
 
+@pytest.mark.parametrize("path", ["fft", "direct"])
+def test_lowpass_vs_reference_fixture(golden, monkeypatch, path):
+    """pyraft's filter on the GPU against the reference's own lowpassino_fbp
+    (pyraft/filters/filters.py:13-68, run from its source into
+    tests/golden/lowpass.npz), including shifted sinogram corners.  Ray
+    counts that are powers of two take the FFT kernel, the others the
+    direct one (both with RG_FILTER_KERNEL=direct)."""
+    if path == "direct":
+        monkeypatch.setenv("RG_FILTER_KERNEL", "direct")
+    g = golden("lowpass")
+    for k in range(int(g["count"])):
+        s, c, want = g[f"sino{k}"], g[f"corners{k}"], g[f"out{k}"]
+        out = rg.lowpassino_fbp(sino_img(s, (c[0], c[1]), (c[2], c[3])))
+        assert rel(out, want) <= 1e-5, k
+
+
 def test_fbp_disk_density(orc):
     """Ram-Lak FBP recovers the density of a uniform disk.  pyraft's
     lowpassino_fbp filter is reproduced as is: its frequency grid

@@ -93,6 +93,19 @@ def test_analytic_radon_convergence(orc):
     assert errs[0] > errs[1] > errs[2] and errs[2] < 0.03, errs
 
 
+def test_lowpass_matches_reference_fixture(orc, golden):
+    """The oracle's lowpassino_fbp and its spatial-tap form against the
+    reference's own pyraft/filters/filters.py:13-68, run from its source
+    (tests/golden/make_golden.py), on default and shifted corners."""
+    g = golden("lowpass")
+    for k in range(int(g["count"])):
+        s, c, want = g[f"sino{k}"], tuple(g[f"corners{k}"]), g[f"out{k}"]
+        np.testing.assert_allclose(orc.lowpassino_fbp(s, c), want, rtol=0, atol=1e-12)
+        taps = orc.lowpass_taps(s.shape[0], c)
+        np.testing.assert_allclose(orc.circular_filter(s, taps), want, rtol=0,
+                                   atol=1e-10 * np.abs(want).max())
+
+
 def test_lowpass_taps_match_fft_filter(orc):
     rng = np.random.default_rng(5)
     s = rng.random((33, 7))
