@@ -246,6 +246,18 @@ size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets);
 int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets,
           void *workspace, size_t workspace_bytes, void *stream);
 
+/* The same EM/OSEM loop over a range of sub-iterations, for checkpointing
+ * and resuming a long reconstruction (the reference keeps no loop state;
+ * its iterates are only pickled, pyraft/raftypes.py:369-390): runs
+ * sub-iterations first .. first + count - 1 from the iterate in image,
+ * where sub-iteration j uses subset j mod nsubsets (rg_em runs 0 ..
+ * niter * nsubsets - 1).  Splitting a run into ranges gives the same
+ * iterate as one call, up to the rounding order of the tile-driven Radon's
+ * atomic ray sums (OSEM subsets).  Workspace: rg_em_workspace.             */
+int rg_em_subiterations(rg_image sino, rg_image image, int method, int nsubsets,
+                        long long first, long long count, void *workspace,
+                        size_t workspace_bytes, void *stream);
+
 /* Transmission EM: x <- x * A^T(b exp(-A x)) / A^T y with
  * y = max(rawsino - dark, 0), b = max(flat - dark, 0) (dark.data may be
  * NULL: no dark field); slant-stack Radon with the exp fused into its

@@ -11,8 +11,8 @@ from .sinogram import (radon, radon_3d_stack, radon_gpu, radon_method, radon_vie
 from .backprojection import backprojection, backprojection_gpu, backprojection_plan, radon_transpose
 from .filters import lowpassino_fbp, ramlak
 from .inversion import fbp, fbp_gpu
-from .iterative import (em, em_gpu, em_plain, em_transmission_gpu, make_em, osem,
-                        osem_batch)
+from .iterative import (em, em_checkpointed, em_gpu, em_plain, em_transmission_gpu, make_em,
+                        osem, osem_batch)
 from .phantom import random_ellipses, shepplogan, phantom_fromdesc
 
 __version__ = "0.1.0"

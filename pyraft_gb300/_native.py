@@ -98,6 +98,7 @@ _SIGS = {
     "rg_fbp": ([_IMG, _IMG, _c_int, _vp, _size_t, _vp], _c_int),
     "rg_em_workspace": ([_IMG, _IMG, _c_int, _c_int], _size_t),
     "rg_em": ([_IMG, _IMG, _c_int, _c_int, _c_int, _vp, _size_t, _vp], _c_int),
+    "rg_em_subiterations": ([_IMG, _IMG, _c_int, _c_int, _ll, _ll, _vp, _size_t, _vp], _c_int),
     "rg_osem_batch_workspace": ([_PI, _PI, _c_int, _c_int], _size_t),
     "rg_osem_batch": ([_PI, _PI, _c_int, _c_int, _c_int, _c_int, _vp, _size_t, _vp], _c_int),
     "rg_em_plain_host": ([_vp, _vp, _c_int, _c_int, _c_int, _c_int, _c_int], _c_int),

@@ -113,8 +113,10 @@ size_t em_dda_ws(int L, int C, int R, int A, int S)
 // raft_em_gpu's pairing) instead of the matched adjoint; its sensitivity
 // B 1 is the FP32-compensated backprojection of ones (the dth scale of B
 // cancels between B r and B 1).
-static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, float *x,
-                      Scratch &s, cudaStream_t st, bool bp = false)
+// Runs sub-iterations first .. first + count - 1; sub-iteration j uses
+// subset j mod S (rg_em: first 0, count niter * S).
+static int em_ss_core(const SSGeom &g, long long first, long long count, int S,
+                      const float *y_am, float *x, Scratch &s, cudaStream_t st, bool bp = false)
 {
     const int N = g.N, R = g.R, A = g.A;
     Holders hold;
@@ -157,8 +159,8 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
             rc = launch_gather(*plans[k], 2, ratio, R, ik, N, 1, nullptr, nullptr, nullptr, st);
         }
     }
-    for (int it = 0; it < niter && !rc; ++it)
-        for (int k = 0; k < S && !rc; ++k) {
+    for (long long j = first; j < first + count && !rc; ++j) {
+            const int k = (int)(j % S);
             if ((rc = launch_line_pairs(x, N, 1, N, prow, pcol, st))) break;
             if ((rc = launch_radon(*plans[k], prow, pcol, ratio, R, y_am, R, st))) break;
             if (plans[k]->rot_ok && fused) {
@@ -177,8 +179,8 @@ static int em_ss_core(const SSGeom &g, int niter, int S, const float *y_am, floa
     return rc;
 }
 
-static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S, void *ws,
-                  size_t wsb, cudaStream_t st)
+static int em_dda(const rg_image &sino, const rg_image &image, long long first, long long count,
+                  int S, void *ws, size_t wsb, cudaStream_t st)
 {
     DDAGeom g;
     g.lines = image.lines; g.columns = image.columns;
@@ -217,9 +219,15 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
         const cudaError_t ce = cudaStreamIsCapturing(st, &cap);
         if (ce != cudaSuccess) rc = cuda_error(ce, "rg_em");
     }
-    if (!rc && niter >= 2 && dda_plans_enabled() && cap == cudaStreamCaptureStatusNone)
+    // (a subset's walks are recorded when the range runs it at least twice)
+    auto uses = [&](int k) {
+        const long long r = ((k - first) % S + S) % S;    // first j >= first with j % S == k
+        return r < count ? (count - r - 1) / S + 1 : 0;
+    };
+    if (!rc && dda_plans_enabled() && cap == cudaStreamCaptureStatusNone)
         for (int k = 0; k < S && !rc; ++k)
-            rc = dda_plan_build(g, cs, k, S, dda_plan_max_bytes(), plans.p[k], st);
+            if (uses(k) >= 2)
+                rc = dda_plan_build(g, cs, k, S, dda_plan_max_bytes(), plans.p[k], st);
     // bp must be zero on entry to transpose_k
     auto radon_k = [&](int k) {
         if (!plans.p[k].steps) return launch_bres_radon(g, cs, x, C, 1, ratio, 1, R, y, k, S, st);
@@ -237,8 +245,8 @@ static int em_dda(const rg_image &sino, const rg_image &image, int niter, int S,
         if ((rc = transpose_k(k))) break;
         rc = launch_invert(bp, inv + (size_t)k * npix, npix, st);
     }
-    for (int it = 0; it < niter && !rc; ++it)
-        for (int k = 0; k < S && !rc; ++k) {
+    for (long long j = first; j < first + count && !rc; ++j) {
+            const int k = (int)(j % S);
             if ((rc = radon_k(k))) break;
             if ((rc = launch_fill(bp, npix, 0.f, st))) break;
             if ((rc = transpose_k(k))) break;
@@ -333,16 +341,15 @@ size_t rg_em_workspace(rg_image sino, rg_image image, int method, int nsubsets)
     return em_ss_ws(image.lines, sino.lines, sino.columns, S);
 }
 
-int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, void *ws,
-          size_t wsb, void *stream)
+static int em_range(rg_image sino, rg_image image, int method, int nsubsets, long long first,
+                    long long count, void *ws, size_t wsb, void *stream)
 {
     if (!sino.data || !image.data) return set_error(RG_EINVAL, "rg_em: null data pointer");
-    if (niter < 0) return set_error(RG_EINVAL, "rg_em: niter < 0");
     if (int rc0 = check_ws(ws)) return rc0;
     if (nsubsets < 1 || nsubsets > sino.columns)
         return set_error(RG_EINVAL, "rg_em: nsubsets must be in [1, nviews]");
     cudaStream_t st = (cudaStream_t)stream;
-    if (method == RG_BRESENHAM) return em_dda(sino, image, niter, nsubsets, ws, wsb, st);
+    if (method == RG_BRESENHAM) return em_dda(sino, image, first, count, nsubsets, ws, wsb, st);
     if (method != RG_SLANTSTACK && method != RG_SLANTSTACK_BP)
         return set_error(RG_EINVAL, "rg_em: unknown method %d", method);
     if (image.lines != image.columns || image.lines < 2 || sino.lines < 2)
@@ -360,10 +367,26 @@ int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, vo
     float *x = (float *)s.take((size_t)N * N * sizeof(float));
     rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, y, st);
     if (!rc) rc = launch_copy2d(image.data, image.column_stride, image.line_stride, x, N, 1, N, N, st);
-    if (!rc) rc = em_ss_core(g, niter, nsubsets, y, x, s, st, method == RG_SLANTSTACK_BP);
+    if (!rc) rc = em_ss_core(g, first, count, nsubsets, y, x, s, st, method == RG_SLANTSTACK_BP);
     if (!rc) rc = launch_copy2d(x, N, 1, image.data, image.column_stride, image.line_stride, N, N, st);
     scratch_end(s);
     return rc;
+}
+
+int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, void *ws,
+          size_t wsb, void *stream)
+{
+    if (niter < 0) return set_error(RG_EINVAL, "rg_em: niter < 0");
+    const long long S = nsubsets < 1 ? 1 : nsubsets;
+    return em_range(sino, image, method, nsubsets, 0, (long long)niter * S, ws, wsb, stream);
+}
+
+int rg_em_subiterations(rg_image sino, rg_image image, int method, int nsubsets, long long first,
+                        long long count, void *ws, size_t wsb, void *stream)
+{
+    if (first < 0 || count < 0)
+        return set_error(RG_EINVAL, "rg_em_subiterations: first and count must be >= 0");
+    return em_range(sino, image, method, nsubsets, first, count, ws, wsb, stream);
 }
 
 }  // extern "C"

@@ -108,6 +108,95 @@ def osem(sino, shape=None, niter=5, nblocks=4, method=radon_method.SLANTSTACK, r
     return _finish_em(x, host, shost)
 
 
+_STATE_KEYS = ("niter", "nsubsets", "method", "shape", "image_corners", "sinogram")
+
+
+def _state_mismatch(state, params):
+    """Name of the first run parameter in which a saved state differs from
+    this call's (None when they all match)."""
+    for k in _STATE_KEYS:
+        a, b = state.get(k), params.get(k)
+        if isinstance(a, (list, tuple)) and isinstance(b, (list, tuple)):
+            if len(a) != len(b) or any(abs(float(u) - float(v)) > 1e-12 * max(1.0, abs(float(v)))
+                                       for u, v in zip(a, b)):
+                return k
+        elif a != b:
+            return k
+    return None
+
+
+def _sinogram_fingerprint(gs):
+    """Shape, corners, and the FP64 sum and sum of squares of a device
+    sinogram: enough to tell a resumed run that it was given other data."""
+    import torch
+    d = gs.data.to(torch.float64)
+    return [float(gs.shape[0]), float(gs.shape[1]), *map(float, gs.top_left),
+            *map(float, gs.bottom_right), float(d.sum()), float((d * d).sum())]
+
+
+def em_checkpointed(sino, shape=None, niter=5, nsubsets=1, method=radon_method.SLANTSTACK,
+                    reference=False, checkpoint=None, every=1, max_subiterations=None,
+                    **kwargs):
+    """EM (nsubsets = 1) or OSEM over interleaved subsets that can be stopped
+    and resumed at any sub-iteration.
+
+    After every `every` sub-iterations the state -- the iterate, the number
+    of sub-iterations done and the run's parameters (niter, nsubsets,
+    method, shape, image corners and a fingerprint of the sinogram) -- is
+    written to `checkpoint` with torch.save (to a temporary file first, then
+    renamed, so an interrupted write leaves the previous state).  A call
+    that finds `checkpoint` continues from it; a state saved for other
+    parameters or another sinogram raises ValueError.  max_subiterations
+    stops this call after that many sub-iterations (the run resumes on the
+    next call).  Each call runs its sub-iterations through
+    rg_em_subiterations, so a run split over calls reaches the iterate of an
+    uninterrupted rg_em call (OSEM subsets up to the rounding order of the
+    tile-driven Radon's atomic ray sums).
+
+    Returns (x, state): x as em/osem return it, state the dict saved last
+    (with "done" True once all niter * nsubsets sub-iterations have run)."""
+    import os
+    import torch
+    if checkpoint is None:
+        raise TypeError('em_checkpointed needs a checkpoint path')
+    if every < 1:
+        raise ValueError('every must be >= 1')
+    if shape is None:
+        shape = [sino.shape[0], sino.shape[0]]
+    m = _method(method, method, reference)
+    gs, shost = to_gpu(sino, (0.0, 1.0), (numpy.pi, -1.0))
+    x, host = _start(shape, kwargs)
+    params = {"niter": int(niter), "nsubsets": int(nsubsets), "method": int(m),
+              "shape": [int(v) for v in x.shape], "image_corners": [*x.top_left, *x.bottom_right],
+              "sinogram": _sinogram_fingerprint(gs)}
+    total = int(niter) * int(nsubsets)
+    done = 0
+    if os.path.exists(checkpoint):
+        state = torch.load(checkpoint, map_location="cpu", weights_only=True)
+        bad = _state_mismatch(state, params)
+        if bad is not None:
+            raise ValueError(f'checkpoint {checkpoint} was saved for another run ({bad} differs)')
+        x.data.copy_(state["x"].to(x.data.device))
+        done = int(state["subiteration"])
+    L = _native.load()
+    a, b = rg_image(gs), rg_image(x)
+    ws_t, ws = workspace(L.rg_em_workspace(a, b, m, int(nsubsets)))
+    wsb = ws_t.numel() if ws_t is not None else 0
+    budget = total - done if max_subiterations is None else min(total - done, max_subiterations)
+    state = dict(params, subiteration=done, done=done >= total, x=x.data.cpu())
+    while budget > 0:
+        c = min(every, budget)
+        _native.check(L.rg_em_subiterations(a, b, m, int(nsubsets), done, c, ws, wsb,
+                                            stream_ptr()))
+        done += c
+        budget -= c
+        state = dict(params, subiteration=done, done=done >= total, x=x.data.cpu())
+        tmp = f"{checkpoint}.tmp"
+        torch.save(state, tmp)
+        os.replace(tmp, checkpoint)
+    return _finish_em(x, host, shost), state
+
+
 def em_gpu(*args):
     """pyraft's em_gpu(s, img_size=rays, niter=20): host sinogram on the
     default geometry -> (img_size, img_size) float32 array, with the
