@@ -198,10 +198,11 @@ __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restri
         const BatchSlice &b = d[find_slice(d, n, item, kGather)];
         const int local = item - b.begin[kGather], tiles = (b.N + 31) / 32;
         if (MODE == 1)
-            gather_tile<1, WMAX, kBatchRows, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
-                                                   nullptr, 0, 0, b.x, b.inv_sens, nullptr,
-                                                   local % tiles, local / tiles, pairs,
-                                                   pair_bytes, 1, 0, true);
+            gather_tile<1, WMAX, kBatchRows, true, false>(b.ratio_am, b.R, b.R, b.views, b.nv,
+                                                          b.N, 1.f, nullptr, 0, 0, b.x,
+                                                          b.inv_sens, nullptr, local % tiles,
+                                                          local / tiles, pairs, pair_bytes, 1,
+                                                          0, true);
         else
             gather_tile<2, WMAX, kBatchRows, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, 1.f,
                                                     b.inv_sens, b.N, 1, nullptr, nullptr, nullptr,
@@ -349,6 +350,7 @@ int dispatch_iteration(const BatchRun &br, cudaStream_t st)
     switch (br.wmax) {
     case 64: return enqueue_iteration<64>(br, st);
     case 128: return enqueue_iteration<128>(br, st);
+    case 160: return enqueue_iteration<160>(br, st);
     case 256: return enqueue_iteration<256>(br, st);
     default: return enqueue_iteration<512>(br, st);
     }
@@ -359,6 +361,7 @@ int dispatch_sensitivity(const BatchRun &br, cudaStream_t st)
     switch (br.wmax) {
     case 64: return enqueue_sensitivity<64>(br, st);
     case 128: return enqueue_sensitivity<128>(br, st);
+    case 160: return enqueue_sensitivity<160>(br, st);
     case 256: return enqueue_sensitivity<256>(br, st);
     default: return enqueue_sensitivity<512>(br, st);
     }
@@ -369,6 +372,7 @@ int dispatch_attrs(BatchRun &br)
     switch (br.wmax) {
     case 64: { int rc = set_smem_attrs<64>(); return rc ? rc : prepare_grids<64>(br); }
     case 128: { int rc = set_smem_attrs<128>(); return rc ? rc : prepare_grids<128>(br); }
+    case 160: { int rc = set_smem_attrs<160>(); return rc ? rc : prepare_grids<160>(br); }
     case 256: { int rc = set_smem_attrs<256>(); return rc ? rc : prepare_grids<256>(br); }
     default: { int rc = set_smem_attrs<512>(); return rc ? rc : prepare_grids<512>(br); }
     }
@@ -553,7 +557,10 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
         for (const SSPlan *p : plans)
             br.tiles = br.tiles && p->tt_ok && p->d_ovid && tt_pads_fit(*p, kBtLines, kBtPad);
     }
-    br.wmax = wneed <= 64 ? 64 : wneed <= 128 ? 128 : wneed <= 256 ? 256 : 512;
+    // 160 entries (40 KB of windows) covers 16-row tiles whenever rays are no
+    // denser than pixels (window <= 31 + 127 sample units + 3), and leaves
+    // room for five CTAs per SM where 256 (64 KB) allows three.
+    br.wmax = wneed <= 64 ? 64 : wneed <= 128 ? 128 : wneed <= 160 ? 160 : wneed <= 256 ? 256 : 512;
     if (wneed > 512) return set_error(RG_EUNSUPPORTED, "gather window of %d exceeds 512", wneed);
 
     Scratch sc;

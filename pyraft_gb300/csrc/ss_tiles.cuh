@@ -402,8 +402,8 @@ __device__ __forceinline__ void tt_walk(unsigned sb, unsigned &L, unsigned dq, u
 // thread t finds view t's rays that cross the window on lines
 // [i0, i0 + kTtLines) (FP32, two rays of margin; the exact int64 check below
 // drops rays that do not cross), the batch's 32-ray chunks are numbered by
-// a prefix sum, and the warps take chunks round robin, so the work spreads
-// evenly whatever the number of views and rays.  A lane walks its ray
+// a prefix sum, and each warp takes a contiguous range of them, so the work
+// spreads evenly whatever the number of views and rays.  A lane walks its ray
 // across the tile's lines and adds partial * Delta to out_am[view][ray].
 // Must be reached by every thread of the CTA (it has barriers).
 constexpr int kTtBatch = 256;
@@ -448,14 +448,41 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             __syncthreads();
         }
         const int nchunks = s_off[nb];
-        int t = 0;                                      // view of the current chunk
-        for (int g = warp; g < nchunks; g += nw) {
-            while (s_off[t + 1] <= g) ++t;              // chunks grow, so t only advances
-            const View &v = views[vid[v0 + t]];
-            const int k = s_klo[t] + ((g - s_off[t]) << 5) + lane;
+        // Warp w takes the contiguous chunks [g0, g1): consecutive chunks
+        // mostly belong to one view, whose constants it keeps in registers
+        // and reloads only when the view changes.
+        const int per = (nchunks + nw - 1) / nw;
+        const int g0 = min(nchunks, warp * per), g1 = min(nchunks, g0 + per);
+        int t = -1;                                     // view of the loaded constants
+        long long ub = 0, vrk = 0, vri = 0;
+        float vdelta = 0.f;
+        int vview = 0, kl = 0, off = 0;
+        for (int g = g0; g < g1; ++g) {
+            int tn = t < 0 ? 0 : t;
+            if (t < 0) {                                // first view: binary search
+                int lo = 0, hi = nb - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_off[mid] <= g) lo = mid; else hi = mid - 1;
+                }
+                tn = lo;
+            }
+            while (s_off[tn + 1] <= g) ++tn;            // chunks grow, so t only advances
+            if (tn != t) {
+                t = tn;
+                const View &v = views[vid[v0 + t]];
+                kl = s_klo[t];
+                off = s_off[t];
+                vrk = v.rk;
+                vri = v.ri;
+                ub = v.r0 + (long long)i0 * v.ri - base_q;
+                vdelta = v.delta;
+                vview = v.view;
+            }
+            const int k = kl + ((g - off) << 5) + lane;
             if (k >= R) continue;
-            const long long u = v.r0 + (long long)k * v.rk + (long long)i0 * v.ri - base_q;
-            const long long ue = u + (long long)(LINES - 1) * v.ri;
+            const long long u = ub + (long long)k * vrk;
+            const long long ue = u + (long long)(LINES - 1) * vri;
             // a crossing ray stays inside the pads (one entry of slack for the
             // Q9.23 stepping); others are margin rays, or (flagged) the plan's
             // pad check failed: they add nothing here
@@ -465,10 +492,10 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                 continue;
             }
             unsigned L = (unsigned)(u >> 9);
-            const unsigned dq = (unsigned)((v.ri + 256) >> 9);
+            const unsigned dq = (unsigned)((vri + 256) >> 9);
             float part = 0.f;
             tt_walk<ROW, LINES, 0>(sbase, L, dq, pb, part);
-            if (part != 0.f) atomicAdd(out_am + (size_t)v.view * out_ld + k, part * v.delta);
+            if (part != 0.f) atomicAdd(out_am + (size_t)vview * out_ld + k, part * vdelta);
         }
         __syncthreads();                                // s_klo / s_off reused
     }
@@ -569,7 +596,13 @@ __device__ __forceinline__ void gather_store(float val, int row, int col, int N,
 // adding the partials in rank order (deterministic).  Splitting the views
 // of every tile over a cluster multiplies the CTA count, so the last wave of
 // a grid of few large tiles no longer leaves most SMs idle.
-template <int MODE, int WMAX, int ROWS, bool EM>
+//
+// KAHAN (MODE 0 and 1): FP32 partial sums per chunk of kSlots views, added
+// across chunks with Kahan compensation (3 ROWS accumulator registers);
+// without it the views' terms are summed straight into ROWS FP32
+// accumulators, for callers whose view count is small (OSEM subsets of the
+// batch: at most a few chunks), where the registers buy occupancy.
+template <int MODE, int WMAX, int ROWS, bool EM, bool KAHAN = true>
 __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int s_ld, int R,
                                             const View *__restrict__ views, int nv, int N,
                                             float scale, float *__restrict__ out, long long cs,
@@ -670,23 +703,32 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
         // sample validity at positions 0 and N-1 of a line (CTA-uniform branch).
         // FP32 partial sums over the chunk (<= 32 views); across chunks they
         // are added with Kahan compensation (FP32) or in FP64 (MODE 2).
-        float part[ROWS];
+        if constexpr (MODE != 2 && !KAHAN) {
+            if (MODE != 0 && border)
+                accumulate<MODE, WMAX, ROWS, true>(acc, pairs, slot, slotP, slotFlags, nslot,
+                                                   lane, warp, col, myrow, N, pair_bytes);
+            else
+                accumulate<MODE, WMAX, ROWS, false>(acc, pairs, slot, slotP, slotFlags, nslot,
+                                                    lane, warp, col, myrow, N, pair_bytes);
+        } else {
+            float part[ROWS];
 #pragma unroll
-        for (int r = 0; r < ROWS; ++r) part[r] = 0.f;
-        if (MODE != 0 && border)
-            accumulate<MODE, WMAX, ROWS, true>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                               warp, col, myrow, N, pair_bytes);
-        else
-            accumulate<MODE, WMAX, ROWS, false>(part, pairs, slot, slotP, slotFlags, nslot, lane,
-                                                warp, col, myrow, N, pair_bytes);
+            for (int r = 0; r < ROWS; ++r) part[r] = 0.f;
+            if (MODE != 0 && border)
+                accumulate<MODE, WMAX, ROWS, true>(part, pairs, slot, slotP, slotFlags, nslot,
+                                                   lane, warp, col, myrow, N, pair_bytes);
+            else
+                accumulate<MODE, WMAX, ROWS, false>(part, pairs, slot, slotP, slotFlags, nslot,
+                                                    lane, warp, col, myrow, N, pair_bytes);
 #pragma unroll
-        for (int r = 0; r < ROWS; ++r) {
-            if (MODE == 2) {
-                acc[r] += (double)part[r];
-            } else {
-                float a = acc[r], c = comp[r];
-                kahan_add(a, c, part[r]);
-                acc[r] = a; comp[r] = c;
+            for (int r = 0; r < ROWS; ++r) {
+                if (MODE == 2) {
+                    acc[r] += (double)part[r];
+                } else {
+                    float a = acc[r], c = comp[r];
+                    kahan_add(a, c, part[r]);
+                    acc[r] = a; comp[r] = c;
+                }
             }
         }
         __syncthreads();
