@@ -133,7 +133,12 @@ __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restric
                                                      unsigned pb)
 {
     extern __shared__ __align__(128) float2 tile[];   // [kBtLines][kTtRowB]
+    static_assert(kBtLines == 16 && kTtWin % 32 == 0 && kTtWin % 16 == 0, "staging layout");
     const unsigned sbase = (unsigned)__cvta_generic_to_shared(tile);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // The pads stay zero for the kernel's life: items rewrite the window only.
+    for (int e = threadIdx.x; e < kBtLines * kTtRowB; e += blockDim.x)
+        tile[e] = make_float2(0.f, 0.f);
     for (;;) {
         const int item = next_item(counter);          // its barriers also end the last item
         if (item >= total) break;
@@ -146,19 +151,44 @@ __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restric
         const int nvo = o ? b.n_cols : b.n_rows;
         if (nvo == 0) continue;                        // CTA-uniform
         const float *__restrict__ x = b.x;
-        for (int e = threadIdx.x; e < kBtLines * kTtRowB; e += blockDim.x) {
-            int r, c;
-            if (o == 0) { r = e / kTtRowB; c = e - r * kTtRowB; }    // along image rows
-            else { c = e / kBtLines; r = e - c * kBtLines; }         // across a column strip
-            const int line = i0 + r, smp = p0 + c - kBtPad - 1;    // sample of entry p0 + c - pad
-            float2 v = make_float2(0.f, 0.f);
-            if (c >= kBtPad && c < kBtPad + kTtWin && line < N && smp >= 0 && smp <= N - 2) {
-                const float s0 = o ? __ldg(x + (size_t)smp * N + line) : __ldg(x + (size_t)line * N + smp);
-                const float s1 = o ? __ldg(x + (size_t)(smp + 1) * N + line)
-                                   : __ldg(x + (size_t)line * N + smp + 1);
-                v = make_pair(s0, s1, true);
+        // Window entry c of tile line r holds the pair of sample p0 + c - 1 of
+        // line i0 + r, read once per sample.
+        if (o == 0) {
+            // along image rows: warp w stages lines w, w + 8, lanes along the
+            // row (coalesced); the next sample comes from the next lane, and
+            // lane 31 reads its own
+            for (int r = warp; r < kBtLines; r += kWarps) {
+                const int line = i0 + r;
+                const bool lv = line < N;
+                const float *__restrict__ xr = x + (size_t)(lv ? line : 0) * N;
+#pragma unroll 1
+                for (int c0 = 0; c0 < kTtWin; c0 += 32) {
+                    const int smp = p0 + c0 + lane - 1;
+                    const float s0 = (lv && smp >= 0 && smp < N) ? __ldg(xr + smp) : 0.f;
+                    float s1 = __shfl_down_sync(0xffffffffu, s0, 1);
+                    if (lane == 31) s1 = (lv && smp + 1 < N) ? __ldg(xr + smp + 1) : 0.f;
+                    tile[r * kTtRowB + kBtPad + c0 + lane] =
+                        make_pair(s0, s1, lv && smp >= 0 && smp <= N - 2);
+                }
             }
-            tile[r * kTtRowB + c] = v;
+        } else {
+            // across a column strip: thread (line t % 16, group t / 16) stages
+            // the group's entries in order, keeping the previous sample;
+            // 16 consecutive lines are 16 consecutive floats of x
+            constexpr int per = kTtWin / 16;
+            const int r = threadIdx.x & 15, cb = (threadIdx.x >> 4) * per;
+            const int line = i0 + r;
+            const bool lv = line < N;
+            int smp = p0 + cb - 1;
+            float s0 = (lv && smp >= 0 && smp < N) ? __ldg(x + (size_t)smp * N + line) : 0.f;
+#pragma unroll 2
+            for (int j = 0; j < per; ++j) {
+                const int sn = smp + 1;
+                const float s1 = (lv && sn >= 0 && sn < N) ? __ldg(x + (size_t)sn * N + line) : 0.f;
+                tile[r * kTtRowB + kBtPad + cb + j] = make_pair(s0, s1, lv && smp >= 0 && smp <= N - 2);
+                s0 = s1;
+                smp = sn;
+            }
         }
         __syncthreads();
         tt_views<kTtRowB, kBtLines, kBtPad>(sbase, p0, i0, b.views, b.ovid + (o ? b.n_rows : 0), nvo, b.R,

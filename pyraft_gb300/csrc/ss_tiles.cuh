@@ -415,7 +415,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                                          float *__restrict__ out_am, int out_ld,
                                          int *__restrict__ err, unsigned pb)
 {
-    __shared__ int s_klo[kTtBatch], s_off[kTtBatch + 1];
+    __shared__ int s_klo[kTtBatch], s_off[kTtBatch + 1], s_wsum[kTtBatch / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int i1 = i0 + LINES - 1;
     const float a = p0 - 1.0f, b = p0 - 1.0f + kTtWin;     // window samples [a, b)
@@ -436,17 +436,21 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             s_klo[threadIdx.x] = klo;
             nch = khi >= klo ? (khi - klo + 32) >> 5 : 0;
         }
-        // exclusive prefix sum of the chunk counts (blockDim.x >= kTtBatch)
-        s_off[threadIdx.x + 1] = nch;
+        // prefix sum of the chunk counts over the CTA (blockDim.x == kTtBatch):
+        // within each warp by shuffles, then over the warps' totals;
+        // s_off[t] = chunks of views < t
+        int acc = nch;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, acc, o);
+            if (lane >= o) acc += y;
+        }
+        if (lane == 31) s_wsum[warp] = acc;
+        __syncthreads();
+        for (int w = 0; w < warp; ++w) acc += s_wsum[w];
+        s_off[threadIdx.x + 1] = acc;
         if (threadIdx.x == 0) s_off[0] = 0;
         __syncthreads();
-        for (int d = 1; d < kTtBatch; d <<= 1) {
-            const int t = threadIdx.x + 1;
-            const int add = (t > d && t <= kTtBatch) ? s_off[t - d] : 0;
-            __syncthreads();
-            if (t <= kTtBatch) s_off[t] += add;
-            __syncthreads();
-        }
         const int nchunks = s_off[nb];
         // Warp w takes the contiguous chunks [g0, g1): consecutive chunks
         // mostly belong to one view, whose constants it keeps in registers
@@ -454,8 +458,9 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
         const int per = (nchunks + nw - 1) / nw;
         const int g0 = min(nchunks, warp * per), g1 = min(nchunks, g0 + per);
         int t = -1;                                     // view of the loaded constants
-        long long ub = 0, vrk = 0, vri = 0;
+        long long ub = 0, vrk = 0, vspan = 0;
         float vdelta = 0.f;
+        unsigned dq = 0;
         int vview = 0, kl = 0, off = 0;
         for (int g = g0; g < g1; ++g) {
             int tn = t < 0 ? 0 : t;
@@ -474,7 +479,8 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                 kl = s_klo[t];
                 off = s_off[t];
                 vrk = v.rk;
-                vri = v.ri;
+                vspan = (long long)(LINES - 1) * v.ri;
+                dq = (unsigned)((v.ri + 256) >> 9);
                 ub = v.r0 + (long long)i0 * v.ri - base_q;
                 vdelta = v.delta;
                 vview = v.view;
@@ -482,7 +488,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             const int k = kl + ((g - off) << 5) + lane;
             if (k >= R) continue;
             const long long u = ub + (long long)k * vrk;
-            const long long ue = u + (long long)(LINES - 1) * vri;
+            const long long ue = u + vspan;
             // a crossing ray stays inside the pads (one entry of slack for the
             // Q9.23 stepping); others are margin rays, or (flagged) the plan's
             // pad check failed: they add nothing here
@@ -492,7 +498,6 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
                 continue;
             }
             unsigned L = (unsigned)(u >> 9);
-            const unsigned dq = (unsigned)((vri + 256) >> 9);
             float part = 0.f;
             tt_walk<ROW, LINES, 0>(sbase, L, dq, pb, part);
             if (part != 0.f) atomicAdd(out_am + (size_t)vview * out_ld + k, part * vdelta);
