@@ -53,7 +53,7 @@ struct BatchSlice {
     float2 *prow, *pcol;   // line pairs of the iterate
     float *x;              // iterate, N x N contiguous
     float *inv_sens;       // 1 / A_s^T 1 of this subset, N x N
-    const int *ovid;       // tile-driven Radon: view indices by orientation
+    const TtView *ttv;     // tile-driven Radon: per-view records by orientation
     int n_rows, n_cols;
     int begin[6];          // first item of this slice in each work list
 };
@@ -191,8 +191,8 @@ __global__ __launch_bounds__(256) void k_batch_tiles(const BatchSlice *__restric
             }
         }
         __syncthreads();
-        tt_views<kTtRowB, kBtLines, kBtPad>(sbase, p0, i0, b.views, b.ovid + (o ? b.n_rows : 0), nvo, b.R,
-                          b.ratio_am, b.R, err, pb);
+        tt_views<kTtRowB, kBtLines, kBtPad>(sbase, p0, i0, b.ttv + (o ? b.n_rows : 0), nvo, b.R,
+                                            b.ratio_am, b.R, err, pb);
     }
 }
 
@@ -639,7 +639,7 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
             d.begin[kEdges] = items_e;
             d.begin[kTiles] = items_t;
             d.begin[kRows] = items_rows[s];
-            d.ovid = (const int *)p->d_ovid;
+            d.ttv = (const TtView *)p->d_ovid;
             d.n_rows = p->n_ovid[0];
             d.n_cols = p->n_ovid[1];
             items_rows[s] += p->nv;

@@ -467,8 +467,8 @@ int launch_radon_tma(const SSPlan &p, const float2 *prow, const float2 *pcol, fl
 
 __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUtensorMap tm_rows,
                                                      const __grid_constant__ CUtensorMap tm_cols,
-                                                     int N, const View *__restrict__ views,
-                                                     const int *__restrict__ ovid, int n_rows,
+                                                     int N, const TtView *__restrict__ ttv,
+                                                     int n_rows,
                                                      int n_cols, int R,
                                                      float *__restrict__ out_am, int out_ld,
                                                      long long zo, int *__restrict__ err,
@@ -479,7 +479,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
     const int o = blockIdx.z & 1, z = blockIdx.z >> 1;
     const int nvo = o ? n_cols : n_rows;
     if (nvo == 0) return;                              // CTA-uniform, before any barrier
-    const int *__restrict__ vid = ovid + (o ? n_rows : 0);
+    const TtView *__restrict__ tv = ttv + (o ? n_rows : 0);
     const CUtensorMap *tm = o ? &tm_cols : &tm_rows;
     const int p0 = blockIdx.x * kTtWin, i0 = blockIdx.y * kTtLines;
     const unsigned sbase = smem_addr(tile);
@@ -510,7 +510,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
         return;
     }
 
-    tt_views<kTtRow>(sbase, p0, i0, views, vid, nvo, R, out_am, out_ld, err, pb);
+    tt_views<kTtRow>(sbase, p0, i0, tv, nvo, R, out_am, out_ld, err, pb);
 }
 
 // out[view][k] = 0 (zeroing pass) or the epilogue of the summed rays, for
@@ -554,8 +554,17 @@ int tt_build(SSPlan &p, const View *hv)
         p.tt_rk_max = std::max(p.tt_rk_max, fabs((double)hv[e].rk) * 2.3283064365386963e-10);
     }
     if (!tt_pads_fit(p, kTtLines, kTtPad)) return RG_OK;
-    RG_CK(cudaMalloc(&p.d_ovid, sizeof(int) * ids.size()));
-    RG_CK(cudaMemcpy(p.d_ovid, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice));
+    std::vector<TtView> tv(ids.size());
+    for (size_t q = 0; q < ids.size(); ++q) {
+        const View &v = hv[ids[q]];
+        tv[q].r0 = v.r0;
+        tv[q].rk = v.rk;
+        tv[q].ri = v.ri;
+        tv[q].delta = v.delta;
+        tv[q].view = v.view;
+    }
+    RG_CK(cudaMalloc(&p.d_ovid, sizeof(TtView) * tv.size()));
+    RG_CK(cudaMemcpy(p.d_ovid, tv.data(), sizeof(TtView) * tv.size(), cudaMemcpyHostToDevice));
     p.tt_ok = true;
     return RG_OK;
 }
@@ -587,7 +596,7 @@ int launch_radon_tiles(const SSPlan &p, const float2 *prow, const float2 *pcol, 
                                (int)smem));
     const dim3 grid((pairs_pitch(N) + kTtWin - 1) / kTtWin, (N + kTtLines - 1) / kTtLines,
                     2 * nz);
-    k_radon_tiles<<<grid, 256, smem, st>>>(tr, tc, N, p.d_views, (const int *)p.d_ovid,
+    k_radon_tiles<<<grid, 256, smem, st>>>(tr, tc, N, (const TtView *)p.d_ovid,
                                            p.n_ovid[0], p.n_ovid[1], R, out_am, out_ld, zo,
                                            device_error_word(), (unsigned)sizeof(float2));
     RG_CK_LAUNCH("k_radon_tiles");

@@ -122,13 +122,24 @@ struct SSPlan {
     // windows fit st_bw entries (nblocks == 0: the direct kernels are used)
     void *d_blocks = nullptr;      // StBlock[nblocks], device
     int nblocks = 0, st_bw = 0;
-    // tile-driven Radon (radon_tma.cu): view indices grouped by orientation
-    // (rows first), device
+    // tile-driven Radon (radon_tma.cu): TtView records grouped by
+    // orientation (rows first), device
     void *d_ovid = nullptr;
     int n_ovid[2] = {0, 0};
     bool tt_ok = false;
     double tt_ri_max = 0.0, tt_rk_max = 0.0;   // max |ri|, |rk| over the views (samples)
 };
+
+// Per-view constants of the tile-driven Radon, grouped by line orientation
+// (rows first): one 32-byte record per view, so that the threads of a CTA
+// read consecutive records (the 112-byte View records, reached through an
+// index, scattered each warp's loads over 32 records).
+struct __align__(16) TtView {
+    long long r0, rk, ri;   // Q32.32 Radon position u = r0 + k rk + i ri
+    float delta;            // ray-sum scale
+    int view;               // sinogram column
+};
+static_assert(sizeof(TtView) == 32, "TtView layout");
 
 // A block of the TMA-staged Radon: views [first, first + count) of a plan,
 // all with the same line orientation.

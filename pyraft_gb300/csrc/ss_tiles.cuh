@@ -410,8 +410,7 @@ constexpr int kTtBatch = 256;
 
 template <int ROW, int LINES = kTtLines, int PAD = kTtPad>
 __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
-                                         const View *__restrict__ views,
-                                         const int *__restrict__ vid, int nvo, int R,
+                                         const TtView *__restrict__ tv, int nvo, int R,
                                          float *__restrict__ out_am, int out_ld,
                                          int *__restrict__ err, unsigned pb)
 {
@@ -425,7 +424,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
         const int nb = min(kTtBatch, nvo - v0);
         int nch = 0;
         if ((int)threadIdx.x < nb) {
-            const View &v = views[vid[v0 + threadIdx.x]];
+            const TtView v = tv[v0 + threadIdx.x];
             const float rk = (float)v.rk * 2.3283064365386963e-10f;
             const float c0 = ((float)v.r0 + (float)i0 * (float)v.ri) * 2.3283064365386963e-10f;
             const float c1 = ((float)v.r0 + (float)i1 * (float)v.ri) * 2.3283064365386963e-10f;
@@ -475,7 +474,7 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
             while (s_off[tn + 1] <= g) ++tn;            // chunks grow, so t only advances
             if (tn != t) {
                 t = tn;
-                const View &v = views[vid[v0 + t]];
+                const TtView v = tv[v0 + t];
                 kl = s_klo[t];
                 off = s_off[t];
                 vrk = v.rk;
