@@ -243,21 +243,22 @@ __global__ __launch_bounds__(256) void k_batch_gather(const BatchSlice *__restri
     }
 }
 
-// Edge pixels left out by k_batch_gather (adjoint_edge_pixel): one warp per
-// edge pixel of every slice (items: slice x (4N - 4)).
+// Edge pixels left out by k_batch_gather (adjoint_edge_group): one CTA per
+// 32 consecutive edge pixels of a slice (items: slice x groups of 32 of its
+// 4N - 4 edge pixels).
 template <int MODE>
-__global__ __launch_bounds__(128) void k_batch_edges(const BatchSlice *__restrict__ d, int n,
+__global__ __launch_bounds__(256) void k_batch_edges(const BatchSlice *__restrict__ d, int n,
                                                      int total)
 {
-    const int item = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (item >= total) return;        // warp-uniform
+    const int item = blockIdx.x;
+    if (item >= total) return;        // CTA-uniform
     const BatchSlice &b = d[find_slice(d, n, item, kEdges)];
-    const int e = item - b.begin[kEdges];
+    const int e0 = (item - b.begin[kEdges]) * 32;
     if (MODE == 1)
-        adjoint_edge_pixel<1, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, e, nullptr, 0, 0,
+        adjoint_edge_group<1, true, 8>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, e0, nullptr, 0, 0,
                                     b.x, b.inv_sens);
     else
-        adjoint_edge_pixel<2, false>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, e, b.inv_sens, b.N,
+        adjoint_edge_group<2, false, 8>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, e0, b.inv_sens, b.N,
                                      1, nullptr, nullptr);
 }
 
@@ -339,8 +340,7 @@ int enqueue_iteration(const BatchRun &br, cudaStream_t st)
                                                                   br.counter,
                                                                   (unsigned)sizeof(float2));
         RG_CK_LAUNCH("k_batch_gather<1>");
-        k_batch_edges<1><<<(br.total[kEdges][0] + 3) / 4, 128, 0, st>>>(d, br.n,
-                                                                       br.total[kEdges][0]);
+        k_batch_edges<1><<<br.total[kEdges][0], 256, 0, st>>>(d, br.n, br.total[kEdges][0]);
         RG_CK_LAUNCH("k_batch_edges<1>");
     }
     return RG_OK;
@@ -357,8 +357,7 @@ int enqueue_sensitivity(const BatchRun &br, cudaStream_t st)
                                                                   br.counter,
                                                                   (unsigned)sizeof(float2));
         RG_CK_LAUNCH("k_batch_gather<2>");
-        k_batch_edges<2><<<(br.total[kEdges][0] + 3) / 4, 128, 0, st>>>(d, br.n,
-                                                                       br.total[kEdges][0]);
+        k_batch_edges<2><<<br.total[kEdges][0], 256, 0, st>>>(d, br.n, br.total[kEdges][0]);
         RG_CK_LAUNCH("k_batch_edges<2>");
     }
     return RG_OK;
@@ -649,7 +648,7 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
         }
         items_lp += tiles * tiles;
         items_g += tiles * tiles_y;
-        items_e += 4 * N - 4;
+        items_e += (4 * N - 4 + 31) / 32;
         items_t += 2 * ((pairs_pitch(N) + kTtWin - 1) / kTtWin) * ((N + kBtLines - 1) / kBtLines);
     }
     br.total[kLP][0] = items_lp;

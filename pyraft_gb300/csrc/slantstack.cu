@@ -368,10 +368,11 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
 }
 
 // Edge pixels of the matched adjoint and of its FP64 sensitivity
-// (adjoint_edge_pixel, ss_tiles.cuh): one warp per pixel of the image's
-// first and last rows and columns.
+// (adjoint_edge_group, ss_tiles.cuh): one CTA per 32 consecutive pixels of
+// the image's first and last rows and columns, its 32 warps splitting the
+// views.
 template <int MODE, bool EM>
-__global__ __launch_bounds__(128) void k_adjoint_edges(const float *__restrict__ s_am, int s_ld,
+__global__ __launch_bounds__(1024) void k_adjoint_edges(const float *__restrict__ s_am, int s_ld,
                                                        int R, const View *__restrict__ views,
                                                        int nv, int N, float *__restrict__ out,
                                                        long long cs, long long ls,
@@ -379,9 +380,7 @@ __global__ __launch_bounds__(128) void k_adjoint_edges(const float *__restrict__
                                                        const float *__restrict__ inv_sens,
                                                        long long zs, long long zo)
 {
-    const int e = blockIdx.x * 4 + (threadIdx.x >> 5);
-    if (e >= 4 * N - 4) return;       // warp-uniform
-    adjoint_edge_pixel<MODE, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, e,
+    adjoint_edge_group<MODE, EM, 32>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, blockIdx.x * 32,
                                  out + blockIdx.z * zo, cs, ls, em_x, inv_sens);
 }
 
@@ -391,8 +390,8 @@ static int adjoint_edges(const SSPlan &p, const float *s_am, int s_ld, float *ou
                          const Stack &z)
 {
     const int N = p.g.N;
-    dim3 grid((4 * N - 4 + 3) / 4, 1, z.n);     // one warp per edge pixel
-    k_adjoint_edges<MODE, EM><<<grid, 128, 0, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs,
+    dim3 grid((4 * N - 4 + 31) / 32, 1, z.n);   // 32 edge pixels per CTA
+    k_adjoint_edges<MODE, EM><<<grid, 1024, 0, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs,
                                                     ls, em_x, inv_sens, z.in, z.out);
     RG_CK_LAUNCH("k_adjoint_edges");
     return RG_OK;

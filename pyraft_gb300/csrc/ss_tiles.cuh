@@ -505,33 +505,46 @@ __device__ __forceinline__ void tt_views(unsigned sbase, int p0, int i0,
     }
 }
 
-// Edge pixel e (of 4N - 4: rows 0 and N-1, then columns 0 and N-1) of the
-// matched adjoint (MODE 1, optionally with the EM update) or of its
-// FP64-accumulated sensitivity (MODE 2), computed by one warp.  The image's
-// first and last rows and columns are the only pixels where the Radon's
-// validity rules at line positions 0 and N-1 apply; the gathers leave them
-// out (edge_fixup) and run the rule-free interior path on every tile.  Lane
-// l sums views l, l + 32, ... straight from the view-major sinogram, with
-// the hat weights and rules of the border path of `accumulate`, and the
-// lanes' sums meet in a fixed butterfly order.
-template <int MODE, bool EM>
-__device__ __forceinline__ void adjoint_edge_pixel(const float *__restrict__ s_am, int s_ld, int R,
+// Edge pixels e0 .. e0 + 31 (of 4N - 4: rows 0 and N-1, then columns 0 and
+// N-1) of the matched adjoint (MODE 1, optionally with the EM update) or of
+// its FP64-accumulated sensitivity (MODE 2), computed by one CTA of WARPS
+// warps.  The image's first and last rows and columns are the only pixels
+// where the Radon's validity rules at line positions 0 and N-1 apply; the
+// gathers leave them out (edge_fixup) and run the rule-free interior path
+// on every tile.  Lane l takes pixel e0 + l, and warp w the views
+// [w nv / WARPS, (w + 1) nv / WARPS): a warp reads each view's constants once for
+// its 32 pixels (the same address in every lane), and neighbouring edge
+// pixels read neighbouring sinogram samples.  Each lane sums its views with
+// the hat weights and rules of the border path of `accumulate` (Kahan-
+// compensated FP32, or FP64 for MODE 2), and the warps' sums meet in
+// shared memory in warp order.  One slice's edges make few groups (128 at
+// 1024^2), so its kernel splits the views over 32 warps; the batch, with
+// many slices, over 8.
+template <int MODE, bool EM, int WARPS>
+__device__ __forceinline__ void adjoint_edge_group(const float *__restrict__ s_am, int s_ld, int R,
                                                    const View *__restrict__ views, int nv, int N,
-                                                   int e, float *__restrict__ out, long long cs,
+                                                   int e0, float *__restrict__ out, long long cs,
                                                    long long ls, float *__restrict__ em_x,
                                                    const float *__restrict__ inv_sens)
 {
-    const int lane = threadIdx.x & 31;
-    int row, col;
-    if (e < N) { row = 0; col = e; }
+    __shared__ float red[WARPS][32];
+    __shared__ double red64[MODE == 2 ? WARPS : 1][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int e = e0 + lane;
+    const bool live = e < 4 * N - 4;
+    int row = 0, col = 0;
+    if (!live) { row = 0; col = 0; }
+    else if (e < N) { row = 0; col = e; }
     else if (e < 2 * N) { row = N - 1; col = e - N; }
     else if (e < 3 * N - 2) { row = e - 2 * N + 1; col = 0; }
     else { row = e - (3 * N - 2) + 1; col = N - 1; }
     float acc = 0.f, comp = 0.f;
     double acc64 = 0.0;
+    const int vb = (int)((long long)nv * warp / WARPS);
+    const int ve = (int)((long long)nv * (warp + 1) / WARPS);
     // unrolled so that several views' loads are in flight per lane
 #pragma unroll 4
-    for (int j = lane; j < nv; j += 32) {
+    for (int j = vb; j < ve; ++j) {
         const View &v = views[j];
         const long long kap = v.k0 + (long long)row * v.krow + (long long)col * v.kcol;
         const int k = (int)(kap >> 32);
@@ -556,16 +569,19 @@ __device__ __forceinline__ void adjoint_edge_pixel(const float *__restrict__ s_a
         if (MODE == 2) acc64 += (double)term;
         else kahan_add(acc, comp, term);
     }
-    float sum = acc - comp;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        if (MODE == 2) acc64 += __shfl_xor_sync(0xffffffffu, acc64, o);
-        else sum += __shfl_xor_sync(0xffffffffu, sum, o);
-    }
-    if (lane != 0) return;
+    if (MODE == 2) red64[warp][lane] = acc64;
+    else red[warp][lane] = acc - comp;
+    __syncthreads();
+    if (warp != 0 || !live) return;
     if (MODE == 2) {
-        out[(long long)row * cs + (long long)col * ls] = (acc64 > 0.0) ? (float)(1.0 / acc64) : 0.f;
-    } else if (EM) {
+        double sum = 0.0;
+        for (int w = 0; w < WARPS; ++w) sum += red64[w][lane];
+        out[(long long)row * cs + (long long)col * ls] = (sum > 0.0) ? (float)(1.0 / sum) : 0.f;
+        return;
+    }
+    float sum = 0.f;
+    for (int w = 0; w < WARPS; ++w) sum += red[w][lane];
+    if (EM) {
         const size_t idx = (size_t)row * N + col;
         em_x[idx] = em_x[idx] * sum * inv_sens[idx];
     } else {
