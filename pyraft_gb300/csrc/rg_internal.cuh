@@ -117,6 +117,9 @@ struct SSPlan {
     bool contiguous = true;        // views are consecutive (not an OSEM subset)
     bool rot_ok = false;           // second half of the views = first half + pi/2, on a grid
                                    // symmetric under a quarter turn (gather_rot.cu)
+    bool mirror_ok = false;        // image and detector centred on 0: pixel (r, c) and
+                                   // (N-1-r, N-1-c) meet a view at mirrored ray positions
+                                   // (gather_tile_mirror)
     int device = -1;
     // TMA-staged Radon (radon_tma.cu): blocks of adjacent views whose line
     // windows fit st_bw entries (nblocks == 0: the direct kernels are used)

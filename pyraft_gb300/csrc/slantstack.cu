@@ -143,6 +143,9 @@ int ss_views_compute(SSPlan &p, const SSGeom &g, const int *views, int nv, View 
     const double pi = 3.14159265358979323846;
     p.rot_ok = nv >= 2 && nv % 2 == 0 && g.A % 2 == 0 && fabs((thf - th0) - pi) <= 1e-12 * pi &&
                g.itl_x == g.ibr_y && g.ibr_x == g.itl_y && g.itl_x == -g.ibr_x;
+    // A half turn maps the grid onto itself and t onto -t: x and y each
+    // centred on 0, and the detector's t range centred on 0.
+    p.mirror_ok = g.itl_x == -g.ibr_x && g.itl_y == -g.ibr_y && g.stl_y == -g.sbr_y;
     for (int e = 0; e < nv / 2 && p.rot_ok; ++e) {
         const int j = views ? views[e] : e, j2 = views ? views[e + nv / 2] : e + nv / 2;
         p.rot_ok = j2 == j + g.A / 2;

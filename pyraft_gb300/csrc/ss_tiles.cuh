@@ -792,4 +792,133 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
     }
 }
 
+// The matched adjoint with the EM update for the tile (tx, ty) and its
+// half-turn mirror, for plans with mirror_ok (image and detector centred on
+// 0).  Pixel (r, c) at ray position kappa = k + f of a view and pixel
+// (N-1-r, N-1-c) at (R-1) - kappa = (R-2-k) + (1-f) of the same view: the
+// mirror's hat weights are the primary's swapped,
+//     primary: s[k] w_a + s[k+1] w_b,   mirror: s[R-2-k] w_b + s[R-1-k] w_a,
+// so one position, one pair of weights and one 128-bit load of the quad
+// {s[k], s[k+1], s[R-2-k], s[R-1-k]} (times the view's Delta) serve both.
+// (The hat weights are continuous where a ray leaves the detector, so this
+// holds at exact ties too; the backprojection's half-open validity range
+// is not symmetric there, so it keeps gather_tile.)  Unlike the
+// quarter-turn pairing it needs no partner view: every view of an OSEM
+// subset pairs with itself.  One CTA sums all views for both tiles, so
+// every pixel's sum is complete here and the update x <- x * sum * inv is
+// applied in this epilogue.  The mirror tile must be another tile of the
+// grid (N a multiple of 2 * 8 * ROWS and of 64); edge pixels are left to
+// adjoint_edge_group.  Windows are staged in chunks of kSlots / 2 views of
+// WMAX quads, the same shared memory as gather_tile's pairs.
+template <int WMAX, int ROWS>
+__device__ __forceinline__ void gather_tile_mirror(const float *__restrict__ s_am, int s_ld, int R,
+                                                   const View *__restrict__ views, int nv, int N,
+                                                   float *__restrict__ em_x,
+                                                   const float *__restrict__ inv_sens,
+                                                   int *__restrict__ err, int tx, int ty,
+                                                   float4 *__restrict__ quads, unsigned quad_bytes)
+{
+    constexpr int TH = kWarps * ROWS;
+    constexpr int kMSlots = kSlots / 2;
+    __shared__ SlotInfo slot[kMSlots];
+    __shared__ int slotW[kMSlots];
+    __shared__ int slotView[kMSlots];
+    __shared__ float slotDelta[kMSlots];
+    __shared__ float slotP[kMSlots];
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int row0 = ty * TH, col0 = tx * kTile;
+    const int col = col0 + lane;
+    const int myrow = row0 + warp * ROWS;
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(quads);
+
+    float accP[ROWS], accM[ROWS];
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) { accP[r] = 0.f; accM[r] = 0.f; }
+
+    for (int chunk = 0; chunk < nv; chunk += kMSlots) {
+        const int nslot = min(kMSlots, nv - chunk);
+        if (warp == 0 && lane < kMSlots) {
+            SlotInfo si = {0u, 0, 0, INT_MIN};
+            int W = 0, view = 0;
+            float P = 0.f, delta = 0.f;
+            if (lane < nslot) {
+                const View &v = views[chunk + lane];
+                const long long cr = v.krow, cc = v.kcol;
+                const long long origin = v.k0 + (long long)row0 * cr + (long long)col0 * cc;
+                const long long dr = (long long)(TH - 1) * cr, dc = (long long)(kTile - 1) * cc;
+                const long long mn = origin + min(0LL, dr) + min(0LL, dc);
+                const long long mx = origin + max(0LL, dr) + max(0LL, dc);
+                const int nlo = (int)(mn >> 32) - 1;
+                const int nhi = (int)(mx >> 32) + 1;
+                if (nhi - nlo + 1 <= WMAX) {
+                    si.nlo = nlo;
+                    si.base = (unsigned)((origin - ((long long)nlo << 32)) >> 9);
+                    si.a = (int)((cc + 256) >> 9);
+                    si.b = (int)((cr + 256) >> 9);
+                    W = nhi - nlo + 1;
+                } else if (err) {
+                    atomicOr(err, 1);
+                }
+                view = v.view;
+                delta = v.delta;
+                P = v.P;
+            }
+            slot[lane] = si;
+            slotW[lane] = W;
+            slotView[lane] = view;
+            slotDelta[lane] = delta;
+            slotP[lane] = P;
+        }
+        __syncthreads();
+
+        // Stage each view's quads: entry e holds samples n, n + 1 and their
+        // mirrors R-2-n, R-1-n (n = nlo + e), zero outside the row.
+        for (int s = warp; s < nslot; s += kWarps) {
+            const int nlo = slot[s].nlo, W = slotW[s];
+            const float *__restrict__ row = s_am + (size_t)slotView[s] * s_ld;
+            const float d = slotDelta[s];
+            for (int e = lane; e < W; e += 32) {
+                const int n = nlo + e, m = R - 2 - n;
+                const float v0 = (n >= 0 && n < R) ? __ldg(row + n) * d : 0.f;
+                const float v1 = (n + 1 >= 0 && n + 1 < R) ? __ldg(row + n + 1) * d : 0.f;
+                const float u0 = (m >= 0 && m < R) ? __ldg(row + m) * d : 0.f;
+                const float u1 = (m + 1 >= 0 && m + 1 < R) ? __ldg(row + m + 1) * d : 0.f;
+                quads[s * WMAX + e] = make_float4(v0, v1, u0, u1);
+            }
+        }
+        __syncthreads();
+
+        for (int s = 0; s < nslot; ++s) {
+            const SlotInfo si = slot[s];
+            if (si.nlo == INT_MIN) continue;
+            const unsigned pw = sbase + (unsigned)(s * WMAX) * quad_bytes;
+            unsigned vpos = si.base + (unsigned)(lane * si.a) + (unsigned)(warp * ROWS * si.b);
+            const float P = slotP[s];
+            const float c0 = 1.f + P, c1 = 1.f - 2.f * P;
+#pragma unroll
+            for (int r = 0; r < ROWS; ++r) {
+                const unsigned addr = (vpos >> 23) * quad_bytes + pw;
+                float a, b, c, d;
+                asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                             : "=f"(a), "=f"(b), "=f"(c), "=f"(d) : "r"(addr));
+                const float w1 = frac_plus_one(vpos);
+                const float wa = fma_sat(-P, w1, c0), wb = fma_sat(P, w1, c1);
+                accP[r] = fmaf(b, wb, fmaf(a, wa, accP[r]));
+                accM[r] = fmaf(c, wb, fmaf(d, wa, accM[r]));
+                vpos += (unsigned)si.b;
+            }
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int r = 0; r < ROWS; ++r) {
+        const int row = myrow + r;
+        if (row == 0 || col == 0 || row == N - 1 || col == N - 1) continue;   // edge pixels
+        gather_store<1, true>(accP[r], row, col, N, nullptr, 0, 0, em_x, inv_sens);
+        gather_store<1, true>(accM[r], N - 1 - row, N - 1 - col, N, nullptr, 0, 0, em_x, inv_sens);
+    }
+}
+
 }  // namespace rg
