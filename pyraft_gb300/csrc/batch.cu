@@ -267,9 +267,10 @@ __global__ __launch_bounds__(256, 4) void k_batch_mirror(const BatchSlice *__res
         if (item >= total) break;
         const BatchSlice &b = d[find_slice(d, n, item, kMirror)];
         const int local = item - b.begin[kMirror], tiles = b.N / 32;
-        gather_tile_mirror<WMAX, kMirrorRows>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N, b.x,
-                                             b.inv_sens, nullptr, local % tiles, local / tiles,
-                                             mquads, quad_bytes);
+        gather_tile_mirror<WMAX, kMirrorRows, true>(b.ratio_am, b.R, b.R, b.views, b.nv, b.N,
+                                                   nullptr, 0, 0, b.x, b.inv_sens, nullptr,
+                                                   local % tiles, local / tiles, mquads,
+                                                   quad_bytes);
     }
 }
 

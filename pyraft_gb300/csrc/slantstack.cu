@@ -370,6 +370,34 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
                                       blockIdx.x % split, MODE != 0);
 }
 
+// The matched adjoint (optionally with the EM update) on tile pairs related
+// by a half turn (gather_tile_mirror, ss_tiles.cuh): blockIdx.y covers the
+// upper half of the tile rows, and the views of a pair may be split over a
+// cluster along x as in k_gather.  Registers are held to 64 (four CTAs per
+// SM), without spills at any tile height: the batched form measured that
+// much faster than the compiler's choice (73 registers at 16 rows).
+template <int WMAX, int ROWS, bool EM>
+__global__ __launch_bounds__(256, 4) void k_gather_mirror(
+    const float *__restrict__ s_am, int s_ld, int R, const View *__restrict__ views, int nv, int N,
+    float *__restrict__ out, long long cs, long long ls, float *__restrict__ em_x,
+    const float *__restrict__ inv_sens, int *__restrict__ err, long long zs, long long zo,
+    unsigned quad_bytes, int split)
+{
+    extern __shared__ __align__(16) float4 mq[];   // [kSlots / 2][WMAX], or 2 ROWS x 256 floats
+    gather_tile_mirror<WMAX, ROWS, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N,
+                                       out + blockIdx.z * zo, cs, ls, em_x, inv_sens, err,
+                                       blockIdx.x / split, blockIdx.y, mq, quad_bytes, split,
+                                       blockIdx.x % split);
+}
+
+// RG_GATHER_MIRROR=0: the one-view adjoint runs tile by tile even where its
+// tiles pair with their half-turn mirrors.
+static bool gather_mirror_enabled()
+{
+    const char *e = getenv("RG_GATHER_MIRROR");
+    return !(e && !strcmp(e, "0"));
+}
+
 // Edge pixels of the matched adjoint and of its FP64 sensitivity
 // (adjoint_edge_group, ss_tiles.cuh): one CTA per 32 consecutive pixels of
 // the image's first and last rows and columns, its 32 warps splitting the
@@ -488,6 +516,45 @@ int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, c
     return best;
 }
 
+template <int WMAX, int ROWS, bool EM>
+static int gather_w_mirror(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
+                           long long ls, float *em_x, const float *inv_sens, int *d_err,
+                           cudaStream_t st, const Stack &z)
+{
+    const int N = p.g.N;
+    // quads of kSlots / 2 views, or the cluster reduction's 2 ROWS x 256 floats
+    const size_t smem = std::max((size_t)(kSlots / 2) * WMAX * sizeof(float4),
+                                 (size_t)2 * ROWS * 256 * sizeof(float));
+    dim3 grid(N / kTile, N / (2 * kWarps * ROWS), z.n);
+    auto k = k_gather_mirror<WMAX, ROWS, EM>;
+    RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int split = pick_split(k, smem, ROWS, p.nv, grid, st);
+    const unsigned qb = (unsigned)sizeof(float4);
+    if (int rc = adjoint_edges<1, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, st, z)) return rc;
+    if (split == 1) {
+        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs, ls, em_x,
+                                   inv_sens, d_err, z.in, z.out, qb, 1);
+        RG_CK_LAUNCH("k_gather_mirror");
+        return RG_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, p.nv, N, out, cs,
+                             ls, em_x, inv_sens, d_err, z.in, z.out, qb, split));
+    RG_CK_LAUNCH("k_gather_mirror (cluster)");
+    return RG_OK;
+}
+
 template <int MODE, int WMAX, int ROWS, bool EM>
 static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                     long long ls, float *em_x, const float *inv_sens, int *d_err,
@@ -496,6 +563,14 @@ static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
     const size_t smem = (size_t)kSlots * WMAX * sizeof(float2);
     dim3 grid((p.g.N + kTile - 1) / kTile, (p.g.N + kWarps * ROWS - 1) / (kWarps * ROWS), z.n);
     const float scale = (MODE == 0) ? p.dth : 1.f;
+    if constexpr (MODE == 1) {
+        // Half-turn mirrored tile pairs (gather_tile_mirror) on a centred
+        // geometry whose tiles pair up.
+        const int N = p.g.N;
+        if (p.mirror_ok && N % 64 == 0 && N % (2 * kWarps * ROWS) == 0 && gather_mirror_enabled())
+            return gather_w_mirror<WMAX, ROWS, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens,
+                                                   d_err, st, z);
+    }
     auto k = k_gather<MODE, WMAX, ROWS, EM>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int split = (MODE == 2) ? 1 : pick_split(k, smem, ROWS, p.nv, grid, st);

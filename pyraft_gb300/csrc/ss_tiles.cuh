@@ -810,13 +810,22 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
 // grid (N a multiple of 2 * 8 * ROWS and of 64); edge pixels are left to
 // adjoint_edge_group.  Windows are staged in chunks of kSlots / 2 views of
 // WMAX quads, the same shared memory as gather_tile's pairs.
-template <int WMAX, int ROWS>
+//
+// EM: x <- x * sum * inv for both pixels (the sums are whole); else the sums
+// are stored to out.  split > 1: the CTA is rank `rank` of a cluster of
+// `split` CTAs sharing the tile pair; it sums views [rank nv / split,
+// (rank + 1) nv / split), the partials meet in distributed shared memory
+// (`quads` must then hold 2 ROWS x 256 floats) and each rank finishes
+// ROWS / split of the rows of both tiles, adding the ranks in order.
+template <int WMAX, int ROWS, bool EM>
 __device__ __forceinline__ void gather_tile_mirror(const float *__restrict__ s_am, int s_ld, int R,
                                                    const View *__restrict__ views, int nv, int N,
-                                                   float *__restrict__ em_x,
+                                                   float *__restrict__ out, long long cs,
+                                                   long long ls, float *__restrict__ em_x,
                                                    const float *__restrict__ inv_sens,
                                                    int *__restrict__ err, int tx, int ty,
-                                                   float4 *__restrict__ quads, unsigned quad_bytes)
+                                                   float4 *__restrict__ quads, unsigned quad_bytes,
+                                                   int split = 1, int rank = 0)
 {
     constexpr int TH = kWarps * ROWS;
     constexpr int kMSlots = kSlots / 2;
@@ -836,8 +845,10 @@ __device__ __forceinline__ void gather_tile_mirror(const float *__restrict__ s_a
 #pragma unroll
     for (int r = 0; r < ROWS; ++r) { accP[r] = 0.f; accM[r] = 0.f; }
 
-    for (int chunk = 0; chunk < nv; chunk += kMSlots) {
-        const int nslot = min(kMSlots, nv - chunk);
+    const int vbeg = (int)((long long)nv * rank / split);
+    const int vend = (int)((long long)nv * (rank + 1) / split);
+    for (int chunk = vbeg; chunk < vend; chunk += kMSlots) {
+        const int nslot = min(kMSlots, vend - chunk);
         if (warp == 0 && lane < kMSlots) {
             SlotInfo si = {0u, 0, 0, INT_MIN};
             int W = 0, view = 0;
@@ -912,12 +923,40 @@ __device__ __forceinline__ void gather_tile_mirror(const float *__restrict__ s_a
         __syncthreads();
     }
 
+    if (split > 1) {
+        // The last chunk ended with a barrier: the staging area is free.
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+        float *red = reinterpret_cast<float *>(quads);    // [2 ROWS][256]
+#pragma unroll
+        for (int r = 0; r < ROWS; ++r) {
+            red[r * 256 + threadIdx.x] = accP[r];
+            red[(ROWS + r) * 256 + threadIdx.x] = accM[r];
+        }
+        cl.sync();
+        const int per = ROWS / split;
+        for (int q = 0; q < per; ++q) {
+            const int r = rank * per + q;
+            float sp = 0.f, sm = 0.f;
+            for (int src = 0; src < split; ++src) {
+                const float *peer = cl.map_shared_rank(red, src);
+                sp += peer[r * 256 + threadIdx.x];
+                sm += peer[(ROWS + r) * 256 + threadIdx.x];
+            }
+            const int row = myrow + r;
+            if (row == 0 || col == 0 || row == N - 1 || col == N - 1) continue;   // edge pixels
+            gather_store<1, EM>(sp, row, col, N, out, cs, ls, em_x, inv_sens);
+            gather_store<1, EM>(sm, N - 1 - row, N - 1 - col, N, out, cs, ls, em_x, inv_sens);
+        }
+        cl.sync();    // no CTA leaves while a peer still reads its partials
+        return;
+    }
 #pragma unroll
     for (int r = 0; r < ROWS; ++r) {
         const int row = myrow + r;
         if (row == 0 || col == 0 || row == N - 1 || col == N - 1) continue;   // edge pixels
-        gather_store<1, true>(accP[r], row, col, N, nullptr, 0, 0, em_x, inv_sens);
-        gather_store<1, true>(accM[r], N - 1 - row, N - 1 - col, N, nullptr, 0, 0, em_x, inv_sens);
+        gather_store<1, EM>(accP[r], row, col, N, out, cs, ls, em_x, inv_sens);
+        gather_store<1, EM>(accM[r], N - 1 - row, N - 1 - col, N, out, cs, ls, em_x, inv_sens);
     }
 }
 

@@ -121,3 +121,19 @@ def test_batch_mirrored_tile_pairs(orc, monkeypatch):
     for (n, r, a), s, o, q in zip(geo, sinos, out, ref):
         assert rel(o, q) <= 1e-5, (n, a)
         assert rel(o, rg.osem(s, (n, n), it, S)) <= 1e-5, (n, a)
+
+
+def test_batch_mirror_sparse_rays_and_off_centre_grid(orc):
+    """The mirrored adjoint with fewer rays than pixels (R < N, centred
+    geometry), beside a slice whose image grid is off centre (its start
+    image carries shifted corners), which must keep the tile-by-tile
+    adjoint: each matches the one-slice OSEM from the same start image."""
+    n, S, it = 256, 4, 2
+    geo = [(200, 150), (256, 121)]
+    ys = [emission(orc, n, r, a, 70 + k) for k, (r, a) in enumerate(geo)]
+    sinos = [rg.image(y, **SINO_C) for y in ys]
+    x0 = [rg.image(np.ones((n, n))),
+          rg.image(np.ones((n, n)), top_left=(-1.0, 0.9), bottom_right=(1.0, -1.1))]
+    out = rg.osem_batch(sinos, None, it, S, x0=x0)
+    for s, o, x in zip(sinos, out, x0):
+        assert rel(o, rg.osem(s, x, it, S)) <= 1e-5
