@@ -516,6 +516,14 @@ int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, c
     return best;
 }
 
+// Whether the matched adjoint of plan p with ROWS rows per thread runs on
+// half-turn mirrored tile pairs: a centred geometry whose tiles pair up.
+static bool mirror_applies(const SSPlan &p, int rows)
+{
+    const int N = p.g.N;
+    return p.mirror_ok && N % 64 == 0 && N % (2 * kWarps * rows) == 0 && gather_mirror_enabled();
+}
+
 template <int WMAX, int ROWS, bool EM>
 static int gather_w_mirror(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                            long long ls, float *em_x, const float *inv_sens, int *d_err,
@@ -566,8 +574,7 @@ static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
     if constexpr (MODE == 1) {
         // Half-turn mirrored tile pairs (gather_tile_mirror) on a centred
         // geometry whose tiles pair up.
-        const int N = p.g.N;
-        if (p.mirror_ok && N % 64 == 0 && N % (2 * kWarps * ROWS) == 0 && gather_mirror_enabled())
+        if (mirror_applies(p, ROWS))
             return gather_w_mirror<WMAX, ROWS, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens,
                                                    d_err, st, z);
     }
