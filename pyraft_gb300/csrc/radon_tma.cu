@@ -77,7 +77,7 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
                                                    float *__restrict__ out_am, int out_ld,
                                                    const float *__restrict__ y_am, int y_ld,
                                                    long long zo, int *__restrict__ err,
-                                                   unsigned pb, int expire_first)
+                                                   unsigned pb, int expire_first, int split)
 {
     extern __shared__ __align__(128) float2 sbuf[];   // [2][kTmLines][BW]
     __shared__ __align__(8) unsigned long long full[2];
@@ -85,10 +85,16 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
     __shared__ int bad[2];                            // window did not fit
     __shared__ long long cr0[kTmViews], crk[kTmViews], cri[kTmViews];
     __shared__ int s_lo, s_hi;
+    __shared__ float red[kTmVpt][256];                 // cluster partials (split > 1)
 
     const StBlock blk = blocks[blockIdx.y];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int k0 = blockIdx.x * kTmRays;
+    // split > 1: this CTA is rank `rank` of a cluster of `split` CTAs along x
+    // that share the ray tile and view block; it walks its share of the
+    // strips, and rank 0 sums the partials (distributed shared memory, rank
+    // order) and writes the epilogue
+    const int rank = blockIdx.x % split;
+    const int k0 = (blockIdx.x / split) * kTmRays;
     constexpr int kRG = 32 / RPL;
     static_assert(RPL == 32 || RPL == 16 || RPL == 8, "rays per load");
     // pair m: ray k0 + 32 (warp & 1) + RPL (m % kRG) + lane % RPL,
@@ -151,8 +157,10 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
     for (int v = 0; v < kTmVpt; ++v) acc[v] = comp[v] = 0.f;
 
     if (Lo <= Hi) {
-        const int sfirst = Lo / kTmLines;
-        const int nstrips = Hi / kTmLines - sfirst + 1;
+        const int nall = Hi / kTmLines - Lo / kTmLines + 1;
+        const int s0 = (int)((long long)nall * rank / split);
+        const int sfirst = Lo / kTmLines + s0;
+        const int nstrips = (int)((long long)nall * (rank + 1) / split) - s0;
         const unsigned sbase = smem_addr(sbuf);
         constexpr unsigned kBufBytes = kTmLines * BW * 8;
 
@@ -185,7 +193,7 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
             }
         };
 
-        if (warp == 0) issue(0);
+        if (warp == 0 && nstrips > 0) issue(0);
         int n = 0;
         bool failed = false;
         for (; n < nstrips; ++n) {
@@ -238,11 +246,32 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
         }
     }
 
+    float tot[kTmVpt];
+#pragma unroll
+    for (int v = 0; v < kTmVpt; ++v) tot[v] = acc[v] - comp[v];
+    if (split > 1) {
+        namespace cg = cooperative_groups;
+        cg::cluster_group cl = cg::this_cluster();
+#pragma unroll
+        for (int v = 0; v < kTmVpt; ++v) red[v][threadIdx.x] = tot[v];
+        cl.sync();
+        if (rank == 0) {
+#pragma unroll
+            for (int v = 0; v < kTmVpt; ++v) tot[v] = 0.f;
+            for (int src = 0; src < split; ++src) {
+                const float *peer = cl.map_shared_rank(&red[0][0], src);
+#pragma unroll
+                for (int v = 0; v < kTmVpt; ++v) tot[v] += peer[v * 256 + threadIdx.x];
+            }
+        }
+        cl.sync();    // no CTA leaves while rank 0 still reads its partials
+        if (rank != 0) return;
+    }
 #pragma unroll
     for (int v = 0; v < kTmVpt; ++v) {
         if (vv_[v] >= blk.count || kk_[v] >= R) continue;
         const View &V = views[blk.first + vv_[v]];
-        const float val = (acc[v] - comp[v]) * V.delta;
+        const float val = tot[v] * V.delta;
         out_am[(size_t)V.view * out_ld + kk_[v]] =
             radon_epilogue(EPI, val, y_am, (size_t)V.view * y_ld + kk_[v]);
     }
@@ -386,6 +415,23 @@ static int radon_rpl()
     return (v == 32 || v == 16 || v == 8) ? v : 8;
 }
 
+// Cluster size of the strip split for a grid of `ctas` CTAs at `slots`
+// resident CTAs.  Measured on GB300 (GUPS, split 1 / 2 / 4): 2048^2 x 1800
+// (8.1 waves unsplit) 3352 / 3383 / 3155; 1536^2 x 1080 3021 / 3131 / 2974;
+// 1024^2 x 1440 2737 / 2821 / 2630; 1024^2 x 720 (1.6 waves) 2452 / 2665 /
+// 2609; 512^2 x 360 1171 / 1449 / 1472.  Each rank repeats the CTA's set-up
+// (about 6 % of a CTA's work at 2048^2), which outweighs the fuller last
+// wave of a split of 4, so: 2 while the unsplit grid is under 10 waves and
+// each rank keeps at least 4 strips of kTmLines lines, else 1 (a stack of
+// 64 slices of 512^2 runs 26 waves).  RG_RADON_SPLIT_TMA=1|2|4 forces it.
+static int tma_pick_split(long long ctas, int slots, int N)
+{
+    const char *e = getenv("RG_RADON_SPLIT_TMA");
+    const int forced = e ? atoi(e) : 0;
+    if (forced == 1 || forced == 2 || forced == 4) return forced;
+    return (ctas < 10LL * slots && (N / kTmLines) / 2 >= 4) ? 2 : 1;
+}
+
 template <int EPI, int BW, int RPL>
 static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensorMap &tc,
                           float *out_am, int out_ld, const float *y_am, int y_ld, int nz,
@@ -395,10 +441,40 @@ static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensor
     auto k = k_radon_tma<EPI, BW, RPL>;
     RG_CK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((p.g.R + kTmRays - 1) / kTmRays, p.nblocks, nz);
-    k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
-                               out_am, out_ld, y_am, y_ld, zo, d_err, (unsigned)sizeof(float2),
-                               test_switch("RG_TEST_EXPIRE_WAIT") ? 1 : 0);
-    RG_CK_LAUNCH("k_radon_tma");
+    // resident CTAs of this instantiation (cached: no queries in a capture)
+    static int slots = 0;
+    if (!slots) {
+        int dev = 0, sms = 0, per = 0;
+        RG_CK(cudaGetDevice(&dev));
+        RG_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        RG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, 256, smem));
+        slots = std::max(1, per) * sms;
+    }
+    const int split = tma_pick_split((long long)grid.x * grid.y * grid.z, slots, p.g.N);
+    const int expire = test_switch("RG_TEST_EXPIRE_WAIT") ? 1 : 0;
+    if (split == 1) {
+        k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
+                                   out_am, out_ld, y_am, y_ld, zo, d_err, (unsigned)sizeof(float2),
+                                   expire, 1);
+        RG_CK_LAUNCH("k_radon_tma");
+        return RG_OK;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = split;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    RG_CK(cudaLaunchKernelEx(&cfg, k, tr, tc, p.g.N, (const View *)p.d_views,
+                             (const StBlock *)p.d_blocks, p.g.R, out_am, out_ld, y_am, y_ld, zo,
+                             d_err, (unsigned)sizeof(float2), expire, split));
+    RG_CK_LAUNCH("k_radon_tma (cluster)");
     return RG_OK;
 }
 

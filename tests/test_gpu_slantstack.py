@@ -609,3 +609,29 @@ def test_em_osem_on_mirrored_tiles(orc, monkeypatch):
         return orc.radon_slantstack_transpose(full, n)
     want = orc.osem_interleaved(y, np.ones((n, n)), fsub, asub, S, 3)
     assert rel(got[0], want) <= 1e-4
+
+
+@pytest.mark.parametrize("n,a", [(256, 360), (128, 200), (512, 90)])
+def test_radon_tma_strip_split(orc, monkeypatch, n, a):
+    """The TMA-staged Radon with its strips split over a cluster of 2 or 4
+    CTAs (the partials meet in distributed shared memory, rank 0 writes the
+    epilogue) against the unsplit launch (1e-6: the ranks' compensated
+    partials are added in rank order) and the oracle (1e-5); also through
+    EM, whose Radon carries the ratio epilogue."""
+    rng = np.random.default_rng(3 * n + a)
+    x = interior_image(rng, n)
+    outs = {}
+    for sp in ("1", "2", "4"):
+        monkeypatch.setenv("RG_RADON_SPLIT_TMA", sp)
+        outs[sp] = np.asarray(rg.radon(rg.image(x), (n, a), SLANT))
+    assert _native.load().rg_device_status() == 0
+    ref = orc.radon_slantstack(x, n, a)
+    for sp in ("2", "4"):
+        assert rel(outs[sp], outs["1"]) <= 1e-6
+    assert rel(outs["4"], ref) <= 1e-5
+    y = np.maximum(ref, 0.0) + 0.1
+    em = {}
+    for sp in ("1", "4"):
+        monkeypatch.setenv("RG_RADON_SPLIT_TMA", sp)
+        em[sp] = np.asarray(rg.em(sino_img(y), (n, n), 3, method=SLANT))
+    assert rel(em["4"], em["1"]) <= 1e-5
