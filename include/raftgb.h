@@ -104,7 +104,8 @@ int rg_radon_slantstack(rg_image phantom, rg_image radon,
  * views and as many rays) or more than 4096 views are rejected with
  * RG_EINVAL.  The first call on a device (and the first after its context
  * was replaced) resolves the array's device address with
- * cudaGetSymbolAddress.  Calls share the array, so calls that overlap on
+ * cudaGetSymbolAddress; make that first call before any stream capture
+ * begins on the device.  Calls share the array, so calls that overlap on
  * the GPU race; each call rewrites all the scratch it reads, so nothing
  * needs clearing between calls.                                             */
 int rg_radon_slantstack_noalloc(rg_image phantom, rg_image radon, void *stream);

@@ -6,11 +6,13 @@
 // kernels on the caller's stream.  No entry point synchronises, except the
 // *_host wrappers and rg_dda_trace.
 #include <cuda_runtime.h>
+#include <ctype.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <complex>
@@ -66,7 +68,11 @@ int scratch_begin(Scratch &s, void *ws, size_t ws_bytes, size_t need, cudaStream
         s.size = ws_bytes;
         return RG_OK;
     }
-    cudaError_t e = cudaMallocAsync((void **)&s.base, need, st);
+    // RG_TEST_FAIL_ALLOC=1 (a test switch) makes this allocation fail as an
+    // exhausted pool would, so tests can see the call report RG_ENOMEM and
+    // leave its output and the library's state untouched
+    cudaError_t e = test_switch("RG_TEST_FAIL_ALLOC") ? cudaErrorMemoryAllocation
+                                                      : cudaMallocAsync((void **)&s.base, need, st);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_error(RG_ENOMEM, "stream-ordered allocation of %zu bytes failed: %s", need,
@@ -297,25 +303,144 @@ static bool is_view_major(const rg_image &s)
 }
 
 // ----------------------------------------------------------------------------
-// Autotuner for the gather tile height (rows per thread: 4 -> 32x32 tiles,
-// 8 -> 32x64 tiles, 16 -> 32x128 tiles).  The first out-of-place backprojection or adjoint of a
-// geometry times the three variants on the caller's own buffers (two timed
-// runs each, CUDA events on the caller's stream; this first call
-// synchronises) and keeps the fastest for the process.  Calls that never
-// tune (inside a stream capture, the EM drivers' fused-update gathers) use
-// the cached choice, or a default by image size: 16 rows from N = 512 up
-// (the measured best on GB300 at 512^2, 1024^2 and 2048^2), 8 from 128, else
-// 4.  The environment variable RG_GATHER_ROWS=4|8|16 forces a choice.
+// Autotuner for the gathers' launch shape: rows per thread (4 -> 32x32
+// tiles, 8 -> 32x64, 16 -> 32x128) and the cluster view split (1, 2 or 4
+// CTAs per tile).  The first out-of-place backprojection or adjoint of a
+// geometry (and the first EM/OSEM run, for its gathers) times the variants
+// on the caller's own buffers, CUDA events on the caller's stream, the
+// median of three timed runs after one warm-up (this first call
+// synchronises), and keeps the fastest for the process.  For each tile
+// height the occupancy rule's split (gather_pick_split) is timed first and
+// another split replaces it only when it is at least 2 % faster, so that
+// timing noise does not move a launch away from the rule; the tile height
+// with the fastest time wins.  Stacks of the geometry take the same choice
+// (tuned on one slice), so their members equal separate calls bit for bit.
+// Calls that never tune (inside a stream capture) use the cached choice, or
+// a default by image size: 16 rows from N = 512 up (the measured best on
+// GB300 at 512^2, 1024^2 and 2048^2), 8 from 128, else 4, with the rule's
+// split.  RG_GATHER_ROWS=4|8|16 and RG_GATHER_SPLIT=1|2|4 force a choice.
+//
+// RG_TUNE_CACHE=<file> keeps the choices across processes: the file is a
+// JSON object, read when a process first needs a choice and rewritten
+// (through a temporary file and a rename) after each new tuning, with one
+// entry per line,
+//     "<GPU name>|sm<cc>|<bp|adj>|N<size>|R<rays>|V<views>|W<windows>":
+//         {"rows": 8, "split": 1}
+// (split 0 stands for the occupancy rule).  Summation order depends on the
+// split, so runs that must agree bit for bit across processes (a resumed EM)
+// pin it with the cache or the two variables.  Processes that tune the same
+// file at the same time may drop each other's new entries.
 
 static std::mutex g_tune_mu;
-static std::map<std::string, int> g_tune;
+static std::map<std::string, TuneChoice> g_tune;
+static bool g_tune_loaded = false;
+
+static std::string device_tag()
+{
+    static std::mutex mu;
+    static std::map<int, std::string> tags;
+    const int d = current_device();
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = tags.find(d);
+    if (it != tags.end()) return it->second;
+    cudaDeviceProp pr;
+    std::string t = "gpu";
+    if (cudaGetDeviceProperties(&pr, d) == cudaSuccess) {
+        t = pr.name;
+        for (char &c : t)
+            if (c == '"' || c == '\\' || c == '|' || (unsigned char)c < 32) c = '_';
+        t += "|sm" + std::to_string(pr.major * 10 + pr.minor);
+    } else {
+        cudaGetLastError();
+    }
+    tags[d] = t;
+    return t;
+}
 
 static std::string tune_key(const SSPlan &p, int mode)
 {
-    KeyBuilder kb;
-    kb.add(current_device()).add(mode == 2 ? 1 : mode).add(p.g.N).add(p.g.R).add(p.nv)
-        .add(p.wmax_bp[0]).add(p.wmax_adj[0]);
-    return kb.s;
+    char b[160];
+    snprintf(b, sizeof b, "|%s|N%d|R%d|V%d|W%d,%d", mode == 0 ? "bp" : "adj", p.g.N, p.g.R, p.nv,
+             p.wmax_bp[0], p.wmax_adj[0]);
+    return device_tag() + b;
+}
+
+static const char *tune_cache_path()
+{
+    const char *e = getenv("RG_TUNE_CACHE");
+    return (e && *e) ? e : nullptr;
+}
+
+// Integer value of "name" inside the JSON object text [b, e), or -1.
+static int json_int_field(const std::string &t, size_t b, size_t e, const char *name)
+{
+    const std::string key = std::string("\"") + name + "\"";
+    const size_t k = t.find(key, b);
+    if (k == std::string::npos || k >= e) return -1;
+    size_t i = k + key.size();
+    while (i < e && (t[i] == ' ' || t[i] == '\t' || t[i] == '\n' || t[i] == '\r')) ++i;
+    if (i >= e || t[i] != ':') return -1;
+    ++i;
+    while (i < e && (t[i] == ' ' || t[i] == '\t' || t[i] == '\n' || t[i] == '\r')) ++i;
+    if (i >= e || t[i] < '0' || t[i] > '9') return -1;
+    return atoi(t.c_str() + i);
+}
+
+// Caller holds g_tune_mu.  Reads every "key": {"rows": r, "split": s} pair
+// of the file, whatever its layout; anything else (a truncated or foreign
+// file) is skipped.
+static void tune_cache_load()
+{
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char *path = tune_cache_path();
+    FILE *f = path ? fopen(path, "r") : nullptr;
+    if (!f) return;
+    std::string t;
+    char buf[4096];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof buf, f)) > 0 && t.size() < (1u << 24)) t.append(buf, n);
+    fclose(f);
+    size_t pos = 0;
+    while (true) {
+        const size_t q1 = t.find('"', pos);
+        if (q1 == std::string::npos) break;
+        const size_t q2 = t.find('"', q1 + 1);
+        if (q2 == std::string::npos) break;
+        pos = q2 + 1;
+        size_t i = q2 + 1;
+        while (i < t.size() && isspace((unsigned char)t[i])) ++i;
+        if (i >= t.size() || t[i] != ':') continue;
+        ++i;
+        while (i < t.size() && isspace((unsigned char)t[i])) ++i;
+        if (i >= t.size() || t[i] != '{') continue;
+        const size_t e = t.find('}', i);
+        if (e == std::string::npos) break;
+        const int rows = json_int_field(t, i, e, "rows");
+        const int split = json_int_field(t, i, e, "split");
+        if ((rows == 4 || rows == 8 || rows == 16) &&
+            (split == 0 || split == 1 || split == 2 || split == 4))
+            g_tune.emplace(t.substr(q1 + 1, q2 - q1 - 1), TuneChoice{rows, split});
+        pos = e + 1;
+    }
+}
+
+// Caller holds g_tune_mu.  A file that cannot be written is left alone: the
+// choices still hold for this process.
+static void tune_cache_save()
+{
+    const char *path = tune_cache_path();
+    if (!path) return;
+    const std::string tmp = std::string(path) + ".tmp" + std::to_string((long long)getpid());
+    FILE *f = fopen(tmp.c_str(), "w");
+    if (!f) return;
+    fprintf(f, "{\n");
+    size_t i = 0;
+    for (const auto &kv : g_tune)
+        fprintf(f, "  \"%s\": {\"rows\": %d, \"split\": %d}%s\n", kv.first.c_str(),
+                kv.second.rows, kv.second.split, ++i < g_tune.size() ? "," : "");
+    fprintf(f, "}\n");
+    if (fclose(f) != 0 || rename(tmp.c_str(), path) != 0) remove(tmp.c_str());
 }
 
 static int env_rows()
@@ -326,22 +451,25 @@ static int env_rows()
     return (v == 4 || v == 8 || v == 16) ? v : 0;
 }
 
-int tuned_rows(const SSPlan &p, int mode)
+TuneChoice tuned_choice(const SSPlan &p, int mode)
 {
-    if (int v = env_rows()) return v;
+    if (int v = env_rows()) return {v, 0};
+    const std::string key = tune_key(p, mode);
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    auto it = g_tune.find(tune_key(p, mode));
+    tune_cache_load();
+    auto it = g_tune.find(key);
     if (it != g_tune.end()) return it->second;
-    return p.g.N >= 512 ? 16 : p.g.N >= 128 ? 8 : 4;
+    return {p.g.N >= 512 ? 16 : p.g.N >= 128 ? 8 : 4, 0};
 }
 
-static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
-                           long long cs, long long ls, cudaStream_t st, void *quads = nullptr)
+int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
+                    long long cs, long long ls, cudaStream_t st, void *quads)
 {
     if (env_rows()) return RG_OK;
     const std::string key = tune_key(p, mode);
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
+        tune_cache_load();
         if (g_tune.count(key)) return RG_OK;
     }
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -350,28 +478,49 @@ static int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_l
     cudaEvent_t a, b;
     RG_CK(cudaEventCreate(&a));
     RG_CK(cudaEventCreate(&b));
-    float best = 1e30f;
-    int pick = 4, rc = RG_OK;
-    for (int rows : {4, 8, 16}) {
-        float tsum = 0.f;
-        for (int rep = 0; rep < 3 && !rc; ++rep) {
+    // median of three timed runs after a warm-up
+    auto time_one = [&](int rows, int split, float &med) {
+        SplitPref pref(split);
+        float t[3];
+        for (int rep = 0; rep < 4; ++rep) {
             cudaEventRecord(a, st);
-            rc = launch_gather(p, mode, s_am, s_ld, out, cs, ls, nullptr, nullptr, nullptr, st, rows,
-                               Stack(), quads);
+            int rc = launch_gather(p, mode, s_am, s_ld, out, cs, ls, nullptr, nullptr, nullptr, st,
+                                   rows, Stack(), quads);
             cudaEventRecord(b, st);
             cudaError_t e = cudaEventSynchronize(b);
             if (!rc && e != cudaSuccess) rc = cuda_error(e, "autotune");
+            if (rc) return rc;
             float ms = 0.f;
             cudaEventElapsedTime(&ms, a, b);
-            if (rep > 0) tsum += ms;
+            if (rep > 0) t[rep - 1] = ms;
         }
-        if (!rc && tsum < best) { best = tsum; pick = rows; }
+        std::sort(t, t + 3);
+        med = t[1];
+        return (int)RG_OK;
+    };
+    float best = 1e30f;
+    TuneChoice pick{4, 0};
+    int rc = RG_OK;
+    for (int rows : {4, 8, 16}) {
+        float t_rule = 0.f;
+        if ((rc = time_one(rows, 0, t_rule))) break;
+        TuneChoice c{rows, 0};
+        float t_c = t_rule;
+        for (int split : {1, 2, 4}) {
+            float t = 0.f;
+            if (rows % split) continue;
+            if ((rc = time_one(rows, split, t))) break;
+            if (t < 0.98f * t_rule && t < t_c) { t_c = t; c.split = split; }
+        }
+        if (rc) break;
+        if (t_c < best) { best = t_c; pick = c; }
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc) return rc;
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tune[key] = pick;
+    tune_cache_save();
     return RG_OK;
 }
 
@@ -428,6 +577,7 @@ size_t rg_radon_slantstack_workspace(rg_image phantom, rg_image radon)
 
 int rg_radon_slantstack(rg_image phantom, rg_image radon, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc = check_ss(phantom, radon);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -463,6 +613,7 @@ int rg_radon_slantstack_stack(rg_image phantom, long long phantom_stride, rg_ima
                               long long radon_stride, int nstack, void *ws, size_t wsb,
                               void *stream)
 {
+    RG_TRACE();
     int rc = check_ss(phantom, radon);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -501,6 +652,7 @@ int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg
                                         long long image_stride, int nstack, void *ws, size_t wsb,
                                         void *stream)
 {
+    RG_TRACE();
     int rc = check_ss(image, sino);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -551,6 +703,7 @@ static rg_image as_f32_view(const rg_image_f64 &d)
 
 int rg_radon_slantstack_f64(rg_image_f64 phantom, rg_image_f64 radon, void *stream)
 {
+    RG_TRACE();
     const rg_image a = as_f32_view(phantom), b = as_f32_view(radon);
     int rc = check_ss(a, b);
     if (rc) return rc;
@@ -563,6 +716,7 @@ int rg_radon_slantstack_f64(rg_image_f64 phantom, rg_image_f64 radon, void *stre
 
 int rg_radon_transpose_slantstack_f64(rg_image_f64 sino, rg_image_f64 image, void *stream)
 {
+    RG_TRACE();
     const rg_image a = as_f32_view(image), b = as_f32_view(sino);
     int rc = check_ss(a, b);
     if (rc) return rc;
@@ -620,6 +774,7 @@ size_t rg_backprojection_slantstack_workspace(rg_image sino, rg_image bp)
 
 int rg_backprojection_slantstack(rg_image sino, rg_image bp, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     return run_gather(0, sino, bp, ws, wsb, stream);
 }
 
@@ -631,6 +786,7 @@ size_t rg_radon_transpose_slantstack_workspace(rg_image sino, rg_image img)
 
 int rg_radon_transpose_slantstack(rg_image sino, rg_image img, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     return run_gather(1, sino, img, ws, wsb, stream);
 }
 
@@ -801,6 +957,7 @@ size_t rg_filter_workspace(rg_image sino, int kind)
 
 int rg_filter(rg_image in, rg_image out, int kind, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc;
     if ((rc = check_image(in, "input sinogram")) || (rc = check_image(out, "output sinogram")))
         return rc;
@@ -833,6 +990,7 @@ size_t rg_fbp_workspace(rg_image sino, rg_image image, int kind)
 
 int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc = check_ss(image, sino);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -921,6 +1079,7 @@ size_t rg_radon_bresenham_workspace(rg_image image, rg_image sino)
 
 int rg_radon_bresenham(rg_image image, rg_image sino, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc = check_dda(image, sino);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -951,6 +1110,7 @@ size_t rg_radon_transpose_bresenham_workspace(rg_image sino, rg_image image)
 
 int rg_radon_transpose_bresenham(rg_image sino, rg_image image, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc = check_dda(image, sino);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -981,6 +1141,7 @@ size_t rg_backprojection_bresenham_workspace(rg_image sino, rg_image image)
 
 int rg_backprojection_bresenham(rg_image sino, rg_image image, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc = check_dda(image, sino);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;
@@ -1011,6 +1172,7 @@ int rg_dda_trace(int lines, int columns, const double img_corners[4], const doub
                  const double *ts, int n, int cap, int *oi, int *oj, double *os, int *ocount,
                  void *stream)
 {
+    RG_TRACE();
     if (lines < 2 || columns < 2 || n < 0 || cap < 0 || !img_corners || (n > 0 && (!thetas || !ts)))
         return set_error(RG_EINVAL, "rg_dda_trace: bad arguments");
     if (n == 0) return RG_OK;
@@ -1038,6 +1200,7 @@ int rg_dda_trace(int lines, int columns, const double img_corners[4], const doub
 int rg_tv(const float *x, int nslices, int size, float eps, double *value, float *grad,
           void *stream)
 {
+    RG_TRACE();
     if (!x || !value) return set_error(RG_EINVAL, "rg_tv: null pointer");
     if (nslices < 1 || nslices > 65535 || size < 1)
         return set_error(RG_EINVAL, "rg_tv: need 1 <= nslices <= 65535 and size >= 1");
@@ -1048,6 +1211,7 @@ int rg_tv(const float *x, int nslices, int size, float eps, double *value, float
 // ---------------------------------------------------------------- phantoms
 int rg_phantom_fromdesc(rg_image image, const double *desc, int n, void *stream)
 {
+    RG_TRACE();
     int rc = check_image(image, "image");
     if (rc) return rc;
     if (n < 0 || (n > 0 && !desc)) return set_error(RG_EINVAL, "bad ellipse table");
@@ -1077,6 +1241,7 @@ int rg_phantom_fromdesc(rg_image image, const double *desc, int n, void *stream)
 
 int rg_radon_fromdesc(rg_image sino, const double *desc, int n, void *stream)
 {
+    RG_TRACE();
     int rc = check_image(sino, "sinogram");
     if (rc) return rc;
     if (n < 0 || (n > 0 && !desc)) return set_error(RG_EINVAL, "bad ellipse table");
@@ -1159,17 +1324,20 @@ static int host_call(int op, float *h_out, const float *h_in, int size, int nray
 
 int rg_radon_slantstack_host(float *h_output, const float *h_input, int size, int nrays, int nangles)
 {
+    RG_TRACE();
     return host_call(0, h_output, h_input, size, nrays, nangles, 0);
 }
 
 int rg_backprojection_slantstack_host(float *h_image, const float *h_sino, int size, int nrays,
                                       int nangles)
 {
+    RG_TRACE();
     return host_call(1, h_image, h_sino, size, nrays, nangles, 0);
 }
 
 int rg_em_host(float *h_output, const float *h_sino, int size, int nrays, int nangles, int niter)
 {
+    RG_TRACE();
     return host_call(2, h_output, h_sino, size, nrays, nangles, niter);
 }
 

@@ -583,6 +583,7 @@ size_t rg_osem_batch_workspace(const rg_image *sinos, const rg_image *images, in
 int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int niter, int nsubsets,
                   int graph, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     if (nslices < 0 || (nslices > 0 && (!sinos || !images)))
         return set_error(RG_EINVAL, "rg_osem_batch: bad slice arrays");
     if (niter < 0) return set_error(RG_EINVAL, "rg_osem_batch: niter < 0");
@@ -769,6 +770,7 @@ int rg_osem_batch(const rg_image *sinos, rg_image *images, int nslices, int nite
 int rg_em_plain_host(float *h_out, const float *h_sino, int size, int nrays, int nangles,
                      int niter, int nsubsets)
 {
+    RG_TRACE();
     if (!h_out || !h_sino || size < 2 || nrays < 2 || nangles < 1 || niter < 0 || nsubsets < 1 ||
         nsubsets > nangles)
         return set_error(RG_EINVAL, "rg_em_plain_host: bad arguments");

@@ -147,7 +147,12 @@ static int em_ss_core(const SSGeom &g, long long first, long long count, int S,
     bool any_rot = false;
     for (int k = 0; k < S; ++k) any_rot = any_rot || plans[k]->rot_ok;
     const bool fused = any_rot && gather_rot_enabled() && em_fusable(N) && !em_unfused();
-    int rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
+    // launch shape of each plan's gathers: timed on the first run of a
+    // geometry outside a stream capture, on gsum (zeroed below)
+    int rc = RG_OK;
+    for (int k = 0; k < S && !rc; ++k)
+        rc = autotune_gather(*plans[k], bp ? 0 : 1, y_am, R, gsum, N, 1, st, quads);
+    if (!rc) rc = launch_fill(ratio, (size_t)R * A, 1.f, st);
     if (!rc && fused) rc = launch_fill(gsum, (size_t)N * N, 0.f, st);
     if (!rc && fused) RG_CK(cudaMemsetAsync(fuse.cnt, 0, cb, st));
     for (int k = 0; k < S && !rc; ++k) {
@@ -322,6 +327,7 @@ size_t rg_em_transmission_workspace(rg_image rawsino, rg_image image)
 int rg_em_transmission(rg_image rawsino, rg_image flat, rg_image dark, rg_image image, int niter,
                        void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     if (!rawsino.data || !flat.data || !image.data)
         return set_error(RG_EINVAL, "rg_em_transmission: null data pointer");
     if (niter < 0) return set_error(RG_EINVAL, "rg_em_transmission: niter < 0");
@@ -376,6 +382,7 @@ static int em_range(rg_image sino, rg_image image, int method, int nsubsets, lon
 int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, void *ws,
           size_t wsb, void *stream)
 {
+    RG_TRACE();
     if (niter < 0) return set_error(RG_EINVAL, "rg_em: niter < 0");
     const long long S = nsubsets < 1 ? 1 : nsubsets;
     return em_range(sino, image, method, nsubsets, 0, (long long)niter * S, ws, wsb, stream);
@@ -384,6 +391,7 @@ int rg_em(rg_image sino, rg_image image, int method, int niter, int nsubsets, vo
 int rg_em_subiterations(rg_image sino, rg_image image, int method, int nsubsets, long long first,
                         long long count, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     if (first < 0 || count < 0)
         return set_error(RG_EINVAL, "rg_em_subiterations: first and count must be >= 0");
     return em_range(sino, image, method, nsubsets, first, count, ws, wsb, stream);

@@ -85,6 +85,7 @@ int rg_radon_slantstack_withmesh(rg_image phantom, long long phantom_stride, rg_
                                  long long radon_stride, int nstack, const double *t,
                                  const double *theta, void *ws, size_t wsb, void *stream)
 {
+    RG_TRACE();
     int rc = validate_ss(phantom, radon);
     if (!rc) rc = check_ws(ws);
     if (rc) return rc;

@@ -20,7 +20,8 @@
 // Host code cannot use the array's name as a device address (it names a
 // host-side shadow), so the first call on each device, with that device
 // current, looks up the device address with cudaGetSymbolAddress and caches
-// it together with the identity of the device's current context.  A call
+// it together with the identity of the device's current context; that first
+// call should come before any stream capture begins on the device.  A call
 // that finds another context there (the old one was destroyed, e.g. by
 // cudaDeviceReset, and the module loaded again) looks the address up anew.
 //
@@ -120,6 +121,7 @@ using namespace rg;
 
 extern "C" int rg_radon_slantstack_noalloc(rg_image phantom, rg_image radon, void *stream)
 {
+    RG_TRACE();
     int rc = validate_ss(phantom, radon);
     if (rc) return rc;
     const int N = phantom.lines, R = radon.lines, A = radon.columns;

@@ -20,9 +20,25 @@
 #include <initializer_list>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/raftgb.h"
 
 namespace rg {
+
+// ----------------------------------------------------------------------------
+// Tracing.  Every compute entry point of the C ABI opens an NVTX range named
+// after itself for the duration of the call (host side: argument checks,
+// plan look-up and the launches it enqueues), so a profiler's timeline shows
+// which library call issued which kernels.  NVTX is header-only; without a
+// profiler attached a range costs a few nanoseconds.
+struct TraceRange {
+    explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+};
+#define RG_TRACE() ::rg::TraceRange rg_trace_range_(__func__)
 
 // ----------------------------------------------------------------------------
 // Per-view constants (one per view of a plan, device resident).
@@ -54,8 +70,9 @@ int set_error(int code, const char *fmt, ...);
 int cuda_error(cudaError_t e, const char *what);
 // True when environment variable `name` is "1" (read per call).  Used for the
 // failure-path test switches RG_TEST_EXPIRE_WAIT (the first mbarrier wait of
-// every CTA of the TMA kernels gives up at once) and RG_TEST_WINDOW_CUT (the
-// TMA gather under-reports its window bound); neither is set in normal use.
+// every CTA of the TMA kernels gives up at once), RG_TEST_WINDOW_CUT (the
+// TMA gather under-reports its window bound) and RG_TEST_FAIL_ALLOC (the
+// stream-ordered scratch allocation fails); none is set in normal use.
 inline bool test_switch(const char *name)
 {
     const char *e = getenv(name);
@@ -237,11 +254,36 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld,
 // Bytes of the paired gathers' quad scratch for nz problems of nv views over
 // R rays: a 16-byte quad per (view pair, sample entry), R + 1 entries.
 size_t gather_quads_bytes(int nv, int R, int nz);
-// Rows per thread picked for (geometry, mode) by the autotuner (api.cu).
-int tuned_rows(const SSPlan &p, int mode);
+// The gather launch shape picked for (geometry, mode) by the autotuner
+// (api.cu): rows per thread and the cluster view split (0: the occupancy
+// rule of gather_pick_split).
+struct TuneChoice {
+    int rows;
+    int split;
+};
+TuneChoice tuned_choice(const SSPlan &p, int mode);
+inline int tuned_rows(const SSPlan &p, int mode) { return tuned_choice(p, mode).rows; }
+// Times the gather variants of (plan, mode) on the caller's buffers the first
+// time a geometry is seen outside a stream capture (out is overwritten) and
+// caches the fastest (api.cu).  quads as for launch_gather.
+int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
+                    long long cs, long long ls, cudaStream_t st, void *quads = nullptr);
 // Cluster size (1, 2 or 4) for the view split of a gather kernel k launched
-// on `grid` with `smem` bytes of shared memory (slantstack.cu).
+// on `grid` with `smem` bytes of shared memory (slantstack.cu): the calling
+// thread's preference (SplitPref) where the kernel can run it, else the
+// occupancy rule.
 int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st);
+// Scoped split preference of the calling thread for the gather launches it
+// makes (0: none); launch_gather sets the tuned one, the autotuner each
+// candidate.
+int split_preference();
+struct SplitPref {
+    explicit SplitPref(int split);
+    ~SplitPref();
+    SplitPref(const SplitPref &) = delete;
+    SplitPref &operator=(const SplitPref &) = delete;
+    int saved;
+};
 // Backprojection (mode 0) or matched adjoint (mode 1, interior pixels: the
 // edge pixels are left to the caller) with views paired a quarter turn
 // apart (p.rot_ok).  Two partial sums are added to each pixel of an output

@@ -428,13 +428,18 @@ static int adjoint_edges(const SSPlan &p, const float *s_am, int s_ld, float *ou
     return RG_OK;
 }
 
-// Cluster size for the view split of a gather launch of `tiles` CTAs: the
-// split in {1, 2, 4} (ROWS divisible by it, >= 64 views per rank) whose
-// last wave is fullest, from the occupancy of the kernel (clusters counted
-// by cudaOccupancyMaxActiveClusters).  Occupancies are cached per kernel, so
-// launches inside a stream capture make no queries once the plain call has
-// run; an uncached query during a capture gives split 1.
-// RG_GATHER_SPLIT=1|2|4 forces a choice.
+// Cluster size for the view split of a gather launch of `tiles` CTAs.  The
+// calling thread's preference (the autotuner's choice for the geometry, or
+// the candidate it is timing) is taken where ROWS is divisible by it, every
+// rank keeps 16 views and the kernel's clusters fit; otherwise the occupancy
+// rule: the split in {1, 2, 4} (ROWS divisible by it, >= 64 views per rank)
+// whose last wave is fullest, from the occupancy of the kernel (clusters
+// counted by cudaOccupancyMaxActiveClusters), on the tiles of one slice:
+// the split changes the summation order, so it follows the geometry alone
+// and a stack's members equal separate calls bit for bit.  Occupancies are
+// cached per kernel, so launches inside a stream capture make no queries
+// once the plain call has run; an uncached query during a capture gives
+// split 1.  RG_GATHER_SPLIT=1|2|4 forces a choice.
 struct SplitOcc {
     int slots[3] = {0, 0, 0};      // concurrent CTAs at split 1, 2, 4
 };
@@ -454,6 +459,12 @@ static int pick_split(K k, size_t smem, int rows, int nv, dim3 grid, cudaStream_
 {
     return gather_pick_split((const void *)k, smem, rows, nv, grid, st);
 }
+
+static thread_local int t_split_pref = 0;
+
+int split_preference() { return t_split_pref; }
+SplitPref::SplitPref(int split) : saved(t_split_pref) { t_split_pref = split; }
+SplitPref::~SplitPref() { t_split_pref = saved; }
 
 int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, cudaStream_t st)
 {
@@ -502,7 +513,17 @@ int gather_pick_split(const void *k, size_t smem, int rows, int nv, dim3 grid, c
         std::lock_guard<std::mutex> lock(g_occ_mu);
         g_occ[key] = occ;
     }
-    const double tiles = (double)grid.x * grid.y * grid.z;
+    // a preferred split (the autotuner's) where every rank keeps 16 views
+    // and the clusters fit on the device
+    const int pref = t_split_pref;
+    if (pref == 1) return 1;
+    if (pref == 2 || pref == 4) {
+        const int t = pref == 2 ? 1 : 2;
+        if (rows % pref == 0 && nv >= 16 * pref && occ.slots[t] > 0) return pref;
+    }
+    // one slice's tiles: the split follows the geometry alone, so a stack
+    // (grid z) sums in the same order as separate calls
+    const double tiles = (double)grid.x * grid.y;
     int best = 1;
     double best_e = 0.0;
     for (int t = 0; t < 3; ++t) {
@@ -651,7 +672,16 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                   long long cs, long long ls, float *em_x, const float *inv_sens, int *d_err,
                   cudaStream_t st, int rows, Stack z, void *quads, const EmFuse *fuse)
 {
-    if (rows == 0) rows = tuned_rows(p, mode);
+    // launch shape: the caller's rows and split preference, else the tuned
+    // choice for this geometry (a stack takes the one-slice choice, so its
+    // members come out as separate calls would give them)
+    int pref = split_preference();
+    if (rows == 0) {
+        const TuneChoice c = tuned_choice(p, mode);
+        rows = c.rows;
+        pref = c.split;
+    }
+    SplitPref use_split(pref);
     // the kernels OR their error bits (window checks, bounded waits) into the
     // device's status word, which rg_device_status() reads and clears
     if (!d_err) d_err = device_error_word();

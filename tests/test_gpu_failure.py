@@ -108,3 +108,31 @@ def test_window_too_narrow_reports_bit_1(orc, lib, monkeypatch):
     out = rg.backprojection(sino, plan)
     assert lib.rg_device_status() == 0
     assert rel(out, orc.backprojection_slantstack(s, n)) <= 1e-5
+
+
+def test_failed_scratch_allocation_reports_enomem(orc, lib, monkeypatch):
+    """A call given no workspace takes its scratch from the stream-ordered
+    pool.  RG_TEST_FAIL_ALLOC=1 makes that allocation fail as an exhausted
+    pool would: the call returns RG_ENOMEM with a message and writes nothing,
+    and the next call on the same context allocates and matches the oracle."""
+    from pyraft_gb300.raftypes import gpu_image, rg_image
+    n, a = 96, 80
+    x = _image(n, 5)
+    d_x = torch.from_numpy(x.astype(np.float32)).cuda()
+    out = torch.full((n, a), float("nan"), dtype=torch.float32, device="cuda")
+    X = rg_image(gpu_image(d_x))
+    S = rg_image(gpu_image(out, (0.0, 1.0), (math.pi, -1.0)))
+    stream = torch.cuda.current_stream().cuda_stream
+    monkeypatch.setenv("RG_TEST_FAIL_ALLOC", "1")
+    assert lib.rg_radon_slantstack(X, S, None, 0, stream) == _native.RG_ENOMEM
+    assert b"allocation" in lib.rg_last_error()
+    img = torch.full((n, n), float("nan"), dtype=torch.float32, device="cuda")
+    I = rg_image(gpu_image(img))
+    assert lib.rg_fbp(S, I, _native.RG_FILTER_RAMLAK, None, 0, stream) == _native.RG_ENOMEM
+    torch.cuda.synchronize()
+    assert torch.isnan(out).all() and torch.isnan(img).all()
+    monkeypatch.delenv("RG_TEST_FAIL_ALLOC")
+    assert lib.rg_radon_slantstack(X, S, None, 0, stream) == _native.RG_OK
+    torch.cuda.synchronize()
+    assert lib.rg_device_status() == 0
+    assert rel(out.cpu().numpy(), orc.radon_slantstack(x, n, a)) <= 1e-5
