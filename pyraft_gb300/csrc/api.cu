@@ -43,6 +43,15 @@ int set_error(int code, const char *fmt, ...)
     return code;
 }
 
+bool pdl_enabled()
+{
+    static const bool on = [] {
+        const char *e = getenv("RG_PDL");
+        return !(e && !strcmp(e, "0"));
+    }();
+    return on;
+}
+
 int cuda_error(cudaError_t e, const char *what)
 {
     return set_error(RG_ECUDA, "%s: %s", what, cudaGetErrorString(e));
@@ -313,8 +322,11 @@ static bool is_view_major(const rg_image &s)
 // height the occupancy rule's split (gather_pick_split) is timed first and
 // another split replaces it only when it is at least 2 % faster, so that
 // timing noise does not move a launch away from the rule; the tile height
-// with the fastest time wins.  Stacks of the geometry take the same choice
-// (tuned on one slice), so their members equal separate calls bit for bit.
+// with the fastest time wins.  One choice holds per geometry, whether the
+// call is one slice or a stack (a stack call times the candidates on the
+// whole stack, whose larger grid may favour another split), so that a
+// stack's members equal separate calls bit for bit; the call that first
+// meets a geometry sets it.
 // Calls that never tune (inside a stream capture) use the cached choice, or
 // a default by image size: 16 rows from N = 512 up (the measured best on
 // GB300 at 512^2, 1024^2 and 2048^2), 8 from 128, else 4, with the rule's
@@ -463,7 +475,7 @@ TuneChoice tuned_choice(const SSPlan &p, int mode)
 }
 
 int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
-                    long long cs, long long ls, cudaStream_t st, void *quads)
+                    long long cs, long long ls, cudaStream_t st, void *quads, const Stack &z)
 {
     if (env_rows()) return RG_OK;
     const std::string key = tune_key(p, mode);
@@ -485,7 +497,7 @@ int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, floa
         for (int rep = 0; rep < 4; ++rep) {
             cudaEventRecord(a, st);
             int rc = launch_gather(p, mode, s_am, s_ld, out, cs, ls, nullptr, nullptr, nullptr, st,
-                                   rows, Stack(), quads);
+                                   rows, z, quads);
             cudaEventRecord(b, st);
             cudaError_t e = cudaEventSynchronize(b);
             if (!rc && e != cudaSuccess) rc = cuda_error(e, "autotune");
@@ -679,10 +691,10 @@ int rg_radon_transpose_slantstack_stack(rg_image sino, long long sino_stride, rg
     zz.n = nstack;
     zz.in = zs;
     zz.out = image_stride;
-    // tile height tuned on the first slice (its output is rewritten below)
+    // launch shape tuned on the whole stack (its output is rewritten below)
     if (!rc)
         rc = autotune_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
-                             st, quads);
+                             st, quads, zz);
     if (!rc)
         rc = launch_gather(ph->p, 1, s_am, R, image.data, image.column_stride, image.line_stride,
                            nullptr, nullptr, nullptr, st, 0, zz, quads);

@@ -20,6 +20,7 @@ __global__ __launch_bounds__(256) void k_to_am(const float *__restrict__ in, lon
                                                float *__restrict__ out, long long zi,
                                                long long zo)
 {
+    pdl_gate();
     in += blockIdx.z * zi;
     out += blockIdx.z * zo;
     __shared__ float t[32][33];
@@ -43,6 +44,7 @@ __global__ __launch_bounds__(256) void k_from_am(const float *__restrict__ am, i
                                                  float *__restrict__ out, long long cs,
                                                  long long ls, long long zi, long long zo)
 {
+    pdl_gate();
     am += blockIdx.z * zi;
     out += blockIdx.z * zo;
     __shared__ float t[32][33];
@@ -66,7 +68,7 @@ int launch_to_am(const float *in, long long cs, long long ls, int R, int A, floa
                  cudaStream_t st, int nz, long long zi, long long zo)
 {
     dim3 grid((A + 31) / 32, (R + 31) / 32, nz);
-    k_to_am<<<grid, 256, 0, st>>>(in, cs, ls, R, A, out_am, zi, zo);
+    RG_CK(launch_pdl(k_to_am, grid, 256, 0, st, 1, in, cs, ls, R, A, out_am, zi, zo));
     RG_CK_LAUNCH("k_to_am");
     return RG_OK;
 }
@@ -75,7 +77,7 @@ int launch_from_am(const float *am, int R, int A, float *out, long long cs, long
                    cudaStream_t st, int nz, long long zi, long long zo)
 {
     dim3 grid((A + 31) / 32, (R + 31) / 32, nz);
-    k_from_am<false><<<grid, 256, 0, st>>>(am, R, A, out, cs, ls, zi, zo);
+    RG_CK(launch_pdl(k_from_am<false>, grid, 256, 0, st, 1, am, R, A, out, cs, ls, zi, zo));
     RG_CK_LAUNCH("k_from_am");
     return RG_OK;
 }
@@ -84,7 +86,7 @@ int launch_add_from_am(const float *am, int R, int A, float *out, long long cs, 
                        cudaStream_t st)
 {
     dim3 grid((A + 31) / 32, (R + 31) / 32, 1);
-    k_from_am<true><<<grid, 256, 0, st>>>(am, R, A, out, cs, ls, 0, 0);
+    RG_CK(launch_pdl(k_from_am<true>, grid, 256, 0, st, 1, am, R, A, out, cs, ls, 0, 0));
     RG_CK_LAUNCH("k_from_am (add)");
     return RG_OK;
 }
@@ -92,6 +94,7 @@ int launch_add_from_am(const float *am, int R, int A, float *out, long long cs, 
 __global__ void k_copy2d(const float *__restrict__ in, long long ics, long long ils,
                          float *__restrict__ out, long long ocs, long long ols, int rows, int cols)
 {
+    pdl_gate();
     const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
     if (c < cols) out[(long long)r * ocs + (long long)c * ols] = in[(long long)r * ics + (long long)c * ils];
 }
@@ -101,13 +104,14 @@ int launch_copy2d(const float *in, long long ics, long long ils, float *out, lon
 {
     if (rows <= 0 || cols <= 0) return RG_OK;
     dim3 grid((cols + 255) / 256, rows);
-    k_copy2d<<<grid, 256, 0, st>>>(in, ics, ils, out, ocs, ols, rows, cols);
+    RG_CK(launch_pdl(k_copy2d, grid, 256, 0, st, 1, in, ics, ils, out, ocs, ols, rows, cols));
     RG_CK_LAUNCH("k_copy2d");
     return RG_OK;
 }
 
 __global__ void k_fill(float *p, size_t n, float v)
 {
+    pdl_gate();
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
          e += (size_t)gridDim.x * blockDim.x)
         p[e] = v;
@@ -117,7 +121,7 @@ int launch_fill(float *p, size_t n, float v, cudaStream_t st)
 {
     if (n == 0) return RG_OK;
     int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-    k_fill<<<blocks, 256, 0, st>>>(p, n, v);
+    RG_CK(launch_pdl(k_fill, blocks, 256, 0, st, 1, p, n, v));
     RG_CK_LAUNCH("k_fill");
     return RG_OK;
 }
@@ -218,6 +222,7 @@ namespace rg {
 __global__ void k_em_update(float *__restrict__ x, const float *__restrict__ bp,
                             const float *__restrict__ inv, size_t n)
 {
+    pdl_gate();
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
          e += (size_t)gridDim.x * blockDim.x)
         x[e] = x[e] * bp[e] * inv[e];
@@ -225,6 +230,7 @@ __global__ void k_em_update(float *__restrict__ x, const float *__restrict__ bp,
 
 __global__ void k_invert(const float *__restrict__ s, float *__restrict__ inv, size_t n)
 {
+    pdl_gate();
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n;
          e += (size_t)gridDim.x * blockDim.x)
         inv[e] = (s[e] > 0.f) ? 1.f / s[e] : 0.f;
@@ -251,7 +257,7 @@ int launch_em_update(float *x, const float *bp, const float *inv, size_t n, cuda
 {
     if (n == 0) return RG_OK;
     int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-    k_em_update<<<blocks, 256, 0, st>>>(x, bp, inv, n);
+    RG_CK(launch_pdl(k_em_update, blocks, 256, 0, st, 1, x, bp, inv, n));
     RG_CK_LAUNCH("k_em_update");
     return RG_OK;
 }
@@ -260,7 +266,7 @@ int launch_invert(const float *sens, float *inv, size_t n, cudaStream_t st)
 {
     if (n == 0) return RG_OK;
     int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
-    k_invert<<<blocks, 256, 0, st>>>(sens, inv, n);
+    RG_CK(launch_pdl(k_invert, blocks, 256, 0, st, 1, sens, inv, n));
     RG_CK_LAUNCH("k_invert");
     return RG_OK;
 }

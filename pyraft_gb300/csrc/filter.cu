@@ -25,6 +25,7 @@ constexpr int kTN = 256, kTK = 256, kNA = 16;
 __global__ __launch_bounds__(256) void k_conv_rows(const float *__restrict__ in, float *__restrict__ out,
                                                    int R, int A, const float *__restrict__ taps)
 {
+    pdl_gate();
     __shared__ float4 sx[kTK][kNA / 4];
     __shared__ float sh[kTN + kTK];
     const int t = threadIdx.x;
@@ -84,7 +85,7 @@ int launch_conv_rows(const float *in_am, float *out_am, int R, int A, const floa
                      cudaStream_t st)
 {
     dim3 grid((R + kTN - 1) / kTN, (A + kNA - 1) / kNA);
-    k_conv_rows<<<grid, 256, 0, st>>>(in_am, out_am, R, A, d_taps);
+    RG_CK(launch_pdl(k_conv_rows, grid, 256, 0, st, 1, in_am, out_am, R, A, d_taps));
     RG_CK_LAUNCH("k_conv_rows");
     return RG_OK;
 }
@@ -119,6 +120,7 @@ __global__ __launch_bounds__(256) void k_ramlak_rows(const float *__restrict__ i
                                                      float *__restrict__ out, int R, int A,
                                                      const float *__restrict__ godd, float h0)
 {
+    pdl_gate();
     __shared__ float4 sxe[kRK / 2];             // even inputs of the tile, 4 views
     __shared__ float4 sxo[kRK / 2];             // odd inputs
     __shared__ float sg0[kRT / 2], sg1[kRT / 2];  // staged taps: index 2i -> sg0[i], 2i+1 -> sg1[i]
@@ -202,7 +204,7 @@ int launch_ramlak_rows(const float *in_am, float *out_am, int R, int A, const fl
                        float h0, cudaStream_t st)
 {
     dim3 grid((R + kRN - 1) / kRN, (A + kRA - 1) / kRA);
-    k_ramlak_rows<<<grid, 256, 0, st>>>(in_am, out_am, R, A, d_godd, h0);
+    RG_CK(launch_pdl(k_ramlak_rows, grid, 256, 0, st, 1, in_am, out_am, R, A, d_godd, h0));
     RG_CK_LAUNCH("k_ramlak_rows");
     return RG_OK;
 }
@@ -402,6 +404,7 @@ __global__ __launch_bounds__(kFftThreads) void k_filter_fft(const float *__restr
                                                             int p, const float2 *__restrict__ tab,
                                                             float g0, bool circ)
 {
+    pdl_gate();
     extern __shared__ __align__(16) float2 z[];          // [M + M/16]
     __shared__ float2 wsum[kFftThreads / 32];
     const int M = 1 << p, H = M >> 1, t = threadIdx.x;
@@ -501,8 +504,8 @@ int launch_filter_fft(const float *in_am, float *out_am, int R, int A, int p, co
     const size_t smem = sizeof(float2) * (((size_t)1 << p) + ((size_t)1 << p) / 16);
     RG_CK(cudaFuncSetAttribute(k_filter_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
-    k_filter_fft<<<(A + 1) / 2, kFftThreads, smem, st>>>(in_am, out_am, R, A, p, d_tab, g0,
-                                                         circ);
+    RG_CK(launch_pdl(k_filter_fft, (A + 1) / 2, kFftThreads, smem, st, 1, in_am, out_am, R, A, p, d_tab, g0,
+                                                         circ));
     RG_CK_LAUNCH("k_filter_fft");
     return RG_OK;
 }

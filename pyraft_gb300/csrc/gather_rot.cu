@@ -73,6 +73,7 @@ constexpr int kTmaMinPairs = 256;
 __global__ void k_zero_image(float *__restrict__ out, int N, long long cs, long long ls,
                              long long zo)
 {
+    pdl_gate();
     out += (long long)blockIdx.z * zo;
     const long long n = (long long)N * N;
     for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < n;
@@ -403,6 +404,7 @@ __global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_
                                                     float *__restrict__ em_x,
                                                     const float *__restrict__ em_inv, int *em_cnt)
 {
+    pdl_gate();
     extern __shared__ __align__(16) float2 pairs[];  // [kPairSlots][WMAX] x {view, partner}
     gather_tile_rot<MODE, WMAX, ROWS, EMF>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
                                 out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
@@ -429,6 +431,7 @@ __global__ void k_pair_quads(const float *__restrict__ s_am, int s_ld, long long
                              float4 *__restrict__ quads, float *__restrict__ zout, int N,
                              long long cs, long long ls, long long zo)
 {
+    pdl_gate();
     if (zout) {
         const long long n = (long long)N * N;
         const long long nt = (long long)gridDim.x * gridDim.y * blockDim.x;
@@ -490,6 +493,7 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
                                                         const float *__restrict__ em_inv,
                                                         int *em_cnt)
 {
+    pdl_gate();
     extern __shared__ __align__(128) float4 qbuf[];   // [kStages][kPairSlots][wb]
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ SlotInfo slot[kStages][kPairSlots];
@@ -612,27 +616,10 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
     const unsigned pb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
-    if (split == 1) {
-        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, half, roff, N, scale, out, cs, ls,
-                                   d_err, z.in, z.out, pb, 1, ex, ei, ec);
-        RG_CK_LAUNCH("k_gather_rot");
-        return RG_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, half, roff, N,
-                             scale, out, cs, ls, d_err, z.in, z.out, pb, split, ex, ei, ec));
-    RG_CK_LAUNCH("k_gather_rot (cluster)");
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+                     s_am, s_ld, p.g.R, (const View *)p.d_views, half, roff, N,
+                     scale, out, cs, ls, d_err, z.in, z.out, pb, split, ex, ei, ec));
+    RG_CK_LAUNCH("k_gather_rot");
     return RG_OK;
 }
 
@@ -651,8 +638,8 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const int Rq = quad_entries(MODE, R);
     {
         dim3 g((Rq + 255) / 256, half, z.n);
-        k_pair_quads<MODE><<<g, 256, 0, st>>>(s_am, s_ld, z.in, R, p.d_views, half, roff, quads,
-                                              zero_out ? out : nullptr, N, cs, ls, z.out);
+        RG_CK(launch_pdl(k_pair_quads<MODE>, g, 256, 0, st, 1, s_am, s_ld, z.in, R, p.d_views, half, roff, quads,
+                                              zero_out ? out : nullptr, N, cs, ls, z.out));
         RG_CK_LAUNCH("k_pair_quads");
     }
     // RG_TEST_WINDOW_CUT=1 (a test switch) under-reports the window bound by
@@ -683,27 +670,10 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
     const unsigned qb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
-    if (split == 1) {
-        k<<<grid, 256, smem, st>>>(tm, p.d_views, half, N, scale, out, cs, ls, d_err, z.out, wb,
-                                   qb, 1, expire, ex, ei, ec);
-        RG_CK_LAUNCH("k_gather_rot_tma");
-        return RG_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
-                             d_err, z.out, wb, qb, split, expire, ex, ei, ec));
-    RG_CK_LAUNCH("k_gather_rot_tma (cluster)");
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+                     tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
+                     d_err, z.out, wb, qb, split, expire, ex, ei, ec));
+    RG_CK_LAUNCH("k_gather_rot_tma");
     return RG_OK;
 }
 
@@ -745,7 +715,7 @@ int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_
 {
     const long long n = (long long)N * N;
     const int blocks = (int)std::min<long long>((n + 255) / 256, 4096);
-    k_zero_image<<<dim3(blocks, 1, z.n), 256, 0, st>>>(out, N, cs, ls, z.out);
+    RG_CK(launch_pdl(k_zero_image, dim3(blocks, 1, z.n), 256, 0, st, 1, out, N, cs, ls, z.out));
     RG_CK_LAUNCH("k_zero_image");
     return RG_OK;
 }

@@ -79,6 +79,7 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
                                                    long long zo, int *__restrict__ err,
                                                    unsigned pb, int expire_first, int split)
 {
+    pdl_gate();
     extern __shared__ __align__(128) float2 sbuf[];   // [2][kTmLines][BW]
     __shared__ __align__(8) unsigned long long full[2];
     __shared__ int xs[2];                             // window start entry per buffer
@@ -452,29 +453,11 @@ static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensor
     }
     const int split = tma_pick_split((long long)grid.x * grid.y * grid.z, slots, p.g.N);
     const int expire = test_switch("RG_TEST_EXPIRE_WAIT") ? 1 : 0;
-    if (split == 1) {
-        k<<<grid, 256, smem, st>>>(tr, tc, p.g.N, p.d_views, (const StBlock *)p.d_blocks, p.g.R,
-                                   out_am, out_ld, y_am, y_ld, zo, d_err, (unsigned)sizeof(float2),
-                                   expire, 1);
-        RG_CK_LAUNCH("k_radon_tma");
-        return RG_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, tr, tc, p.g.N, (const View *)p.d_views,
-                             (const StBlock *)p.d_blocks, p.g.R, out_am, out_ld, y_am, y_ld, zo,
-                             d_err, (unsigned)sizeof(float2), expire, split));
-    RG_CK_LAUNCH("k_radon_tma (cluster)");
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+                     tr, tc, p.g.N, (const View *)p.d_views,
+                     (const StBlock *)p.d_blocks, p.g.R, out_am, out_ld, y_am, y_ld, zo,
+                     d_err, (unsigned)sizeof(float2), expire, split));
+    RG_CK_LAUNCH("k_radon_tma");
     return RG_OK;
 }
 
@@ -550,6 +533,7 @@ __global__ __launch_bounds__(256) void k_radon_tiles(const __grid_constant__ CUt
                                                      long long zo, int *__restrict__ err,
                                                      unsigned pb)
 {
+    pdl_gate();
     extern __shared__ __align__(128) float2 tile[];   // [kTtLines][kTtRow]
     __shared__ __align__(8) unsigned long long full;
     const int o = blockIdx.z & 1, z = blockIdx.z >> 1;
@@ -597,6 +581,7 @@ __global__ __launch_bounds__(256) void k_views_rows(const View *__restrict__ vie
                                                     const float *__restrict__ y_am, int y_ld,
                                                     long long zo)
 {
+    pdl_gate();
     const int k = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
     if (k >= R || j >= nv) return;
     const int view = views[j].view;
@@ -664,24 +649,24 @@ int launch_radon_tiles(const SSPlan &p, const float2 *prow, const float2 *pcol, 
     if (!rc) rc = encode_pairs_map(&tc, pcol, N, nz, zp, kTtWin, 1);
     if (rc) return rc;
     const dim3 gv((R + 255) / 256, p.nv, nz);
-    k_views_rows<kEpiSum, true><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am, out_ld, nullptr,
-                                                    0, zo);
+    RG_CK(launch_pdl(k_views_rows<kEpiSum, true>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am, out_ld, nullptr,
+                                                    0, zo));
     RG_CK_LAUNCH("k_views_rows (zero)");
     const size_t smem = (size_t)kTtLines * kTtRow * 8;
     RG_CK(cudaFuncSetAttribute(k_radon_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
     const dim3 grid((pairs_pitch(N) + kTtWin - 1) / kTtWin, (N + kTtLines - 1) / kTtLines,
                     2 * nz);
-    k_radon_tiles<<<grid, 256, smem, st>>>(tr, tc, N, (const TtView *)p.d_ovid,
+    RG_CK(launch_pdl(k_radon_tiles, grid, 256, smem, st, 1, tr, tc, N, (const TtView *)p.d_ovid,
                                            p.n_ovid[0], p.n_ovid[1], R, out_am, out_ld, zo,
-                                           device_error_word(), (unsigned)sizeof(float2));
+                                           device_error_word(), (unsigned)sizeof(float2)));
     RG_CK_LAUNCH("k_radon_tiles");
     if (epi == kEpiRatio)
-        k_views_rows<kEpiRatio, false><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am, out_ld,
-                                                           y_am, y_ld, zo);
+        RG_CK(launch_pdl(k_views_rows<kEpiRatio, false>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am, out_ld,
+                                                           y_am, y_ld, zo));
     else if (epi == kEpiTransmission)
-        k_views_rows<kEpiTransmission, false><<<gv, 256, 0, st>>>(p.d_views, p.nv, R, out_am,
-                                                                  out_ld, y_am, y_ld, zo);
+        RG_CK(launch_pdl(k_views_rows<kEpiTransmission, false>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am,
+                                                                  out_ld, y_am, y_ld, zo));
     RG_CK_LAUNCH("k_views_rows (epilogue)");
     return RG_OK;
 }

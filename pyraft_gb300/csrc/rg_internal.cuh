@@ -18,6 +18,7 @@
 #include <stdlib.h>
 
 #include <initializer_list>
+#include <utility>
 #include <string>
 
 #include <nvtx3/nvToolsExt.h>
@@ -90,6 +91,61 @@ inline bool test_switch(const char *name)
         cudaError_t e_ = cudaGetLastError();                            \
         if (e_ != cudaSuccess) return ::rg::cuda_error(e_, what);       \
     } while (0)
+
+// ----------------------------------------------------------------------------
+// Programmatic dependent launch.  The operators run as chains of short
+// kernels on one stream (an EM/OSEM sub-iteration is five or six).  A kernel
+// launched by launch_pdl may be scheduled while the kernel before it on the
+// stream is still finishing its last wave: its CTAs are dispatched and reach
+// pdl_gate(), which first lets the next kernel be scheduled the same way and
+// then waits (griddepcontrol.wait) until the preceding grid has completed and
+// its memory operations are visible.  Every kernel launched by launch_pdl
+// calls pdl_gate() before it touches global memory, so the stream's order is
+// kept exactly; what overlaps is launch latency and the dispatch of CTAs
+// into the previous kernel's tail.  A dependent grid is scheduled only once
+// every CTA of its predecessor has started, so waiting CTAs never keep a
+// predecessor's CTAs off the GPU.  For a kernel launched without the
+// attribute (or after a copy or another library's kernel) the gate returns
+// at once.  RG_PDL=0 (read once per process) launches without the
+// attribute.
+bool pdl_enabled();
+__device__ __forceinline__ void pdl_gate()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Launch kernel k (which begins with pdl_gate()) on `grid` x `block` with
+// `smem` bytes of dynamic shared memory on stream st, in clusters of
+// `cluster` CTAs along x when cluster > 1, with programmatic dependent
+// launch unless RG_PDL=0.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       int cluster, Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[2];
+    unsigned na = 0;
+    if (pdl_enabled()) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    if (cluster > 1) {
+        at[na].id = cudaLaunchAttributeClusterDimension;
+        at[na].val.clusterDim.x = (unsigned)cluster;
+        at[na].val.clusterDim.y = 1;
+        at[na].val.clusterDim.z = 1;
+        ++na;
+    }
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = na ? at : nullptr;
+    cfg.numAttrs = na;
+    return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 // Bump allocator over one scratch block (caller's workspace or a
 // stream-ordered allocation that is released on the same stream).
@@ -263,11 +319,13 @@ struct TuneChoice {
 };
 TuneChoice tuned_choice(const SSPlan &p, int mode);
 inline int tuned_rows(const SSPlan &p, int mode) { return tuned_choice(p, mode).rows; }
-// Times the gather variants of (plan, mode) on the caller's buffers the first
-// time a geometry is seen outside a stream capture (out is overwritten) and
-// caches the fastest (api.cu).  quads as for launch_gather.
+// Times the gather variants of (plan, mode) on the caller's buffers (a
+// stack of z.n problems when z says so) the first time a geometry is seen
+// outside a stream capture (out is overwritten) and caches the fastest
+// (api.cu).  quads as for launch_gather.
 int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
-                    long long cs, long long ls, cudaStream_t st, void *quads = nullptr);
+                    long long cs, long long ls, cudaStream_t st, void *quads = nullptr,
+                    const Stack &z = Stack());
 // Cluster size (1, 2 or 4) for the view split of a gather kernel k launched
 // on `grid` with `smem` bytes of shared memory (slantstack.cu): the calling
 // thread's preference (SplitPref) where the kernel can run it, else the

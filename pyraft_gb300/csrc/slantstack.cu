@@ -199,6 +199,7 @@ __global__ __launch_bounds__(256) void k_line_pairs(const float *__restrict__ im
                                                     float2 *__restrict__ pcol, long long zi,
                                                     long long zp)
 {
+    pdl_gate();
     line_pairs_tile(img + blockIdx.z * zi, cs, ls, N, prow + blockIdx.z * zp,
                     pcol + blockIdx.z * zp, blockIdx.x, blockIdx.y);
 }
@@ -207,7 +208,7 @@ int launch_line_pairs(const float *img, long long cs, long long ls, int N, float
                       float2 *pcol, cudaStream_t st, int nz, long long zi, long long zp)
 {
     dim3 grid((N + 31) / 32, (N + 31) / 32, nz);
-    k_line_pairs<<<grid, 256, 0, st>>>(img, cs, ls, N, prow, pcol, zi, zp);
+    RG_CK(launch_pdl(k_line_pairs, grid, 256, 0, st, 1, img, cs, ls, N, prow, pcol, zi, zp));
     RG_CK_LAUNCH("k_line_pairs");
     return RG_OK;
 }
@@ -220,6 +221,7 @@ __global__ __launch_bounds__(128) void k_radon(const float2 *__restrict__ prow,
                                                const float *__restrict__ y_am, int y_ld,
                                                long long zp, long long zo, int split)
 {
+    pdl_gate();
     radon_tile<EPI>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
                     out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x / split, blockIdx.y,
                     split, blockIdx.x % split);
@@ -276,26 +278,10 @@ static int launch_radon_direct1(const SSPlan &p, const float2 *prow, const float
     dim3 grid((R + 31) / 32, (p.nv + 3) / 4, nz);
     auto k = k_radon<EPI>;
     const int split = radon_split(k, (long long)grid.x * grid.y * grid.z, st);
-    if (split == 1) {
-        k<<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am, out_ld, y_am, y_ld,
-                                zp, zo, 1);
-        RG_CK_LAUNCH("k_radon");
-        return RG_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
-    cfg.blockDim = dim3(128);
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, prow, pcol, N, (const View *)p.d_views, p.nv, R, out_am,
-                             out_ld, y_am, y_ld, zp, zo, split));
-    RG_CK_LAUNCH("k_radon (cluster)");
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 128, 0, st, split,
+                     prow, pcol, N, (const View *)p.d_views, p.nv, R, out_am,
+                     out_ld, y_am, y_ld, zp, zo, split));
+    RG_CK_LAUNCH("k_radon");
     return RG_OK;
 }
 
@@ -307,6 +293,7 @@ __global__ __launch_bounds__(128) void k_radon2(const float2 *__restrict__ prow,
                                                 const float *__restrict__ y_am, int y_ld,
                                                 long long zp, long long zo)
 {
+    pdl_gate();
     radon_tile2<EPI>(prow + blockIdx.z * zp, pcol + blockIdx.z * zp, N, views, nv, R,
                        out_am + blockIdx.z * zo, out_ld, y_am, y_ld, blockIdx.x, blockIdx.y);
 }
@@ -332,14 +319,14 @@ int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float 
     if (radon_views_per_thread(p) == 2) {
         dim3 grid((R + 31) / 32, (p.nv + 7) / 8, nz);
         if (epi == kEpiRatio)
-            k_radon2<kEpiRatio><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
-                                                      out_ld, y_am, y_ld, zp, zo);
+            RG_CK(launch_pdl(k_radon2<kEpiRatio>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views, p.nv, R, out_am,
+                                                      out_ld, y_am, y_ld, zp, zo));
         else if (epi == kEpiTransmission)
-            k_radon2<kEpiTransmission><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R,
-                                                             out_am, out_ld, y_am, y_ld, zp, zo);
+            RG_CK(launch_pdl(k_radon2<kEpiTransmission>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views, p.nv, R,
+                                                             out_am, out_ld, y_am, y_ld, zp, zo));
         else
-            k_radon2<kEpiSum><<<grid, 128, 0, st>>>(prow, pcol, N, p.d_views, p.nv, R, out_am,
-                                                    out_ld, nullptr, 0, zp, zo);
+            RG_CK(launch_pdl(k_radon2<kEpiSum>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views, p.nv, R, out_am,
+                                                    out_ld, nullptr, 0, zp, zo));
         RG_CK_LAUNCH("k_radon2");
         return RG_OK;
     }
@@ -363,6 +350,7 @@ __global__ __launch_bounds__(256) void k_gather(const float *__restrict__ s_am, 
                                                 int *__restrict__ err, long long zs,
                                                 long long zo, unsigned pair_bytes, int split)
 {
+    pdl_gate();
     extern __shared__ float2 pairs[];          // [kSlots][WMAX]
     gather_tile<MODE, WMAX, ROWS, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, scale,
                                       out + blockIdx.z * zo, cs, ls, em_x, inv_sens, err,
@@ -383,6 +371,7 @@ __global__ __launch_bounds__(256, 4) void k_gather_mirror(
     const float *__restrict__ inv_sens, int *__restrict__ err, long long zs, long long zo,
     unsigned quad_bytes, int split)
 {
+    pdl_gate();
     extern __shared__ __align__(16) float4 mq[];   // [kSlots / 2][WMAX], or 2 ROWS x 256 floats
     gather_tile_mirror<WMAX, ROWS, EM>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N,
                                        out + blockIdx.z * zo, cs, ls, em_x, inv_sens, err,
@@ -411,6 +400,7 @@ __global__ __launch_bounds__(1024) void k_adjoint_edges(const float *__restrict_
                                                        const float *__restrict__ inv_sens,
                                                        long long zs, long long zo)
 {
+    pdl_gate();
     adjoint_edge_group<MODE, EM, 32>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, blockIdx.x * 32,
                                  out + blockIdx.z * zo, cs, ls, em_x, inv_sens);
 }
@@ -422,8 +412,8 @@ static int adjoint_edges(const SSPlan &p, const float *s_am, int s_ld, float *ou
 {
     const int N = p.g.N;
     dim3 grid((4 * N - 4 + 31) / 32, 1, z.n);   // 32 edge pixels per CTA
-    k_adjoint_edges<MODE, EM><<<grid, 1024, 0, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs,
-                                                    ls, em_x, inv_sens, z.in, z.out);
+    RG_CK(launch_pdl(k_adjoint_edges<MODE, EM>, grid, 1024, 0, st, 1, s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs,
+                                                    ls, em_x, inv_sens, z.in, z.out));
     RG_CK_LAUNCH("k_adjoint_edges");
     return RG_OK;
 }
@@ -560,27 +550,10 @@ static int gather_w_mirror(const SSPlan &p, const float *s_am, int s_ld, float *
     const int split = pick_split(k, smem, ROWS, p.nv, grid, st);
     const unsigned qb = (unsigned)sizeof(float4);
     if (int rc = adjoint_edges<1, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, st, z)) return rc;
-    if (split == 1) {
-        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs, ls, em_x,
-                                   inv_sens, d_err, z.in, z.out, qb, 1);
-        RG_CK_LAUNCH("k_gather_mirror");
-        return RG_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, p.nv, N, out, cs,
-                             ls, em_x, inv_sens, d_err, z.in, z.out, qb, split));
-    RG_CK_LAUNCH("k_gather_mirror (cluster)");
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+                     s_am, s_ld, p.g.R, (const View *)p.d_views, p.nv, N, out, cs,
+                     ls, em_x, inv_sens, d_err, z.in, z.out, qb, split));
+    RG_CK_LAUNCH("k_gather_mirror");
     return RG_OK;
 }
 
@@ -608,27 +581,10 @@ static int gather_w(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
         if (int rc = adjoint_edges<MODE, EM>(p, s_am, s_ld, out, cs, ls, em_x, inv_sens, st, z))
             return rc;
     }
-    if (split == 1) {
-        k<<<grid, 256, smem, st>>>(s_am, s_ld, p.g.R, p.d_views, p.nv, p.g.N, scale, out, cs, ls,
-                                   em_x, inv_sens, d_err, z.in, z.out, pb, 1);
-        RG_CK_LAUNCH("k_gather");
-        return RG_OK;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = split;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(grid.x * split, grid.y, grid.z);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    RG_CK(cudaLaunchKernelEx(&cfg, k, s_am, s_ld, p.g.R, (const View *)p.d_views, p.nv, p.g.N,
-                             scale, out, cs, ls, em_x, inv_sens, d_err, z.in, z.out, pb, split));
-    RG_CK_LAUNCH("k_gather (cluster)");
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+                     s_am, s_ld, p.g.R, (const View *)p.d_views, p.nv, p.g.N,
+                     scale, out, cs, ls, em_x, inv_sens, d_err, z.in, z.out, pb, split));
+    RG_CK_LAUNCH("k_gather");
     return RG_OK;
 }
 
