@@ -341,11 +341,12 @@ def osem_compare(torch, rg, nslices, niter, nsubsets, plain_stride, seed=7, rank
     return res
 
 
-def em_run(torch, rg, n=1024, nviews=720, seed=5):
+def em_run(torch, rg, n=1024, nviews=720, seed=5, only=None, osem_iters=10):
     """Config-3 workload: 1024^2 emission slice (random ellipses), 720 views,
     1024 rays, Poisson counts with mean 50 per bin; plain EM 100 iterations
     vs OSEM 10 interleaved subsets x 10 iterations, x0 = 1, FP64
-    sensitivities.  One slice per call through rg_em."""
+    sensitivities.  One slice per call through rg_em.  only="em" or "osem"
+    runs one of the two (profiling); osem_iters sets the OSEM iterations."""
     import numpy as np
     from pyraft_gb300 import _native
     from pyraft_gb300.raftypes import rg_image
@@ -362,7 +363,8 @@ def em_run(torch, rg, n=1024, nviews=720, seed=5):
     X = rg_image(rg.gpu_image(x))
     sp = torch.cuda.current_stream().cuda_stream
     out = {}
-    for name, it, subsets in (("em_100", 100, 1), ("osem_10x10", 10, 10)):
+    runs = [("em_100", 100, 1), (f"osem_10x{osem_iters}", osem_iters, 10)]
+    for name, it, subsets in [r for r in runs if only is None or r[0].startswith(only)]:
         wsb = L.rg_em_workspace(S, X, _native.RG_SLANTSTACK, subsets)
         ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
         x.fill_(1.0)
@@ -434,6 +436,10 @@ def main():
                     help="timed runs of the whole batched OSEM (median)")
     ap.add_argument("--no-osem", action="store_true",
                     help="FBP line without its osem object (quick runs)")
+    ap.add_argument("--em-only", choices=["em", "osem"], default=None,
+                    help="--workload em: run only EM-100 or only the OSEM part (profiling)")
+    ap.add_argument("--osem-iters", type=int, default=10,
+                    help="--workload em: OSEM iterations (10 subsets each)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     warm = max(3, args.warmup)
@@ -445,7 +451,8 @@ def main():
         import pyraft_gb300 as rg
         torch.cuda.set_device(local)
         print(json.dumps({"workload": "EM 100 iterations vs OSEM 10x10, 1024^2, 720 views",
-                          **em_run(torch, rg)}))
+                          **em_run(torch, rg, only=args.em_only,
+                                   osem_iters=args.osem_iters)}))
         return
     if args.workload == "tvls":
         import torch

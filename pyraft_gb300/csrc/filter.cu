@@ -504,8 +504,8 @@ int launch_filter_fft(const float *in_am, float *out_am, int R, int A, int p, co
     const size_t smem = sizeof(float2) * (((size_t)1 << p) + ((size_t)1 << p) / 16);
     RG_CK(cudaFuncSetAttribute(k_filter_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
-    RG_CK(launch_pdl(k_filter_fft, (A + 1) / 2, kFftThreads, smem, st, 1, in_am, out_am, R, A, p, d_tab, g0,
-                                                         circ));
+    RG_CK(launch_pdl(k_filter_fft, (A + 1) / 2, kFftThreads, smem, st, 1, in_am, out_am, R, A, p,
+                     d_tab, g0, circ));
     RG_CK_LAUNCH("k_filter_fft");
     return RG_OK;
 }

@@ -638,8 +638,8 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const int Rq = quad_entries(MODE, R);
     {
         dim3 g((Rq + 255) / 256, half, z.n);
-        RG_CK(launch_pdl(k_pair_quads<MODE>, g, 256, 0, st, 1, s_am, s_ld, z.in, R, p.d_views, half, roff, quads,
-                                              zero_out ? out : nullptr, N, cs, ls, z.out));
+        RG_CK(launch_pdl(k_pair_quads<MODE>, g, 256, 0, st, 1, s_am, s_ld, z.in, R, p.d_views,
+                         half, roff, quads, zero_out ? out : nullptr, N, cs, ls, z.out));
         RG_CK_LAUNCH("k_pair_quads");
     }
     // RG_TEST_WINDOW_CUT=1 (a test switch) under-reports the window bound by

@@ -649,8 +649,8 @@ int launch_radon_tiles(const SSPlan &p, const float2 *prow, const float2 *pcol, 
     if (!rc) rc = encode_pairs_map(&tc, pcol, N, nz, zp, kTtWin, 1);
     if (rc) return rc;
     const dim3 gv((R + 255) / 256, p.nv, nz);
-    RG_CK(launch_pdl(k_views_rows<kEpiSum, true>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am, out_ld, nullptr,
-                                                    0, zo));
+    RG_CK(launch_pdl(k_views_rows<kEpiSum, true>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am,
+                     out_ld, nullptr, 0, zo));
     RG_CK_LAUNCH("k_views_rows (zero)");
     const size_t smem = (size_t)kTtLines * kTtRow * 8;
     RG_CK(cudaFuncSetAttribute(k_radon_tiles, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -658,15 +658,15 @@ int launch_radon_tiles(const SSPlan &p, const float2 *prow, const float2 *pcol, 
     const dim3 grid((pairs_pitch(N) + kTtWin - 1) / kTtWin, (N + kTtLines - 1) / kTtLines,
                     2 * nz);
     RG_CK(launch_pdl(k_radon_tiles, grid, 256, smem, st, 1, tr, tc, N, (const TtView *)p.d_ovid,
-                                           p.n_ovid[0], p.n_ovid[1], R, out_am, out_ld, zo,
-                                           device_error_word(), (unsigned)sizeof(float2)));
+                     p.n_ovid[0], p.n_ovid[1], R, out_am, out_ld, zo, device_error_word(),
+                     (unsigned)sizeof(float2)));
     RG_CK_LAUNCH("k_radon_tiles");
     if (epi == kEpiRatio)
-        RG_CK(launch_pdl(k_views_rows<kEpiRatio, false>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am, out_ld,
-                                                           y_am, y_ld, zo));
+        RG_CK(launch_pdl(k_views_rows<kEpiRatio, false>, gv, 256, 0, st, 1, p.d_views, p.nv, R,
+                         out_am, out_ld, y_am, y_ld, zo));
     else if (epi == kEpiTransmission)
-        RG_CK(launch_pdl(k_views_rows<kEpiTransmission, false>, gv, 256, 0, st, 1, p.d_views, p.nv, R, out_am,
-                                                                  out_ld, y_am, y_ld, zo));
+        RG_CK(launch_pdl(k_views_rows<kEpiTransmission, false>, gv, 256, 0, st, 1, p.d_views,
+                         p.nv, R, out_am, out_ld, y_am, y_ld, zo));
     RG_CK_LAUNCH("k_views_rows (epilogue)");
     return RG_OK;
 }

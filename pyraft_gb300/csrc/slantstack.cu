@@ -319,14 +319,14 @@ int launch_radon(const SSPlan &p, const float2 *prow, const float2 *pcol, float 
     if (radon_views_per_thread(p) == 2) {
         dim3 grid((R + 31) / 32, (p.nv + 7) / 8, nz);
         if (epi == kEpiRatio)
-            RG_CK(launch_pdl(k_radon2<kEpiRatio>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views, p.nv, R, out_am,
-                                                      out_ld, y_am, y_ld, zp, zo));
+            RG_CK(launch_pdl(k_radon2<kEpiRatio>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views,
+                             p.nv, R, out_am, out_ld, y_am, y_ld, zp, zo));
         else if (epi == kEpiTransmission)
-            RG_CK(launch_pdl(k_radon2<kEpiTransmission>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views, p.nv, R,
-                                                             out_am, out_ld, y_am, y_ld, zp, zo));
+            RG_CK(launch_pdl(k_radon2<kEpiTransmission>, grid, 128, 0, st, 1, prow, pcol, N,
+                             p.d_views, p.nv, R, out_am, out_ld, y_am, y_ld, zp, zo));
         else
-            RG_CK(launch_pdl(k_radon2<kEpiSum>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views, p.nv, R, out_am,
-                                                    out_ld, nullptr, 0, zp, zo));
+            RG_CK(launch_pdl(k_radon2<kEpiSum>, grid, 128, 0, st, 1, prow, pcol, N, p.d_views,
+                             p.nv, R, out_am, out_ld, nullptr, 0, zp, zo));
         RG_CK_LAUNCH("k_radon2");
         return RG_OK;
     }
@@ -412,8 +412,8 @@ static int adjoint_edges(const SSPlan &p, const float *s_am, int s_ld, float *ou
 {
     const int N = p.g.N;
     dim3 grid((4 * N - 4 + 31) / 32, 1, z.n);   // 32 edge pixels per CTA
-    RG_CK(launch_pdl(k_adjoint_edges<MODE, EM>, grid, 1024, 0, st, 1, s_am, s_ld, p.g.R, p.d_views, p.nv, N, out, cs,
-                                                    ls, em_x, inv_sens, z.in, z.out));
+    RG_CK(launch_pdl(k_adjoint_edges<MODE, EM>, grid, 1024, 0, st, 1, s_am, s_ld, p.g.R,
+                     p.d_views, p.nv, N, out, cs, ls, em_x, inv_sens, z.in, z.out));
     RG_CK_LAUNCH("k_adjoint_edges");
     return RG_OK;
 }
