@@ -510,18 +510,29 @@ int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, floa
         med = t[1];
         return (int)RG_OK;
     };
+    // A shape that the geometry does not support (a window too wide for the
+    // tile height) is skipped; any other failure ends the call.
     float best = 1e30f;
     TuneChoice pick{4, 0};
-    int rc = RG_OK;
+    int rc = RG_OK, unsupported = RG_OK;
     for (int rows : {4, 8, 16}) {
         float t_rule = 0.f;
-        if ((rc = time_one(rows, 0, t_rule))) break;
+        if ((rc = time_one(rows, 0, t_rule)) == RG_EUNSUPPORTED) {
+            unsupported = rc;
+            rc = RG_OK;
+            continue;
+        }
+        if (rc) break;
         TuneChoice c{rows, 0};
         float t_c = t_rule;
         for (int split : {1, 2, 4}) {
             float t = 0.f;
             if (rows % split) continue;
-            if ((rc = time_one(rows, split, t))) break;
+            if ((rc = time_one(rows, split, t)) == RG_EUNSUPPORTED) {
+                rc = RG_OK;
+                continue;
+            }
+            if (rc) break;
             if (t < 0.98f * t_rule && t < t_c) { t_c = t; c.split = split; }
         }
         if (rc) break;
@@ -530,6 +541,7 @@ int autotune_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, floa
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (rc) return rc;
+    if (best == 1e30f) return unsupported;   // no tile height fits this geometry
     std::lock_guard<std::mutex> lock(g_tune_mu);
     g_tune[key] = pick;
     tune_cache_save();
