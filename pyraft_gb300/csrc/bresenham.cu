@@ -224,6 +224,114 @@ __device__ __forceinline__ bool dda_end(const DDA &it)
 }
 
 // ----------------------------------------------------------------------------
+// The walk's decisions in integer arithmetic.  After the walk's first FP64
+// add, epsilon is a multiple of ulp(epsilon) >= ulp(epsilon_update), so
+// epsilon, epsilon_update u and delta_slow d are all integer multiples of
+// q = min(ulp(u), ulp(d)), a power of two.  In units of q:
+// - fl(eps + u) is the integer sum rounded to 53 significant bits, to
+//   nearest, ties to even (round53): the FP64 add of two multiples of q;
+// - with u <= d and eps <= d before every add (it holds by induction once
+//   it holds at the start), an eps above d is at most 2d, so fl(eps - d) is
+//   exact (Sterbenz) and is the integer difference;
+// - the comparison eps > d is the integer comparison;
+// - the sigma split at a slow move, (float)fl(d - eps_prev), is
+//   __ll2float_rn(round53(D - E_prev)) times q as a float (exact scaling).
+// So the integer walk visits the pixels the FP64 walk visits and gives the
+// same FP32 sigma bit for bit, without the FP64 pipe (a small fraction of
+// the FP32 rate on GB300).  A ray takes it when the conditions hold (u in
+// (0, d], eps in [0, d] and a multiple of q, d / q and u / q below 2^60, q
+// representable as a normal float); otherwise it stays on the FP64 walk.
+struct DDAInt {
+    unsigned long long E, U, D;
+    float qf;      // q as a float
+};
+
+__device__ __forceinline__ unsigned long long round53(unsigned long long s)
+{
+    const int n = 64 - __clzll((long long)s);   // bit length (0 for s == 0)
+    if (n <= 53) return s;
+    const int sh = n - 53;
+    const unsigned long long half = 1ull << (sh - 1);
+    const unsigned long long low = s & ((half << 1) - 1);
+    unsigned long long r = s >> sh;
+    r += (low > half || (low == half && (r & 1))) ? 1ull : 0ull;
+    return r << sh;
+}
+
+__device__ __forceinline__ bool dda_int_init(const DDA &it, DDAInt &w)
+{
+    const double u = it.epsilon_update, d = it.delta_slow, e = it.epsilon;
+    if (!(u > 0.0) || !(u <= d) || !(e >= 0.0) || !(e <= d)) return false;
+    const int eu = (int)((__double_as_longlong(u) >> 52) & 0x7FF);
+    const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7FF);
+    if (eu == 0 || ed == 0 || eu == 0x7FF || ed == 0x7FF) return false;
+    const int kq = min(eu, ed) - 1023 - 52;               // q = 2^kq
+    if (kq < -100 || kq > 100) return false;
+    const double inv_q = __longlong_as_double((long long)(1023 - kq) << 52);
+    const double Ud = u * inv_q, Dd = d * inv_q, Ed = e * inv_q;   // exact scalings
+    if (!(Dd < 0x1p60) || !(Ud < 0x1p60)) return false;
+    const long long E = __double2ll_rn(Ed);
+    if ((double)E != Ed) return false;                    // epsilon not a multiple of q
+    w.U = (unsigned long long)__double2ll_rn(Ud);
+    w.D = (unsigned long long)__double2ll_rn(Dd);
+    w.E = (unsigned long long)E;
+    w.qf = __int_as_float((127 + kq) << 23);
+    return true;
+}
+
+// dda_update<kDdaSigma32> on the integer state.
+__device__ __forceinline__ void dda_int_update(DDA &it, DDAInt &w)
+{
+    if (it.slow_move) {
+        if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
+        it.sigma32 = it.sigma_tilde32 - it.sigma32;
+        it.slow_move = 0;
+    } else {
+        if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
+        const unsigned long long prev = w.E;
+        w.E = round53(w.E + w.U);
+        if (w.E > w.D) {
+            it.slow_move = 1;
+            w.E -= w.D;
+            it.sigma32 = (__ll2float_rn((long long)round53(w.D - prev)) * w.qf) *
+                         it.sigma_per_eps32;
+        } else {
+            it.sigma32 = it.sigma_tilde32;
+        }
+    }
+}
+
+// The FP32-sigma walk of `it` (set up by dda_set_t<kDdaSigma32>), at most
+// cap steps: visit(i, j, sigma32, slow_move) before each update, slow_move
+// being the move that update makes.  FP64 updates run until the walk's
+// first epsilon add (at most two), then the integer walk where it applies
+// (fp64_walk == 0), else FP64 to the end.
+template <class Visit>
+__device__ __forceinline__ int dda_walk32(DDA &it, int cap, int fp64_walk, Visit &&visit)
+{
+    int step = 0;
+    bool added = false;
+    for (; step < cap && !dda_end(it) && !added; ++step) {
+        visit(it.i, it.j, it.sigma32, it.slow_move);
+        added = !it.slow_move;
+        dda_update<kDdaSigma32>(it);
+    }
+    DDAInt w;
+    if (added && !fp64_walk && dda_int_init(it, w)) {
+        for (; step < cap && !dda_end(it); ++step) {
+            visit(it.i, it.j, it.sigma32, it.slow_move);
+            dda_int_update(it, w);
+        }
+    } else {
+        for (; step < cap && !dda_end(it); ++step) {
+            visit(it.i, it.j, it.sigma32, it.slow_move);
+            dda_update<kDdaSigma32>(it);
+        }
+    }
+    return step;
+}
+
+// ----------------------------------------------------------------------------
 
 template <bool RATIO>
 __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__restrict__ cs_tab,
@@ -231,7 +339,7 @@ __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__r
                                                     long long ils, float *__restrict__ out,
                                                     long long ocs, long long ols,
                                                     const float *__restrict__ y_am, int first,
-                                                    int stride)
+                                                    int stride, int fp64_walk)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;   // ray
     const int j = first + blockIdx.y * stride;             // view
@@ -243,19 +351,27 @@ __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__r
     dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     float acc = 0.f, comp = 0.f;
     const int cap = 2 * (g.lines + g.columns) + 8;
-    for (int step = 0; step < cap && !dda_end(it); ++step) {
-        const float x = __ldg(img + (long long)it.i * ics + (long long)it.j * ils) * it.sigma32;
+    dda_walk32(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
+        const float x = __ldg(img + (long long)pi * ics + (long long)pj * ils) * sg;
         const float y = x - comp, t = acc + y;
         comp = (t - acc) - y;
         acc = t;
-        dda_update<kDdaSigma32>(it);
-    }
+    });
     float val = acc - comp;
     if (RATIO) {
         const float yv = y_am[(size_t)j * g.R + i];
         val = (val != 0.f) ? yv / val : 0.f;
     }
     out[(long long)i * ocs + (long long)j * ols] = val;
+}
+
+// RG_DDA_FP64=1 (read per call) keeps the DDA Radon, transpose and walk
+// recording on the FP64 walk: the integer walk's reference for tests and
+// A/B timing; both visit the same pixels with the same FP32 sigma.
+static int dda_fp64_walk()
+{
+    const char *e = getenv("RG_DDA_FP64");
+    return (e && e[0] == '1' && e[1] == 0) ? 1 : 0;
 }
 
 int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, long long ics,
@@ -267,10 +383,10 @@ int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, lo
     dim3 grid((g.R + 127) / 128, nv);
     if (y_am)
         k_bres_radon<true><<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, y_am,
-                                                 first, stride);
+                                                 first, stride, dda_fp64_walk());
     else
         k_bres_radon<false><<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, nullptr,
-                                                  first, stride);
+                                                  first, stride, dda_fp64_walk());
     RG_CK_LAUNCH("k_bres_radon");
     return RG_OK;
 }
@@ -280,7 +396,8 @@ int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, lo
 __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double *__restrict__ cs_tab,
                                                         const float *__restrict__ s_am,
                                                         float *__restrict__ img_c, int first,
-                                                        int stride, float *__restrict__ den)
+                                                        int stride, float *__restrict__ den,
+                                                        int fp64_walk)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = first + blockIdx.y * stride;
@@ -293,12 +410,11 @@ __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double 
     const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
     dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
-    for (int step = 0; step < cap && !dda_end(it); ++step) {
-        const size_t e = (size_t)it.i * g.columns + it.j;
-        if (sv != 0.f) atomicAdd(img_c + e, sv * it.sigma32);
-        if (den) atomicAdd(den + e, it.sigma32);
-        dda_update<kDdaSigma32>(it);
-    }
+    dda_walk32(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
+        const size_t e = (size_t)pi * g.columns + pj;
+        if (sv != 0.f) atomicAdd(img_c + e, sv * sg);
+        if (den) atomicAdd(den + e, sg);
+    });
 }
 
 // Normalised backprojection in FP64: sum(s sigma) and sum(sigma) per pixel.
@@ -357,7 +473,8 @@ int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_a
     const int nv = (g.A - first + stride - 1) / stride;
     if (nv <= 0) return RG_OK;
     dim3 grid((g.R + 127) / 128, nv);
-    k_bres_transpose<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride, nullptr);
+    k_bres_transpose<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride, nullptr,
+                                           dda_fp64_walk());
     RG_CK_LAUNCH("k_bres_transpose");
     return RG_OK;
 }
@@ -431,7 +548,7 @@ template <bool W>
 __global__ __launch_bounds__(128) void k_dda_plan(DDAGeom g, const double *__restrict__ cs_tab,
                                                   int first, int stride,
                                                   DDARayRec *__restrict__ rays,
-                                                  float *__restrict__ steps)
+                                                  float *__restrict__ steps, int fp64_walk)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = first + blockIdx.y * stride;
@@ -454,11 +571,11 @@ __global__ __launch_bounds__(128) void k_dda_plan(DDAGeom g, const double *__res
         rays[r].dslow = cm ? it.Delta_slow * g.lines : it.Delta_slow * g.columns;
     }
     int moved_slow = 0;
-    for (; n < cap && !dda_end(it); ++n) {
-        if (W) steps[off + n] = __uint_as_float((__float_as_uint(it.sigma32) & ~1u) | moved_slow);
-        moved_slow = it.slow_move;
-        dda_update<kDdaSigma32>(it);
-    }
+    dda_walk32(it, cap, fp64_walk, [&](int, int, float sg, int slow) {
+        if (W) steps[off + n] = __uint_as_float((__float_as_uint(sg) & ~1u) | moved_slow);
+        moved_slow = slow;
+        ++n;
+    });
     if (!W) rays[r].count = n;
 }
 
@@ -580,7 +697,8 @@ int dda_plan_build(const DDAGeom &g, const double *d_cs, int first, int stride,
     RG_CK(cudaMalloc(&p.rays, sizeof(DDARayRec) * (size_t)p.nrays));
     DDARayRec *rays = (DDARayRec *)p.rays;
     dim3 grid((g.R + 127) / 128, nv);
-    k_dda_plan<false><<<grid, 128, 0, st>>>(g, d_cs, first, stride, rays, nullptr);
+    k_dda_plan<false><<<grid, 128, 0, st>>>(g, d_cs, first, stride, rays, nullptr,
+                                            dda_fp64_walk());
     RG_CK_LAUNCH("k_dda_plan (count)");
     std::vector<DDARayRec> h((size_t)p.nrays);
     RG_CK(cudaMemcpyAsync(h.data(), rays, sizeof(DDARayRec) * h.size(), cudaMemcpyDeviceToHost, st));
@@ -599,7 +717,8 @@ int dda_plan_build(const DDAGeom &g, const double *d_cs, int first, int stride,
     }
     RG_CK(cudaMemcpyAsync(rays, h.data(), sizeof(DDARayRec) * h.size(), cudaMemcpyHostToDevice, st));
     RG_CK(cudaMalloc(&p.steps, bytes));
-    k_dda_plan<true><<<grid, 128, 0, st>>>(g, d_cs, first, stride, rays, (float *)p.steps);
+    k_dda_plan<true><<<grid, 128, 0, st>>>(g, d_cs, first, stride, rays, (float *)p.steps,
+                                           dda_fp64_walk());
     RG_CK_LAUNCH("k_dda_plan (record)");
     RG_CK(cudaStreamSynchronize(st));   // h is released on return
     p.total = total;

@@ -1,0 +1,141 @@
+"""The DDA walk's epsilon accumulator in exact integer arithmetic.
+
+The walk (raft/raft_ddaiterator.c:196-248) decides its slow-axis moves with
+FP64 arithmetic: a fast step adds epsilon_update u to epsilon, and when
+epsilon exceeds delta_slow d it moves on the slow axis and subtracts d.
+GB300 runs FP64 at a small fraction of its FP32 rate, so the kernels make
+the same decisions with 64-bit integers (bresenham.cu, DDAInt):
+- after the walk's first FP64 add, epsilon is a multiple of ulp(epsilon),
+  which is at least ulp(u); so epsilon, u and d are all integer multiples of
+  q = min(ulp(u), ulp(d)), a power of two;
+- fl(eps + u) is then the integer sum rounded to 53 significant bits, to
+  nearest, ties to even (round53 below), times q;
+- while u <= d and epsilon <= d before each add, an epsilon that exceeds d
+  is at most 2d, so eps - d is exact (Sterbenz) and needs no rounding;
+- the sigma split at a slow move uses fl(d - eps_prev) = round53(D - E) q.
+This test restates that integer walk in Python (exact integers) and checks
+it against IEEE FP64 arithmetic (numpy float64, no contraction) step by
+step, on random and edge-case (u, d, eps0), including the kernel's
+conditions for taking the integer path.  It runs on the CPU.
+"""
+import math
+
+import numpy as np
+import pytest
+
+
+def round53(s):
+    """s > 0 (int) rounded to 53 significant bits, to nearest, ties to even."""
+    n = s.bit_length()
+    if n <= 53:
+        return s
+    sh = n - 53
+    low = s & ((1 << sh) - 1)
+    half = 1 << (sh - 1)
+    s >>= sh
+    if low > half or (low == half and (s & 1)):
+        s += 1
+    return s << sh
+
+
+def int_path_ok(u, d, eps):
+    """The kernel's conditions for the integer walk, checked after the first
+    FP64 add (eps = epsilon then)."""
+    if not (0.0 < u <= d) or eps > d:
+        return False
+    q = min(math.ulp(u), math.ulp(d))
+    if q < 2.0 ** -1000:
+        return False
+    return (d + u) / q < 2.0 ** 61 and (eps / q).is_integer()
+
+
+def fp64_steps(u, d, eps, n):
+    """n fast steps of the FP64 walk: (eps after each step, slow flag,
+    fl(d - eps_prev) at slow moves)."""
+    u, d, eps = np.float64(u), np.float64(d), np.float64(eps)
+    out = []
+    for _ in range(n):
+        prev = eps
+        eps = eps + u
+        slow = bool(eps > d)
+        diff = None
+        if slow:
+            eps = eps - d
+            diff = float(d - prev)
+        out.append((float(eps), slow, diff))
+    return out
+
+
+def int_steps(u, d, eps, n):
+    q = min(math.ulp(u), math.ulp(d))
+    U, D, E = int(u / q), int(d / q), int(eps / q)
+    assert U * q == u and D * q == d and E * q == eps
+    out = []
+    for _ in range(n):
+        prev = E
+        E = round53(E + U)
+        slow = E > D
+        diff = None
+        if slow:
+            E = E - D
+            diff = round53(D - prev) * q if D > prev else float(D - prev) * q
+        out.append((E * q, slow, diff))
+    return out
+
+
+def first_add(u, d, eps0):
+    eps = np.float64(eps0) + np.float64(u)
+    if eps > d:
+        eps = eps - np.float64(d)
+    return float(eps)
+
+
+def _check(u, d, eps0, n=4000):
+    eps1 = first_add(u, d, eps0)
+    if not int_path_ok(u, d, eps1):
+        return False
+    assert int_steps(u, d, eps1, n) == fp64_steps(u, d, eps1, n)
+    return True
+
+
+def test_round53_matches_fp64_addition():
+    rng = np.random.default_rng(1)
+    for _ in range(20000):
+        a, b = rng.random() * 10.0 ** rng.integers(-6, 3), rng.random() * 10.0 ** rng.integers(-6, 3)
+        q = min(math.ulp(a), math.ulp(b))
+        A, B = int(a / q), int(b / q)
+        assert round53(A + B) * q == float(np.float64(a) + np.float64(b))
+
+
+@pytest.mark.parametrize("n", [64, 255, 1024, 2048, 4097])
+def test_integer_walk_equals_fp64_walk_on_view_grids(n):
+    """u = dy |tan| and d = dx for an n x n grid on [-1, 1]^2 over views
+    spread in [0, pi), with the walk's possible starting epsilons."""
+    rng = np.random.default_rng(n)
+    dx = 2.0 / (n - 1)
+    taken = 0
+    for theta in np.concatenate([np.linspace(0.0, np.pi, 181, endpoint=False)[1:],
+                                 rng.random(60) * np.pi]):
+        c, s = math.cos(theta), math.sin(theta)
+        if abs(dx * s) <= abs(dx * c):
+            u = abs(dx * s / c)
+        else:
+            u = abs(dx * c / s)
+        for eps0 in (0.0, u / 3.0, dx * rng.random(), dx, 0.5 * dx, 1e-17):
+            taken += _check(u, dx, eps0, n=2 * n)
+    assert taken > 200
+
+
+def test_integer_walk_edge_cases():
+    d = 2.0 / 2047
+    for u in (d, np.nextafter(d, 0.0), d / 2, d / 3, d * 0.999999999, d / 100.0):
+        for eps0 in (0.0, np.nextafter(d, 0.0), d, u, d - u):
+            assert _check(u, d, eps0, n=3000)
+
+
+def test_path_conditions_reject_what_they_must():
+    d = 2.0 / 1023
+    assert not int_path_ok(2.0 * d, d, 0.0)          # u > d: two slow moves per step
+    assert not int_path_ok(d * 2.0 ** -20, d, 0.0)   # d / q beyond 2^61: FP64 walk
+    assert not int_path_ok(d / 3.0, d, 1.5 * d)      # epsilon above d
+    assert int_path_ok(d / 3.0, d, 0.0)

@@ -94,3 +94,42 @@ def test_phantoms(orc, golden):
     sl = golden("sl64")
     fd = rg.radon(orc.SHEPP_LOGAN, (64, 48))
     assert rel(fd, sl["fromdesc"]) <= 1e-6
+
+
+@pytest.mark.parametrize("n,r,a,corners", [
+    (1024, 1024, 720, None),
+    (2048, 2048, 1800, None),
+    (255, 301, 181, None),
+    (200, 160, 97, ((0.3, 1.0), (0.3 + math.pi, -1.0))),
+])
+def test_integer_walk_equals_fp64_walk(monkeypatch, n, r, a, corners):
+    """The DDA kernels make the walk's decisions in 64-bit integer arithmetic
+    wherever it reproduces FP64 exactly (bresenham.cu, DDAInt), and keep the
+    FP64 walk elsewhere.  The Radon of an image of distinct random values
+    sums every ray's visited pixels times its FP32 sigma in a fixed order, so
+    one pixel or sigma off in any ray would change that ray's sum: the
+    integer walk's Radon must equal the FP64 walk's (RG_DDA_FP64=1) bit for
+    bit, at the benchmark sizes and on odd, offset geometries."""
+    g = torch.Generator(device="cuda").manual_seed(n + a)
+    x = rg.gpu_image(torch.rand((n, n), device="cuda", generator=g) + 0.5)
+    kw = dict(top_left=corners[0], bottom_right=corners[1]) if corners else {}
+    outs = []
+    for fp64 in ("1", "0"):
+        monkeypatch.setenv("RG_DDA_FP64", fp64)
+        outs.append(rg.radon(x, (r, a), BRES, **kw).data.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert np.isfinite(outs[1]).all() and outs[1].any()
+
+
+def test_dda_em_integer_walk_matches_fp64_walk(monkeypatch):
+    """The DDA EM records each ray's walk once (k_dda_plan) and replays it;
+    with the recording made by the integer walk it agrees with the FP64
+    walk's to FP32 rounding (the transpose replay adds with atomics)."""
+    rng = np.random.default_rng(3)
+    y = rng.poisson(30.0, size=(256, 180)).astype(np.float64)
+    s = rg.image(y, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
+    outs = []
+    for fp64 in ("1", "0"):
+        monkeypatch.setenv("RG_DDA_FP64", fp64)
+        outs.append(np.asarray(rg.em(s, (256, 256), 5, method=BRES)))
+    assert rel(outs[1], outs[0]) <= 1e-6
