@@ -10,7 +10,11 @@
 // contracts into FMA; with the view cos/sin taken from the host libm (as the
 // reference does) the visited pixel sequence is bit-identical to the
 // reference's.  The axis-aligned branches set sigma to sigma_tilde on entry
-// (the reference leaves it unset, raft/raft_ddaiterator.c:118-129).
+// (the reference leaves it unset, raft/raft_ddaiterator.c:118-129).  The
+// FP32-summing kernels continue each walk after its first epsilon add in
+// exact 64-bit integer arithmetic that reproduces those FP64 operations
+// (DDAInt, dda_walk32): the same pixels and FP32 sigma, without the FP64
+// pipe.
 //
 // Radon: one thread per (ray, view); lanes run over rays, so the
 // view-major output is written coalesced.  Sums are FP32 products of the
@@ -243,19 +247,41 @@ __device__ __forceinline__ bool dda_end(const DDA &it)
 // representable as a normal float); otherwise it stays on the FP64 walk.
 struct DDAInt {
     unsigned long long E, U, D;
-    float qf;      // q as a float
+    int kq;        // q = 2^kq
 };
 
+// s (< 2^63) rounded to 53 significant bits, to nearest, ties to even:
+// adding half - 1 plus the kept part's lowest bit, then truncating, rounds
+// to nearest with ties to even.  No branch: sh is 0 below 2^53.
 __device__ __forceinline__ unsigned long long round53(unsigned long long s)
 {
     const int n = 64 - __clzll((long long)s);   // bit length (0 for s == 0)
-    if (n <= 53) return s;
-    const int sh = n - 53;
-    const unsigned long long half = 1ull << (sh - 1);
-    const unsigned long long low = s & ((half << 1) - 1);
-    unsigned long long r = s >> sh;
-    r += (low > half || (low == half && (r & 1))) ? 1ull : 0ull;
-    return r << sh;
+    const int sh = max(n - 53, 0);
+    const unsigned long long half = (1ull << sh) >> 1;
+    const unsigned long long bias = half ? half - 1 + ((s >> sh) & 1ull) : 0ull;
+    return ((s + bias) >> sh) << sh;
+}
+
+// RN_f32(r) * 2^kq for an integer r < 2^62, built from the integer (r is
+// rounded to 24 bits, to nearest, ties to even) so that no 64-bit
+// conversion runs on the FP64 pipe.  The result is a normal float for the
+// kq that dda_int_init admits.
+__device__ __forceinline__ float f32_scaled(unsigned long long r, int kq)
+{
+    if (r == 0) return 0.f;
+    int n = 64 - __clzll((long long)r);
+    unsigned long long m;
+    if (n > 24) {
+        const int sh = n - 24;
+        m = (r + ((1ull << (sh - 1)) - 1) + ((r >> sh) & 1ull)) >> sh;
+        if (m >> 24) {
+            m >>= 1;
+            ++n;
+        }
+    } else {
+        m = r << (24 - n);
+    }
+    return __uint_as_float(((unsigned)(n - 1 + kq + 127) << 23) | ((unsigned)m & 0x7FFFFFu));
 }
 
 __device__ __forceinline__ bool dda_int_init(const DDA &it, DDAInt &w)
@@ -266,7 +292,7 @@ __device__ __forceinline__ bool dda_int_init(const DDA &it, DDAInt &w)
     const int ed = (int)((__double_as_longlong(d) >> 52) & 0x7FF);
     if (eu == 0 || ed == 0 || eu == 0x7FF || ed == 0x7FF) return false;
     const int kq = min(eu, ed) - 1023 - 52;               // q = 2^kq
-    if (kq < -100 || kq > 100) return false;
+    if (kq < -100 || kq > 60) return false;
     const double inv_q = __longlong_as_double((long long)(1023 - kq) << 52);
     const double Ud = u * inv_q, Dd = d * inv_q, Ed = e * inv_q;   // exact scalings
     if (!(Dd < 0x1p60) || !(Ud < 0x1p60)) return false;
@@ -275,30 +301,8 @@ __device__ __forceinline__ bool dda_int_init(const DDA &it, DDAInt &w)
     w.U = (unsigned long long)__double2ll_rn(Ud);
     w.D = (unsigned long long)__double2ll_rn(Dd);
     w.E = (unsigned long long)E;
-    w.qf = __int_as_float((127 + kq) << 23);
+    w.kq = kq;
     return true;
-}
-
-// dda_update<kDdaSigma32> on the integer state.
-__device__ __forceinline__ void dda_int_update(DDA &it, DDAInt &w)
-{
-    if (it.slow_move) {
-        if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
-        it.sigma32 = it.sigma_tilde32 - it.sigma32;
-        it.slow_move = 0;
-    } else {
-        if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
-        const unsigned long long prev = w.E;
-        w.E = round53(w.E + w.U);
-        if (w.E > w.D) {
-            it.slow_move = 1;
-            w.E -= w.D;
-            it.sigma32 = (__ll2float_rn((long long)round53(w.D - prev)) * w.qf) *
-                         it.sigma_per_eps32;
-        } else {
-            it.sigma32 = it.sigma_tilde32;
-        }
-    }
 }
 
 // The FP32-sigma walk of `it` (set up by dda_set_t<kDdaSigma32>), at most
@@ -318,9 +322,36 @@ __device__ __forceinline__ int dda_walk32(DDA &it, int cap, int fp64_walk, Visit
     }
     DDAInt w;
     if (added && !fp64_walk && dda_int_init(it, w)) {
-        for (; step < cap && !dda_end(it); ++step) {
-            visit(it.i, it.j, it.sigma32, it.slow_move);
-            dda_int_update(it, w);
+        // The integer walk (dda_update<kDdaSigma32> on w), one fast move per
+        // iteration in every lane, so that the lanes of a warp, whose rays
+        // are at different phases of their slow moves, stay together; only
+        // the visit and the slow move that a fast move triggers are
+        // predicated.
+        if (it.slow_move && step < cap && !dda_end(it)) {   // pending from the FP64 steps
+            visit(it.i, it.j, it.sigma32, 1);
+            ++step;
+            if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
+            it.sigma32 = it.sigma_tilde32 - it.sigma32;
+            it.slow_move = 0;
+        }
+        while (step < cap && !dda_end(it)) {
+            visit(it.i, it.j, it.sigma32, 0);
+            ++step;
+            if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
+            const unsigned long long prev = w.E;
+            w.E = round53(w.E + w.U);
+            if (w.E <= w.D) {
+                it.sigma32 = it.sigma_tilde32;
+                continue;
+            }
+            // fl(eps - d) is exact; the split is (float)fl(d - eps_prev) * s
+            w.E -= w.D;
+            const float split = f32_scaled(round53(w.D - prev), w.kq) * it.sigma_per_eps32;
+            if (step >= cap || dda_end(it)) break;
+            visit(it.i, it.j, split, 1);
+            ++step;
+            if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
+            it.sigma32 = it.sigma_tilde32 - split;
         }
     } else {
         for (; step < cap && !dda_end(it); ++step) {

@@ -139,3 +139,51 @@ def test_path_conditions_reject_what_they_must():
     assert not int_path_ok(d * 2.0 ** -20, d, 0.0)   # d / q beyond 2^61: FP64 walk
     assert not int_path_ok(d / 3.0, d, 1.5 * d)      # epsilon above d
     assert int_path_ok(d / 3.0, d, 0.0)
+
+
+def f32_scaled(r, kq):
+    """RN_f32(r) * 2^kq built from the integer r (bresenham.cu, f32_scaled):
+    r rounded to 24 bits, to nearest, ties to even, then exponent and
+    mantissa assembled."""
+    if r == 0:
+        return np.float32(0.0)
+    n = r.bit_length()
+    if n > 24:
+        sh = n - 24
+        m = (r + (1 << (sh - 1)) - 1 + ((r >> sh) & 1)) >> sh
+        if m >> 24:
+            m >>= 1
+            n += 1
+    else:
+        m = r << (24 - n)
+    bits = ((n - 1 + kq + 127) << 23) | (m & 0x7FFFFF)
+    return np.array([bits], dtype=np.uint32).view(np.float32)[0]
+
+
+def test_split_as_float_matches_conversion():
+    """The sigma split needs (float)fl(d - eps_prev): the kernels build it
+    from round53(D - E_prev) with integer operations; it must equal the
+    FP64 value converted to FP32."""
+    rng = np.random.default_rng(7)
+    vals = [1, 2, 3, (1 << 24) - 1, 1 << 24, (1 << 24) + 1, (1 << 25) - 1, (1 << 53) - 1,
+            (1 << 61) + 12345]
+    vals += [int(rng.integers(1, 1 << 62)) for _ in range(20000)]
+    vals += [int(rng.integers(1, 1 << 30)) << int(rng.integers(0, 30)) for _ in range(5000)]
+    for r in vals:
+        r53 = round53(r)
+        for kq in (-100, -62, -1, 0):
+            want = np.float32(np.float64(float(r53) * 2.0 ** kq))
+            assert f32_scaled(r53, kq) == want, (r, kq)
+
+
+def test_branch_free_rounding_equals_round53():
+    """The kernels round with one add and a truncation (bias = half - 1 plus
+    the kept part's lowest bit); that is round53 above."""
+    rng = np.random.default_rng(11)
+    vals = [0, 1, (1 << 53) - 1, 1 << 53, (1 << 53) + 1, (1 << 54) + 2, (1 << 54) + 6,
+            (1 << 62) - 1] + [int(rng.integers(0, 1 << 62)) for _ in range(50000)]
+    for s in vals:
+        sh = max(s.bit_length() - 53, 0)
+        half = (1 << sh) >> 1
+        bias = half - 1 + ((s >> sh) & 1) if half else 0
+        assert ((s + bias) >> sh) << sh == round53(s) if s else s == 0
