@@ -260,16 +260,42 @@ __device__ __forceinline__ void rot_em_finish(int row0, int col0, int N, float *
         }
         const int r = (b / nb) * 32 + er, c = (b % nb) * 32 + ec;
         const size_t i = (size_t)r * N + c;
-        float4 o = make_float4(cx.x * cg.x * ci.x, cx.y * cg.y * ci.y, cx.z * cg.z * ci.z,
-                               cx.w * cg.w * ci.w);
-        if (MODE != 0) {                              // edge pixels keep their value
-            if (r == 0 || r == N - 1) o = cx;
-            if (c == 0) o.x = cx.x;
-            if (c + 3 == N - 1) o.w = cx.w;
+        const float4 o = make_float4(cx.x * cg.x * ci.x, cx.y * cg.y * ci.y,
+                                     cx.z * cg.z * ci.z, cx.w * cg.w * ci.w);
+        // The adjoint's edge pixels belong to the edge CTAs of the same
+        // launch (rot_edges), which may update them at the same time: only
+        // the interior ones are stored here.
+        if (MODE == 0 || (r != 0 && r != N - 1 && c != 0 && c + 3 != N - 1)) {
+            *reinterpret_cast<float4 *>(x + i) = o;
+        } else if (r != 0 && r != N - 1) {
+            if (c != 0) x[i] = o.x;
+            x[i + 1] = o.y;
+            x[i + 2] = o.z;
+            if (c + 3 != N - 1) x[i + 3] = o.w;
         }
-        *reinterpret_cast<float4 *>(x + i) = o;
         __stcg(reinterpret_cast<float4 *>(gsum + i), make_float4(0.f, 0.f, 0.f, 0.f));
     }
+}
+
+// The matched adjoint's edge pixels (the first and last rows and columns,
+// where the Radon's validity rules at line positions 0 and N - 1 apply, and
+// which the paired gathers leave out), computed by the last `edge_rows` rows
+// of CTAs of a paired gather's grid: 32 pixels per CTA, the views split over
+// its warps (adjoint_edge_group), with the EM update where the gather fuses
+// it.  They run beside the tiles, in the grid's last wave, instead of as a
+// launch of their own.  Every thread of the CTA calls this.
+template <bool EMF>
+__device__ __forceinline__ void rot_edges(const float *__restrict__ s_am, int s_ld, int R,
+                                          const View *__restrict__ views, int nv, int N,
+                                          float *__restrict__ out, long long cs, long long ls,
+                                          float *__restrict__ em_x,
+                                          const float *__restrict__ em_inv, int edge_rows)
+{
+    const int g = ((int)blockIdx.y - ((int)gridDim.y - edge_rows)) * (int)gridDim.x +
+                  (int)blockIdx.x;
+    if (g * 32 < 4 * N - 4)
+        adjoint_edge_group<1, EMF, kWarps>(s_am, s_ld, R, views, nv, N, g * 32, out, cs, ls, em_x,
+                                           em_inv);
 }
 
 // Warp w covers columns 8 (w & 3) .. + 8 and rows 4 ROWS (w >> 2) .. + 4
@@ -402,9 +428,15 @@ __global__ __launch_bounds__(256) void k_gather_rot(const float *__restrict__ s_
                                                     int *__restrict__ err, long long zs,
                                                     long long zo, unsigned quad_bytes, int split,
                                                     float *__restrict__ em_x,
-                                                    const float *__restrict__ em_inv, int *em_cnt)
+                                                    const float *__restrict__ em_inv, int *em_cnt,
+                                                    int edge_rows)
 {
     pdl_gate();
+    if (MODE == 1 && (int)blockIdx.y >= (int)gridDim.y - edge_rows) {
+        rot_edges<EMF>(s_am + blockIdx.z * zs, s_ld, R, views, 2 * half, N, out + blockIdx.z * zo,
+                       cs, ls, em_x, em_inv, edge_rows);
+        return;
+    }
     extern __shared__ __align__(16) float2 pairs[];  // [kPairSlots][WMAX] x {view, partner}
     gather_tile_rot<MODE, WMAX, ROWS, EMF>(s_am + blockIdx.z * zs, s_ld, R, views, half, roff, N, scale,
                                 out + blockIdx.z * zo, cs, ls, err, blockIdx.x / split,
@@ -491,9 +523,16 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
                                                         int expire_first,
                                                         float *__restrict__ em_x,
                                                         const float *__restrict__ em_inv,
-                                                        int *em_cnt)
+                                                        int *em_cnt,
+                                                        const float *__restrict__ s_am, int s_ld,
+                                                        int R, long long zs, int edge_rows)
 {
     pdl_gate();
+    if (MODE == 1 && (int)blockIdx.y >= (int)gridDim.y - edge_rows) {
+        rot_edges<EMF>(s_am + blockIdx.z * zs, s_ld, R, views, 2 * half, N, out + blockIdx.z * zo,
+                       cs, ls, em_x, em_inv, edge_rows);
+        return;
+    }
     extern __shared__ __align__(128) float4 qbuf[];   // [kStages][kPairSlots][wb]
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ SlotInfo slot[kStages][kPairSlots];
@@ -598,9 +637,19 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
     if (EMF) rot_em_finish<MODE, ROWS>(row0, col0, N, out, em_x, em_inv, em_cnt, 2 * split);
 }
 
+// CTA rows to append to a paired gather's grid of gx CTAs per row for the
+// adjoint's edge pixels (32 per CTA), or 0.
+static int edge_rows_for(int N, int gx, bool edges)
+{
+    if (!edges) return 0;
+    const int groups = (4 * N - 4 + 31) / 32;
+    return (groups + gx - 1) / gx;
+}
+
 template <int MODE, int WMAX, int ROWS>
 int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
-                 long long ls, int *d_err, cudaStream_t st, const Stack &z, const EmFuse *em)
+                 long long ls, int *d_err, cudaStream_t st, const Stack &z, const EmFuse *em,
+                 bool edges)
 {
     float *ex = em ? em->x : nullptr;
     const float *ei = em ? em->inv : nullptr;
@@ -616,9 +665,10 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
     const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
     const unsigned pb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
-    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+    const int er = edge_rows_for(N, (int)grid.x * split, MODE == 1 && edges);
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y + er, grid.z), 256, smem, st, split,
                      s_am, s_ld, p.g.R, (const View *)p.d_views, half, roff, N,
-                     scale, out, cs, ls, d_err, z.in, z.out, pb, split, ex, ei, ec));
+                     scale, out, cs, ls, d_err, z.in, z.out, pb, split, ex, ei, ec, er));
     RG_CK_LAUNCH("k_gather_rot");
     return RG_OK;
 }
@@ -629,7 +679,7 @@ int quad_box(int w) { return (w + 7) & ~7; }
 template <int MODE, int ROWS>
 int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                    long long ls, int *d_err, cudaStream_t st, const Stack &z, float4 *quads,
-                   int w, bool zero_out, const EmFuse *em)
+                   int w, bool zero_out, const EmFuse *em, bool edges)
 {
     float *ex = em ? em->x : nullptr;
     const float *ei = em ? em->inv : nullptr;
@@ -670,9 +720,10 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const int split = gather_pick_split((const void *)k, smem, ROWS, half, grid, st);
     const unsigned qb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
-    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
+    const int er = edge_rows_for(N, (int)grid.x * split, MODE == 1 && edges);
+    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y + er, grid.z), 256, smem, st, split,
                      tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
-                     d_err, z.out, wb, qb, split, expire, ex, ei, ec));
+                     d_err, z.out, wb, qb, split, expire, ex, ei, ec, s_am, s_ld, R, z.in, er));
     RG_CK_LAUNCH("k_gather_rot_tma");
     return RG_OK;
 }
@@ -690,19 +741,19 @@ bool gather_rot_use_tma(int pairs)
 template <int MODE, int ROWS>
 int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                     long long ls, int *d_err, cudaStream_t st, const Stack &z, void *quads,
-                    bool zero_out, const EmFuse *em)
+                    bool zero_out, const EmFuse *em, bool edges)
 {
     const int t = ROWS == 16 ? 2 : ROWS == 8 ? 1 : 0;
     const int w = MODE == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
     if (quads && quad_box(w) <= kQuadBox && p.nv / 2 <= 65535 && gather_rot_use_tma(p.nv / 2))
         return gather_rot_tma<MODE, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z,
-                                          (float4 *)quads, w, zero_out, em);
+                                          (float4 *)quads, w, zero_out, em, edges);
     if (zero_out)
         if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
-    if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
-    if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
-    if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
-    if (w <= 512) return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em);
+    if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 512) return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
     return set_error(RG_EUNSUPPORTED,
                      "gather window of %d samples per tile exceeds 512 "
                      "(image much coarser than the ray spacing)", w);
@@ -728,7 +779,7 @@ size_t gather_quads_bytes(int nv, int R, int nz)
 
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z, void *quads, bool zero_out, const EmFuse *em)
+                      const Stack &z, void *quads, bool zero_out, const EmFuse *em, bool edges)
 {
     const bool zo = zero_out;
     if (em && (!em_fusable(p.g.N) || z.n != 1 || out != em->gsum || cs != p.g.N || ls != 1 ||
@@ -736,13 +787,13 @@ int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, fl
         return set_error(RG_EINVAL, "fused EM gather: one N x N slice, N a multiple of 32, "
                                     "into its own zeroed partial-sum buffer");
     if (mode == 0) {
-        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
-        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
-        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
+        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
+        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
+        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
     }
-    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
-    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
-    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em);
+    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
+    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
+    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
 }
 
 }  // namespace rg

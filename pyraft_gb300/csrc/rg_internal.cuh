@@ -342,15 +342,18 @@ struct SplitPref {
     SplitPref &operator=(const SplitPref &) = delete;
     int saved;
 };
-// Backprojection (mode 0) or matched adjoint (mode 1, interior pixels: the
-// edge pixels are left to the caller) with views paired a quarter turn
-// apart (p.rot_ok).  Two partial sums are added to each pixel of an output
-// that is zeroed first: by this call when zero_out (in the quad prepass
-// where it runs), else by the caller.  With `em` (one slice, out = em->gsum,
-// N x N contiguous) the EM update is fused as described at EmFuse.
+// Backprojection (mode 0) or matched adjoint (mode 1) with views paired a
+// quarter turn apart (p.rot_ok).  Two partial sums are added to each
+// interior pixel of an output that is zeroed first: by this call when
+// zero_out (in the quad prepass where it runs), else by the caller.  The
+// adjoint's edge pixels are computed by extra CTAs of the same launch when
+// `edges` (stored, or EM-updated), else left to the caller.  With `em` (one
+// slice, out = em->gsum, N x N contiguous) the EM update is fused as
+// described at EmFuse.
 int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, float *out,
                       long long cs, long long ls, int *d_err, cudaStream_t st, int rows,
-                      const Stack &z, void *quads, bool zero_out, const EmFuse *em = nullptr);
+                      const Stack &z, void *quads, bool zero_out, const EmFuse *em = nullptr,
+                      bool edges = false);
 // Whether launch_gather takes the paired path where a plan allows it
 // (RG_GATHER_ROT=0 turns it off).
 bool gather_rot_enabled();

@@ -391,29 +391,37 @@ static bool gather_mirror_enabled()
 // (adjoint_edge_group, ss_tiles.cuh): one CTA per 32 consecutive pixels of
 // the image's first and last rows and columns, its 32 warps splitting the
 // views.
-template <int MODE, bool EM>
-__global__ __launch_bounds__(1024) void k_adjoint_edges(const float *__restrict__ s_am, int s_ld,
-                                                       int R, const View *__restrict__ views,
-                                                       int nv, int N, float *__restrict__ out,
-                                                       long long cs, long long ls,
-                                                       float *__restrict__ em_x,
-                                                       const float *__restrict__ inv_sens,
-                                                       long long zs, long long zo)
+// WARPS warps per CTA split a group's views.  32 for the gathers whose edge
+// pixels have no other home; 8 for the stacks of the paired gathers, whose
+// one-slice form computes its edges with 8 warps inside the gather's own
+// launch (rot_edges): the same split sums in the same order, so a stack's
+// members equal separate calls bit for bit.
+template <int MODE, bool EM, int WARPS>
+__global__ __launch_bounds__(WARPS * 32) void k_adjoint_edges(const float *__restrict__ s_am,
+                                                              int s_ld, int R,
+                                                              const View *__restrict__ views,
+                                                              int nv, int N,
+                                                              float *__restrict__ out,
+                                                              long long cs, long long ls,
+                                                              float *__restrict__ em_x,
+                                                              const float *__restrict__ inv_sens,
+                                                              long long zs, long long zo)
 {
     pdl_gate();
-    adjoint_edge_group<MODE, EM, 32>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N, blockIdx.x * 32,
-                                 out + blockIdx.z * zo, cs, ls, em_x, inv_sens);
+    adjoint_edge_group<MODE, EM, WARPS>(s_am + blockIdx.z * zs, s_ld, R, views, nv, N,
+                                        blockIdx.x * 32, out + blockIdx.z * zo, cs, ls, em_x,
+                                        inv_sens);
 }
 
-template <int MODE, bool EM>
+template <int MODE, bool EM, int WARPS = 32>
 static int adjoint_edges(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                          long long ls, float *em_x, const float *inv_sens, cudaStream_t st,
                          const Stack &z)
 {
     const int N = p.g.N;
     dim3 grid((4 * N - 4 + 31) / 32, 1, z.n);   // 32 edge pixels per CTA
-    RG_CK(launch_pdl(k_adjoint_edges<MODE, EM>, grid, 1024, 0, st, 1, s_am, s_ld, p.g.R,
-                     p.d_views, p.nv, N, out, cs, ls, em_x, inv_sens, z.in, z.out));
+    RG_CK(launch_pdl(k_adjoint_edges<MODE, EM, WARPS>, grid, WARPS * 32, 0, st, 1, s_am, s_ld,
+                     p.g.R, p.d_views, p.nv, N, out, cs, ls, em_x, inv_sens, z.in, z.out));
     RG_CK_LAUNCH("k_adjoint_edges");
     return RG_OK;
 }
@@ -667,19 +675,22 @@ int launch_gather(const SSPlan &p, int mode, const float *s_am, int s_ld, float 
                          "matched adjoint needs ray spacing >= pixel spacing along each line "
                          "(nrays <= size for the default extents)");
     if (mode == 1) {
+        // For one slice, the paired gathers compute the edge pixels in extra
+        // CTAs of their own launch (rot_edges), which fill the grid's last
+        // wave; a stack's many-wave grid gains nothing from them, and its
+        // edges keep a kernel of their own, with the same 8-warp view split.
         if (!em_x && p.rot_ok && gather_rot_enabled()) {
             if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
-            if (int rc = adjoint_edges<1, false>(p, s_am, s_ld, out, cs, ls, nullptr, nullptr, st, z))
-                return rc;
+            if (z.n > 1)
+                if (int rc = adjoint_edges<1, false, kWarps>(p, s_am, s_ld, out, cs, ls, nullptr,
+                                                             nullptr, st, z))
+                    return rc;
             return launch_gather_rot(p, 1, s_am, s_ld, out, cs, ls, d_err, st, rows, z, quads,
-                                     false);
+                                     false, nullptr, z.n == 1);
         }
-        if (fused) {
-            if (int rc = adjoint_edges<1, true>(p, s_am, s_ld, nullptr, 0, 0, em_x, inv_sens, st, z))
-                return rc;
+        if (fused)
             return launch_gather_rot(p, 1, s_am, s_ld, ef.gsum, p.g.N, 1, d_err, st, rows, z,
-                                     quads, false, &ef);
-        }
+                                     quads, false, &ef, true);
         if (em_x)
             return gather_rows<1, true>(p, rows, s_am, s_ld, out, cs, ls, em_x, inv_sens, d_err, st, z);
         return gather_rows<1, false>(p, rows, s_am, s_ld, out, cs, ls, nullptr, nullptr, d_err, st, z);
