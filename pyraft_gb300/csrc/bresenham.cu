@@ -11,10 +11,10 @@
 // reference does) the visited pixel sequence is bit-identical to the
 // reference's.  The axis-aligned branches set sigma to sigma_tilde on entry
 // (the reference leaves it unset, raft/raft_ddaiterator.c:118-129).  The
-// FP32-summing kernels continue each walk after its first epsilon add in
-// exact 64-bit integer arithmetic that reproduces those FP64 operations
-// (DDAInt, dda_walk32): the same pixels and FP32 sigma, without the FP64
-// pipe.
+// Radon, transpose, walk recording and normalised backprojection continue
+// each walk after its first epsilon add in exact 64-bit integer arithmetic
+// that reproduces those FP64 operations (DDAInt, dda_walk): the same pixels
+// and the same FP32 or FP64 sigma, without most of the FP64 work.
 //
 // Radon: one thread per (ray, view); lanes run over rays, so the
 // view-major output is written coalesced.  Sums are FP32 products of the
@@ -305,58 +305,74 @@ __device__ __forceinline__ bool dda_int_init(const DDA &it, DDAInt &w)
     return true;
 }
 
-// The FP32-sigma walk of `it` (set up by dda_set_t<kDdaSigma32>), at most
-// cap steps: visit(i, j, sigma32, slow_move) before each update, slow_move
-// being the move that update makes.  FP64 updates run until the walk's
+// The walk of `it` (set up by dda_set_t<FORM>, FORM kDdaSigma32 or
+// kDdaSigma64), at most cap steps: visit(i, j, sigma, slow_move) before each
+// update, sigma being it.sigma32 (FP32 form) or it.sigma (FP64 form) and
+// slow_move the move that update makes.  FP64 updates run until the walk's
 // first epsilon add (at most two), then the integer walk where it applies
-// (fp64_walk == 0), else FP64 to the end.
-template <class Visit>
-__device__ __forceinline__ int dda_walk32(DDA &it, int cap, int fp64_walk, Visit &&visit)
+// (fp64_walk == 0), else FP64 to the end.  The integer walk makes one fast
+// move per iteration in every lane, so that the lanes of a warp, whose rays
+// are at different phases of their slow moves, stay together; only the
+// visit and the slow move that a fast move triggers are predicated.  The
+// sigma split at a slow move is the FP64 walk's: (float)fl(d - eps_prev) * s
+// in FP32 (built from the rounded integer, f32_scaled), fl(fl(d - eps_prev)
+// * s) in FP64 (the difference is an exact double, and scaling s by 2^kq
+// first leaves the product's rounding unchanged).
+template <int FORM, class Visit>
+__device__ __forceinline__ int dda_walk(DDA &it, int cap, int fp64_walk, Visit &&visit)
 {
+    static_assert(FORM == kDdaSigma32 || FORM == kDdaSigma64, "sigma form");
+    auto sig = [&]() {
+        if constexpr (FORM == kDdaSigma32) return it.sigma32;
+        else return it.sigma;
+    };
     int step = 0;
     bool added = false;
     for (; step < cap && !dda_end(it) && !added; ++step) {
-        visit(it.i, it.j, it.sigma32, it.slow_move);
+        visit(it.i, it.j, sig(), it.slow_move);
         added = !it.slow_move;
-        dda_update<kDdaSigma32>(it);
+        dda_update<FORM>(it);
     }
     DDAInt w;
     if (added && !fp64_walk && dda_int_init(it, w)) {
-        // The integer walk (dda_update<kDdaSigma32> on w), one fast move per
-        // iteration in every lane, so that the lanes of a warp, whose rays
-        // are at different phases of their slow moves, stay together; only
-        // the visit and the slow move that a fast move triggers are
-        // predicated.
+        // sigma_per_eps times q, exact (a power-of-two scaling)
+        const double sp_q = it.sigma_per_eps * __longlong_as_double((long long)(1023 + w.kq) << 52);
         if (it.slow_move && step < cap && !dda_end(it)) {   // pending from the FP64 steps
-            visit(it.i, it.j, it.sigma32, 1);
+            visit(it.i, it.j, sig(), 1);
             ++step;
             if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
-            it.sigma32 = it.sigma_tilde32 - it.sigma32;
+            if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32 - it.sigma32;
+            else it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
             it.slow_move = 0;
         }
         while (step < cap && !dda_end(it)) {
-            visit(it.i, it.j, it.sigma32, 0);
+            visit(it.i, it.j, sig(), 0);
             ++step;
             if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
             const unsigned long long prev = w.E;
             w.E = round53(w.E + w.U);
             if (w.E <= w.D) {
-                it.sigma32 = it.sigma_tilde32;
+                if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32;
+                else it.sigma = it.sigma_tilde;
                 continue;
             }
-            // fl(eps - d) is exact; the split is (float)fl(d - eps_prev) * s
-            w.E -= w.D;
-            const float split = f32_scaled(round53(w.D - prev), w.kq) * it.sigma_per_eps32;
+            w.E -= w.D;                          // fl(eps - d), exact
+            const unsigned long long diff = round53(w.D - prev);
+            if constexpr (FORM == kDdaSigma32)
+                it.sigma32 = f32_scaled(diff, w.kq) * it.sigma_per_eps32;
+            else
+                it.sigma = __dmul_rn(__ll2double_rn((long long)diff), sp_q);
             if (step >= cap || dda_end(it)) break;
-            visit(it.i, it.j, split, 1);
+            visit(it.i, it.j, sig(), 1);
             ++step;
             if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
-            it.sigma32 = it.sigma_tilde32 - split;
+            if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32 - it.sigma32;
+            else it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
         }
     } else {
         for (; step < cap && !dda_end(it); ++step) {
-            visit(it.i, it.j, it.sigma32, it.slow_move);
-            dda_update<kDdaSigma32>(it);
+            visit(it.i, it.j, sig(), it.slow_move);
+            dda_update<FORM>(it);
         }
     }
     return step;
@@ -382,7 +398,7 @@ __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__r
     dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     float acc = 0.f, comp = 0.f;
     const int cap = 2 * (g.lines + g.columns) + 8;
-    dda_walk32(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
+    dda_walk<kDdaSigma32>(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
         const float x = __ldg(img + (long long)pi * ics + (long long)pj * ils) * sg;
         const float y = x - comp, t = acc + y;
         comp = (t - acc) - y;
@@ -396,9 +412,10 @@ __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__r
     out[(long long)i * ocs + (long long)j * ols] = val;
 }
 
-// RG_DDA_FP64=1 (read per call) keeps the DDA Radon, transpose and walk
-// recording on the FP64 walk: the integer walk's reference for tests and
-// A/B timing; both visit the same pixels with the same FP32 sigma.
+// RG_DDA_FP64=1 (read per call) keeps the DDA Radon, transpose, walk
+// recording and normalised backprojection on the FP64 walk: the integer
+// walk's reference for tests and A/B timing; both visit the same pixels
+// with the same sigma.
 static int dda_fp64_walk()
 {
     const char *e = getenv("RG_DDA_FP64");
@@ -441,7 +458,7 @@ __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double 
     const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
     dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
-    dda_walk32(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
+    dda_walk<kDdaSigma32>(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
         const size_t e = (size_t)pi * g.columns + pj;
         if (sv != 0.f) atomicAdd(img_c + e, sv * sg);
         if (den) atomicAdd(den + e, sg);
@@ -455,7 +472,7 @@ __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double 
 __global__ __launch_bounds__(128) void k_bres_norm_sums(DDAGeom g, const double *__restrict__ cs_tab,
                                                         const float *__restrict__ s_am,
                                                         double *__restrict__ num,
-                                                        double *__restrict__ den)
+                                                        double *__restrict__ den, int fp64_walk)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int j = blockIdx.y;
@@ -467,12 +484,11 @@ __global__ __launch_bounds__(128) void k_bres_norm_sums(DDAGeom g, const double 
     const double dts = __ddiv_rn(__dsub_rn(g.sbr_y, g.stl_y), (double)(g.R - 1));
     dda_set_t<kDdaSigma64>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
-    for (int step = 0; step < cap && !dda_end(it); ++step) {
-        const size_t e = (size_t)it.i * g.columns + it.j;
-        if (sv != 0.0) atomicAdd(num + e, sv * it.sigma);
-        atomicAdd(den + e, it.sigma);
-        dda_update<kDdaSigma64>(it);
-    }
+    dda_walk<kDdaSigma64>(it, cap, fp64_walk, [&](int pi, int pj, double sg, int) {
+        const size_t e = (size_t)pi * g.columns + pj;
+        if (sv != 0.0) atomicAdd(num + e, sv * sg);
+        atomicAdd(den + e, sg);
+    });
 }
 
 // out(strided) = num / den, 0 where den == 0.
@@ -490,7 +506,7 @@ int launch_bres_normalised(const DDAGeom &g, const double *d_cs, const float *s_
                            double *den, float *out, long long cs, long long ls, cudaStream_t st)
 {
     dim3 grid((g.R + 127) / 128, g.A);
-    k_bres_norm_sums<<<grid, 128, 0, st>>>(g, d_cs, s_am, num, den);
+    k_bres_norm_sums<<<grid, 128, 0, st>>>(g, d_cs, s_am, num, den, dda_fp64_walk());
     RG_CK_LAUNCH("k_bres_norm_sums");
     dim3 g2((g.columns + 127) / 128, g.lines);
     k_bres_normalise<<<g2, 128, 0, st>>>(num, den, g.lines, g.columns, out, cs, ls);
@@ -602,7 +618,7 @@ __global__ __launch_bounds__(128) void k_dda_plan(DDAGeom g, const double *__res
         rays[r].dslow = cm ? it.Delta_slow * g.lines : it.Delta_slow * g.columns;
     }
     int moved_slow = 0;
-    dda_walk32(it, cap, fp64_walk, [&](int, int, float sg, int slow) {
+    dda_walk<kDdaSigma32>(it, cap, fp64_walk, [&](int, int, float sg, int slow) {
         if (W) steps[off + n] = __uint_as_float((__float_as_uint(sg) & ~1u) | moved_slow);
         moved_slow = slow;
         ++n;

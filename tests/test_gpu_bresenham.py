@@ -133,3 +133,19 @@ def test_dda_em_integer_walk_matches_fp64_walk(monkeypatch):
         monkeypatch.setenv("RG_DDA_FP64", fp64)
         outs.append(np.asarray(rg.em(s, (256, 256), 5, method=BRES)))
     assert rel(outs[1], outs[0]) <= 1e-6
+
+
+def test_normalised_backprojection_integer_walk_matches_fp64_walk(monkeypatch):
+    """The normalised DDA backprojection (sum of s sigma over sum of sigma,
+    FP64 sums) takes the integer walk with FP64 sigma; its sums are FP64
+    atomics in a varying order, so the two walks agree to FP64 rounding
+    (one pixel off in any ray would show at the 1e-3 level)."""
+    rng = np.random.default_rng(5)
+    n, r, a = 512, 512, 360
+    s = rg.image(rng.random((r, a)) + 0.5, top_left=(0.0, 1.0), bottom_right=(math.pi, -1.0))
+    plan = rg.backprojection_plan((r, a), (n, n), 0, BRES)
+    outs = []
+    for fp64 in ("1", "0"):
+        monkeypatch.setenv("RG_DDA_FP64", fp64)
+        outs.append(np.asarray(rg.backprojection(s, plan), np.float64))
+    assert rel(outs[1], outs[0]) <= 1e-12
