@@ -50,7 +50,8 @@ img = torch.full((512, 512), float("nan"), device="cuda")
 _native.check(L.rg_fbp(rg_image(gpu_image(s, *C)), rg_image(gpu_image(img)),
                        _native.RG_FILTER_RAMLAK, None, 0, st))
 out["fbp"] = img
-y = torch.poisson(20.0 * torch.rand((256, 720), device="cuda", generator=g))
+y = torch.poisson(20.0 * torch.rand((256, 720), device="cuda", generator=g), generator=g)
+out["em_input"] = y
 out["em"] = rg.em(gpu_image(y, *C), (256, 256), 6, method=rg.radon_method.SLANTSTACK).data
 torch.cuda.synchronize()
 assert L.rg_device_status() == 0
