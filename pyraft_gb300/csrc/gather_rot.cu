@@ -750,10 +750,14 @@ int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
                                           (float4 *)quads, w, zero_out, em, edges);
     if (zero_out)
         if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
-    if (w <= 64) return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
-    if (w <= 128) return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
-    if (w <= 256) return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
-    if (w <= 512) return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 64)
+        return gather_rot_w<MODE, 64, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 128)
+        return gather_rot_w<MODE, 128, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 256)
+        return gather_rot_w<MODE, 256, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
+    if (w <= 512)
+        return gather_rot_w<MODE, 512, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z, em, edges);
     return set_error(RG_EUNSUPPORTED,
                      "gather window of %d samples per tile exceeds 512 "
                      "(image much coarser than the ray spacing)", w);
@@ -787,13 +791,13 @@ int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, fl
         return set_error(RG_EINVAL, "fused EM gather: one N x N slice, N a multiple of 32, "
                                     "into its own zeroed partial-sum buffer");
     if (mode == 0) {
-        if (rows == 16) return gather_rot_rows<0, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
-        if (rows == 8) return gather_rot_rows<0, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
-        return gather_rot_rows<0, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
+        auto f = rows == 16 ? gather_rot_rows<0, 16> : rows == 8 ? gather_rot_rows<0, 8>
+                                                                  : gather_rot_rows<0, 4>;
+        return f(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, false);
     }
-    if (rows == 16) return gather_rot_rows<1, 16>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
-    if (rows == 8) return gather_rot_rows<1, 8>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
-    return gather_rot_rows<1, 4>(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
+    auto f = rows == 16 ? gather_rot_rows<1, 16> : rows == 8 ? gather_rot_rows<1, 8>
+                                                              : gather_rot_rows<1, 4>;
+    return f(p, s_am, s_ld, out, cs, ls, d_err, st, z, quads, zo, em, edges);
 }
 
 }  // namespace rg

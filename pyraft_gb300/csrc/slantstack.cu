@@ -389,13 +389,12 @@ static bool gather_mirror_enabled()
 
 // Edge pixels of the matched adjoint and of its FP64 sensitivity
 // (adjoint_edge_group, ss_tiles.cuh): one CTA per 32 consecutive pixels of
-// the image's first and last rows and columns, its 32 warps splitting the
-// views.
-// WARPS warps per CTA split a group's views.  32 for the gathers whose edge
-// pixels have no other home; 8 for the stacks of the paired gathers, whose
-// one-slice form computes its edges with 8 warps inside the gather's own
-// launch (rot_edges): the same split sums in the same order, so a stack's
-// members equal separate calls bit for bit.
+// the image's first and last rows and columns, its WARPS warps splitting
+// the views: 32 for the gathers whose edge pixels have no other home; 8 for
+// the stacks of the paired gathers, whose one-slice form computes its edges
+// with 8 warps inside the gather's own launch (rot_edges), so that the
+// same split sums in the same order and a stack's members equal separate
+// calls bit for bit.
 template <int MODE, bool EM, int WARPS>
 __global__ __launch_bounds__(WARPS * 32) void k_adjoint_edges(const float *__restrict__ s_am,
                                                               int s_ld, int R,
