@@ -196,8 +196,9 @@ __device__ __forceinline__ void rot_finish(const float (&accB)[ROWS], const floa
 // (barrier, then a device-scope fence by the counting thread); the CTA that
 // arrives last fences again, resets the counter and applies
 // x <- x * gsum * inv to the block, zeroing gsum there for the next call.
-// The adjoint leaves edge pixels to the caller (k_adjoint_edges).  No
-// thread waits on another CTA.  Every thread of the CTA calls this.
+// The adjoint's edge pixels are updated by the launch's edge CTAs
+// (rot_edges) or by the caller's edge kernel, never here.  No thread waits
+// on another CTA.  Every thread of the CTA calls this.
 template <int MODE, int ROWS>
 __device__ __forceinline__ void rot_em_finish(int row0, int col0, int N, float *__restrict__ gsum,
                                               float *__restrict__ x,
@@ -310,8 +311,9 @@ __device__ __forceinline__ int rot_rofs()
     return 4 * ROWS * (threadIdx.x >> 7) + ((threadIdx.x & 31) >> 3);
 }
 
-// MODE 0: backprojection; MODE 1: matched adjoint (edge pixels left to
-// k_adjoint_edges, as in gather_tile with edge_fixup).  Stages each chunk's
+// MODE 0: backprojection; MODE 1: matched adjoint (edge pixels left to the
+// edge CTAs, rot_edges, or to k_adjoint_edges, as in gather_tile with
+// edge_fixup).  Stages each chunk's
 // quads with loads from the sinogram.
 template <int MODE, int WMAX, int ROWS, bool EMF>
 __device__ __forceinline__ void gather_tile_rot(const float *__restrict__ s_am, int s_ld, int R,

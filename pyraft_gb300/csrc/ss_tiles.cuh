@@ -647,8 +647,8 @@ __device__ __forceinline__ void gather_tile(const float *__restrict__ s_am, int 
     const int myrow = row0 + warp * ROWS;
     // edge_fixup (adjoint modes): every tile takes the interior path and the
     // image's edge pixels (row or column 0 or N-1, the only pixels where the
-    // position-0 / N-1 validity rules apply) are left to k_adjoint_edges,
-    // which recomputes them with the rules; otherwise border tiles apply the
+    // position-0 / N-1 validity rules apply) are left to the edge kernels,
+    // which compute them with the rules; otherwise border tiles apply the
     // rules inline.
     const bool border = !edge_fixup &&
                         (row0 == 0 || col0 == 0 || row0 + TH >= N || col0 + kTile >= N);
