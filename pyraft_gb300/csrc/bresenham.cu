@@ -224,7 +224,9 @@ __device__ __forceinline__ void dda_set_t(DDA &it, double t)
 
 __device__ __forceinline__ bool dda_end(const DDA &it)
 {
-    return (it.i < 0) || (it.i >= it.lines) || (it.j < 0) || (it.j >= it.columns);
+    // i outside [0, lines) or j outside [0, columns): negative indices wrap
+    // to large unsigned values
+    return ((unsigned)it.i >= (unsigned)it.lines) | ((unsigned)it.j >= (unsigned)it.columns);
 }
 
 // ----------------------------------------------------------------------------
@@ -380,7 +382,9 @@ __device__ __forceinline__ int dda_walk(DDA &it, int cap, int fp64_walk, Visit &
 
 // ----------------------------------------------------------------------------
 
-template <bool RATIO>
+// I32: every pixel offset (row ics + column ils) fits in an int, so the
+// walk's per-pixel address is 32-bit arithmetic.
+template <bool RATIO, bool I32>
 __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__restrict__ cs_tab,
                                                     const float *__restrict__ img, long long ics,
                                                     long long ils, float *__restrict__ out,
@@ -398,8 +402,11 @@ __global__ __launch_bounds__(128) void k_bres_radon(DDAGeom g, const double *__r
     dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     float acc = 0.f, comp = 0.f;
     const int cap = 2 * (g.lines + g.columns) + 8;
+    const int ics32 = (int)ics, ils32 = (int)ils;
     dda_walk<kDdaSigma32>(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
-        const float x = __ldg(img + (long long)pi * ics + (long long)pj * ils) * sg;
+        const float *px = I32 ? img + (pi * ics32 + pj * ils32)
+                              : img + (long long)pi * ics + (long long)pj * ils;
+        const float x = __ldg(px) * sg;
         const float y = x - comp, t = acc + y;
         comp = (t - acc) - y;
         acc = t;
@@ -429,18 +436,22 @@ int launch_bres_radon(const DDAGeom &g, const double *d_cs, const float *img, lo
     const int nv = (g.A - first + stride - 1) / stride;
     if (nv <= 0) return RG_OK;
     dim3 grid((g.R + 127) / 128, nv);
-    if (y_am)
-        k_bres_radon<true><<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, y_am,
-                                                 first, stride, dda_fp64_walk());
-    else
-        k_bres_radon<false><<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, nullptr,
-                                                  first, stride, dda_fp64_walk());
+    // offsets of the image's pixels in 32 bits when they fit
+    const long long span = (long long)(g.lines - 1) * (ics < 0 ? -ics : ics) +
+                           (long long)(g.columns - 1) * (ils < 0 ? -ils : ils);
+    const bool i32 = span < (1LL << 31) - 1;
+    auto k = y_am ? (i32 ? k_bres_radon<true, true> : k_bres_radon<true, false>)
+                  : (i32 ? k_bres_radon<false, true> : k_bres_radon<false, false>);
+    k<<<grid, 128, 0, st>>>(g, d_cs, img, ics, ils, out, ocs, ols, y_am, first, stride,
+                            dda_fp64_walk());
     RG_CK_LAUNCH("k_bres_radon");
     return RG_OK;
 }
 
 // s(i, j) = s_am[j * R + i]; img_c: contiguous lines x columns, pre-zeroed.
-// den != nullptr: also accumulate the intersection lengths.
+// den != nullptr: also accumulate the intersection lengths.  I32: lines x
+// columns fits in an int, so pixel indices are 32-bit arithmetic.
+template <bool I32>
 __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double *__restrict__ cs_tab,
                                                         const float *__restrict__ s_am,
                                                         float *__restrict__ img_c, int first,
@@ -459,7 +470,8 @@ __global__ __launch_bounds__(128) void k_bres_transpose(DDAGeom g, const double 
     dda_set_t<kDdaSigma32>(it, __dadd_rn(g.stl_y, __dmul_rn((double)i, dts)));
     const int cap = 2 * (g.lines + g.columns) + 8;
     dda_walk<kDdaSigma32>(it, cap, fp64_walk, [&](int pi, int pj, float sg, int) {
-        const size_t e = (size_t)pi * g.columns + pj;
+        const long long e = I32 ? (long long)(pi * g.columns + pj)
+                                : (long long)pi * g.columns + pj;
         if (sv != 0.f) atomicAdd(img_c + e, sv * sg);
         if (den) atomicAdd(den + e, sg);
     });
@@ -520,8 +532,9 @@ int launch_bres_transpose(const DDAGeom &g, const double *d_cs, const float *s_a
     const int nv = (g.A - first + stride - 1) / stride;
     if (nv <= 0) return RG_OK;
     dim3 grid((g.R + 127) / 128, nv);
-    k_bres_transpose<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride, nullptr,
-                                           dda_fp64_walk());
+    auto k = (long long)g.lines * g.columns < (1LL << 31) ? k_bres_transpose<true>
+                                                          : k_bres_transpose<false>;
+    k<<<grid, 128, 0, st>>>(g, d_cs, s_am, img_c, first, stride, nullptr, dda_fp64_walk());
     RG_CK_LAUNCH("k_bres_transpose");
     return RG_OK;
 }
