@@ -32,6 +32,7 @@
 #include <cuda.h>
 #include <string.h>
 
+#include <algorithm>
 #include <climits>
 #include <mutex>
 #include <vector>
@@ -73,7 +74,8 @@ template <int EPI, int BW, int RPL>
 __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CUtensorMap tm_rows,
                                                    const __grid_constant__ CUtensorMap tm_cols,
                                                    int N, const View *__restrict__ views,
-                                                   const StBlock *__restrict__ blocks, int R,
+                                                   const StBlock *__restrict__ blocks,
+                                                   const unsigned *__restrict__ order, int R,
                                                    float *__restrict__ out_am, int out_ld,
                                                    const float *__restrict__ y_am, int y_ld,
                                                    long long zo, int *__restrict__ err,
@@ -88,14 +90,16 @@ __global__ __launch_bounds__(256, 3) void k_radon_tma(const __grid_constant__ CU
     __shared__ int s_lo, s_hi;
     __shared__ float red[kTmVpt][256];                 // cluster partials (split > 1)
 
-    const StBlock blk = blocks[blockIdx.y];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // split > 1: this CTA is rank `rank` of a cluster of `split` CTAs along x
     // that share the ray tile and view block; it walks its share of the
     // strips, and rank 0 sums the partials (distributed shared memory, rank
-    // order) and writes the epilogue
+    // order) and writes the epilogue.  The cluster's (ray tile, view block)
+    // comes from the plan's dispatch order (most lines first).
     const int rank = blockIdx.x % split;
-    const int k0 = (blockIdx.x / split) * kTmRays;
+    const unsigned ord = order[blockIdx.x / split + (gridDim.x / split) * blockIdx.y];
+    const StBlock blk = blocks[ord & 0xffffu];
+    const int k0 = (int)(ord >> 16) * kTmRays;
     constexpr int kRG = 32 / RPL;
     static_assert(RPL == 32 || RPL == 16 || RPL == 8, "rays per load");
     // pair m: ray k0 + 32 (warp & 1) + RPL (m % kRG) + lane % RPL,
@@ -324,6 +328,44 @@ static bool radon_kernel_direct()
     return e && !strcmp(e, "direct");
 }
 
+// Dispatch order of the TMA Radon's CTAs, as (ray tile << 16 | block): the
+// CTA of ray tile t and view block b walks the strips of lines that any of
+// its rays meets, so the central ray tiles of oblique views carry several
+// times the lines of the edge tiles.  Launched in grid order, the last wave
+// mixes heavy and light CTAs and the SMs that drew heavy ones finish late;
+// issued longest first (CTAs are dispatched in linear order), the last wave
+// holds the lightest CTAs.  A CTA's lines are estimated from its corner
+// rays (a ray's first and last line are monotone in its position on the
+// detector, so the corner rays bound the tile's).
+static std::vector<unsigned> st_cta_order(const std::vector<StBlock> &bl, const View *hv, int N,
+                                          int R)
+{
+    const int T = (R + kTmRays - 1) / kTmRays, nb = (int)bl.size();
+    std::vector<int> strips((size_t)T * nb, 0);
+    for (int b = 0; b < nb; ++b)
+        for (int t = 0; t < T; ++t) {
+            int Lo = INT_MAX, Hi = INT_MIN;
+            for (int c = 0; c < bl[b].count; ++c) {
+                const View &v = hv[bl[b].first + c];
+                for (int kk : {t * kTmRays, std::min(t * kTmRays + kTmRays - 1, R - 1)}) {
+                    int lo, hi;
+                    radon_line_range(v.r0 + (long long)kk * v.rk, v.ri, N, lo, hi);
+                    if (lo <= hi) {
+                        Lo = std::min(Lo, lo);
+                        Hi = std::max(Hi, hi);
+                    }
+                }
+            }
+            strips[(size_t)b * T + t] = Lo <= Hi ? Hi / kTmLines - Lo / kTmLines + 1 : 0;
+        }
+    std::vector<unsigned> order((size_t)T * nb);
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (unsigned)i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](unsigned a, unsigned b) { return strips[a] > strips[b]; });
+    for (unsigned &o : order) o = ((o % (unsigned)T) << 16) | (o / (unsigned)T);
+    return order;
+}
+
 int st_blocks_build(SSPlan &p, const View *hv)
 {
     p.nblocks = 0;
@@ -355,8 +397,12 @@ int st_blocks_build(SSPlan &p, const View *hv)
         // worth it only when blocks share their windows among several views
         if (!fits || (int)bl.size() > 65535 || nv < 6 * (int)bl.size()) continue;
         if (bw == 128 && nv < 12 * (int)bl.size()) continue;   // 256 packs more views
-        RG_CK(cudaMalloc(&p.d_blocks, sizeof(StBlock) * bl.size()));
-        RG_CK(cudaMemcpy(p.d_blocks, bl.data(), sizeof(StBlock) * bl.size(),
+        const std::vector<unsigned> order = st_cta_order(bl, hv, N, R);
+        const size_t bb = sizeof(StBlock) * bl.size();
+        RG_CK(cudaMalloc(&p.d_blocks, bb + sizeof(unsigned) * order.size()));
+        RG_CK(cudaMemcpy(p.d_blocks, bl.data(), bb, cudaMemcpyHostToDevice));
+        p.d_border = (const unsigned *)((char *)p.d_blocks + bb);
+        RG_CK(cudaMemcpy((void *)p.d_border, order.data(), sizeof(unsigned) * order.size(),
                          cudaMemcpyHostToDevice));
         p.nblocks = (int)bl.size();
         p.st_bw = bw;
@@ -455,7 +501,8 @@ static int launch_tma_rpl(const SSPlan &p, const CUtensorMap &tr, const CUtensor
     const int expire = test_switch("RG_TEST_EXPIRE_WAIT") ? 1 : 0;
     RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y, grid.z), 256, smem, st, split,
                      tr, tc, p.g.N, (const View *)p.d_views,
-                     (const StBlock *)p.d_blocks, p.g.R, out_am, out_ld, y_am, y_ld, zo,
+                     (const StBlock *)p.d_blocks, p.d_border, p.g.R, out_am, out_ld, y_am,
+                     y_ld, zo,
                      d_err, (unsigned)sizeof(float2), expire, split));
     RG_CK_LAUNCH("k_radon_tma");
     return RG_OK;

@@ -197,6 +197,9 @@ struct SSPlan {
     // TMA-staged Radon (radon_tma.cu): blocks of adjacent views whose line
     // windows fit st_bw entries (nblocks == 0: the direct kernels are used)
     void *d_blocks = nullptr;      // StBlock[nblocks], device
+    // the same allocation, after the blocks: the TMA Radon's CTA order,
+    // (ray tile << 16 | block) for ceil(R / 64) x nblocks CTAs, most lines first
+    const unsigned *d_border = nullptr;
     int nblocks = 0, st_bw = 0;
     // tile-driven Radon (radon_tma.cu): TtView records grouped by
     // orientation (rows first), device

@@ -179,6 +179,7 @@ void ss_plan_free(SSPlan &p)
     p.d_views = nullptr;
     if (p.d_blocks) cudaFree(p.d_blocks);
     p.d_blocks = nullptr;
+    p.d_border = nullptr;
     p.nblocks = 0;
     if (p.d_ovid) cudaFree(p.d_ovid);
     p.d_ovid = nullptr;

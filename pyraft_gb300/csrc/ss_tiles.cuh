@@ -71,7 +71,8 @@ __device__ __forceinline__ void kahan_add(float &sum, float &c, float x)
 // Lines i (in [0, N-1]) whose sample u0 + i*q lies in [-0.5, N - 0.5]: a
 // superset of the valid samples [0, N-1) with half a sample of margin,
 // checked exactly at both ends so every index used stays in [-1, N-1].
-__device__ __forceinline__ void radon_line_range(long long u0, long long q, int N, int &lo,
+// (Also called on the host, to estimate the TMA Radon's work per CTA.)
+__host__ __device__ __forceinline__ void radon_line_range(long long u0, long long q, int N, int &lo,
                                                  int &hi)
 {
     // float error of the estimate is < 1e-3 samples; the ends are then exact
