@@ -463,20 +463,23 @@ static int radon_rpl()
 }
 
 // Cluster size of the strip split for a grid of `ctas` CTAs at `slots`
-// resident CTAs.  Measured on GB300 (GUPS, split 1 / 2 / 4): 2048^2 x 1800
-// (8.1 waves unsplit) 3352 / 3383 / 3155; 1536^2 x 1080 3021 / 3131 / 2974;
-// 1024^2 x 1440 2737 / 2821 / 2630; 1024^2 x 720 (1.6 waves) 2452 / 2665 /
-// 2609; 512^2 x 360 1171 / 1449 / 1472.  Each rank repeats the CTA's set-up
-// (about 6 % of a CTA's work at 2048^2), which outweighs the fuller last
-// wave of a split of 4, so: 2 while the unsplit grid is under 10 waves and
-// each rank keeps at least 4 strips of kTmLines lines, else 1 (a stack of
-// 64 slices of 512^2 runs 26 waves).  RG_RADON_SPLIT_TMA=1|2|4 forces it.
+// resident CTAs.  Measured on GB300 with the CTAs dispatched longest first
+// (GUPS, split 1 / 2 / 4; waves of the unsplit grid): 2048^2 x 1800 (8.1)
+// 3462 / 3419 / 3195; 1536^2 x 1080 (3.6) 3297 / 3267 / 3036; 1024^2 x 1440
+// (3.2) 2993 / 2945 / 2668; 1024^2 x 720 (1.6) 2862 / 2873-2895 / 2665;
+// 512^2 x 360 (0.4) 916 / 1519 / 1628.  Each rank repeats the CTA's set-up
+// and the ranks' partials meet in distributed shared memory, so a split pays
+// only where the unsplit grid leaves SMs idle: 1 from 2.5 waves up, 2 from
+// one wave, else 4, with at least 4 strips of kTmLines lines per rank.
+// RG_RADON_SPLIT_TMA=1|2|4 forces it.
 static int tma_pick_split(long long ctas, int slots, int N)
 {
     const char *e = getenv("RG_RADON_SPLIT_TMA");
     const int forced = e ? atoi(e) : 0;
     if (forced == 1 || forced == 2 || forced == 4) return forced;
-    return (ctas < 10LL * slots && (N / kTmLines) / 2 >= 4) ? 2 : 1;
+    int s = ctas >= 5LL * slots / 2 ? 1 : ctas >= slots ? 2 : 4;
+    while (s > 1 && (N / kTmLines) / s < 4) s /= 2;
+    return s;
 }
 
 template <int EPI, int BW, int RPL>
