@@ -51,9 +51,9 @@ UPDATES = N * N * A
 # ncu's cache flush between kernels sends to DRAM) and the zeroed image that
 # the two partial sums per pixel are added to (16.8 MB).
 BP_TRAFFIC_BYTES = 14850304 + 46378496
-# kernels of one FBP step: k_to_am, k_filter_fft, k_pair_quads (which also
-# zeroes the output), k_gather_rot_tma
-LAUNCHES_PER_FBP = 4
+# kernels of one FBP step: k_to_am, k_filter_fft (which writes the
+# backprojection's quads and zeroes the output), k_gather_rot_tma
+LAUNCHES_PER_FBP = 3
 
 
 def smem_roofline(updates, ms, sms, sm_mhz, traffic, compulsory, hbm_peak, hbm_kind):
@@ -662,7 +662,11 @@ def main():
         return t0.elapsed_time(t1) / K
 
     run_stream(warm)
-    p_ms = run_stream(args.steps)
+    # three runs of `steps` slices each, the median reported: one run's
+    # throughput follows the host thread that enqueues it, and a stall of
+    # that thread (seen once in tens of runs) starves the streams
+    p_runs = [run_stream(args.steps) for _ in range(3)]
+    p_ms = statistics.median(p_runs)
     if dist:
         t = torch.tensor([p_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -691,7 +695,8 @@ def main():
                 "mode": "streamed slices: step k+1's upload and step k-1's download overlap "
                         "step k's FBP (two buffer sets, three CUDA streams); L2 flushed before "
                         "every FBP inside the timed region; time = first upload to last "
-                        "download over all steps",
+                        "download over all steps; the median of three such runs",
+                "runs_ms_per_step": [round(x, 4) for x in p_runs],
                 "serial": {"value": round(world * UPDATES / (e_ms * 1e-3) / 1e9, 3),
                            "ms_per_step": round(e_ms, 4),
                            "mode": "upload, FBP, download back to back on one stream, "

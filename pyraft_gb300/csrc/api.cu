@@ -1012,6 +1012,19 @@ size_t rg_fbp_workspace(rg_image sino, rg_image image, int kind)
     return ws_total({b, b, quads_ws(sino)});
 }
 
+}  // extern "C"
+namespace rg {
+// RG_FBP_QUADS=0 (read per call) keeps the FBP's filter and the gather's quad
+// prepass as separate launches: the reference arrangement for tests, which
+// must give the same bits.
+static bool fbp_quads_enabled()
+{
+    const char *e = getenv("RG_FBP_QUADS");
+    return !(e && e[0] == '0' && e[1] == 0);
+}
+}  // namespace rg
+extern "C" {
+
 int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *stream)
 {
     RG_TRACE();
@@ -1035,11 +1048,34 @@ int rg_fbp(rg_image sino, rg_image image, int kind, void *ws, size_t wsb, void *
         rc = launch_to_am(sino.data, sino.column_stride, sino.line_stride, R, A, a, st);
         src = a;
     }
-    if (!rc && !(rc = filter_rows(kind, src, b, R, A, taps, st)) &&
-        !(rc = autotune_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
-                               st, quads)))
-        rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride, image.line_stride,
-                           nullptr, nullptr, nullptr, st, 0, Stack(), quads);
+    // The gather's launch shape is tuned (the first call for a geometry)
+    // before the filter runs, on the unfiltered rows: its timings do not
+    // depend on the data.
+    if (!rc)
+        rc = autotune_gather(ph->p, 0, src, R, image.data, image.column_stride,
+                             image.line_stride, st, quads);
+    if (!rc) {
+        if (taps->fft_p && !taps->fft_circ && fbp_quads_enabled() &&
+            gather_quads_form(ph->p, quads)) {
+            // the FFT filter writes the paired gather's quads and zeroes the
+            // image itself: the filtered rows are never stored, and the
+            // gather's prepass launch is not needed
+            rc = launch_filter_fft_quads(src, R, A, taps->fft_p, (const float2 *)taps->p,
+                                         taps->h0, (const View *)ph->p.d_views, ph->p.nv / 2,
+                                         ph->p.g.A / 2, (float4 *)quads, image.data, ph->p.g.N,
+                                         image.column_stride, image.line_stride, st);
+            if (!rc) {
+                QuadsPrefilled given;
+                rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride,
+                                   image.line_stride, nullptr, nullptr, nullptr, st, 0, Stack(),
+                                   quads);
+            }
+        } else if (!(rc = filter_rows(kind, src, b, R, A, taps, st))) {
+            rc = launch_gather(ph->p, 0, b, R, image.data, image.column_stride,
+                               image.line_stride, nullptr, nullptr, nullptr, st, 0, Stack(),
+                               quads);
+        }
+    }
     scratch_end(s);
     return rc;
 }

@@ -16,7 +16,7 @@
 // FFMAs) and the 511 taps it meets are staged in shared memory; each thread
 // keeps 16 accumulators, i.e. 16 FFMA per 1 + 4 shared loads.  Per-tile
 // partial sums are added with Kahan compensation.
-#include "rg_internal.cuh"
+#include "ss_tiles.cuh"
 
 namespace rg {
 
@@ -399,10 +399,28 @@ __device__ __forceinline__ void fft_mid_pass(float2 *z, int p, const float2 *__r
     }
 }
 
+// QUADS (the FBP form, launch_filter_fft_quads): the CTA of view pair j
+// transforms sinogram rows views[j].view and views[j].view + roff, the rows
+// of a view and its partner a quarter turn on, and writes the pair's quads
+// for the paired backprojection instead of the filtered rows: entry e < R - 1
+// holds both rows' sample pairs at e, the float4 that the gather's prepass
+// (k_pair_quads<0>) builds from the filtered rows, bit for bit.  The CTAs
+// also zero the N x N output that the gather adds its partial sums to, as
+// that prepass does.  Linear convolution only (circ false).
+struct FilterQuads {
+    const View *views;
+    int roff;
+    float4 *quads;
+    float *zout;
+    int N;
+    long long cs, ls;
+};
+
+template <bool QUADS>
 __global__ __launch_bounds__(kFftThreads) void k_filter_fft(const float *__restrict__ in,
                                                             float *__restrict__ out, int R, int A,
                                                             int p, const float2 *__restrict__ tab,
-                                                            float g0, bool circ)
+                                                            float g0, bool circ, FilterQuads fq)
 {
     pdl_gate();
     extern __shared__ __align__(16) float2 z[];          // [M + M/16]
@@ -410,10 +428,10 @@ __global__ __launch_bounds__(kFftThreads) void k_filter_fft(const float *__restr
     const int M = 1 << p, H = M >> 1, t = threadIdx.x;
     const float2 *__restrict__ tw = tab;
     const float2 *__restrict__ gb = tab + H;
-    const int a0 = 2 * blockIdx.x;
-    const bool two = a0 + 1 < A;
+    const int a0 = QUADS ? fq.views[blockIdx.x].view : 2 * blockIdx.x;
+    const bool two = QUADS || a0 + 1 < A;
     const float *__restrict__ x = in + (size_t)a0 * R;
-    const float *__restrict__ y = x + R;                 // read only when `two`
+    const float *__restrict__ y = x + (size_t)(QUADS ? fq.roff : 1) * R;   // read only when `two`
 
     // v[n] for n in [0, R), else 0
     auto v = [&](int n) {
@@ -485,14 +503,36 @@ __global__ __launch_bounds__(kFftThreads) void k_filter_fft(const float *__restr
 #pragma unroll
     for (int w = 0; w < kFftThreads / 32; ++w) tot = cadd(tot, wsum[w]);
     const float dcx = tot.x * g0, dcy = tot.y * g0;
-    float *__restrict__ ox = out + (size_t)a0 * R;
-    for (int n = t; n < R; n += kFftThreads) {
-        // n >= H only in the circular form (R = M)
-        const int n0 = n < H ? n : n - H;
-        const float2 u = cmulc(z[fpad(n0 + H)], __ldg(tw + n0));
-        const float2 r = n < H ? cadd(z[fpad(n0)], u) : csub(z[fpad(n0)], u);
-        ox[n] = r.x + dcx;
-        if (two) ox[R + n] = r.y + dcy;
+    if constexpr (QUADS) {
+        // output n < R <= H reads z[n] and z[n + H] only: store it in z[n]
+        for (int n = t; n < R; n += kFftThreads) {
+            const float2 u = cmulc(z[fpad(n + H)], __ldg(tw + n));
+            const float2 r = cadd(z[fpad(n)], u);
+            z[fpad(n)] = make_float2(r.x + dcx, r.y + dcy);
+        }
+        __syncthreads();
+        float4 *__restrict__ qd = fq.quads + (size_t)blockIdx.x * (R - 1);
+        for (int e = t; e < R - 1; e += kFftThreads) {
+            const float2 s0 = z[fpad(e)], s1 = z[fpad(e + 1)];
+            const float2 a = make_pair(s0.x, s1.x, true), b = make_pair(s0.y, s1.y, true);
+            qd[e] = make_float4(a.x, a.y, b.x, b.y);
+        }
+        const long long n = (long long)fq.N * fq.N;
+        for (long long i = (long long)blockIdx.x * kFftThreads + t; i < n;
+             i += (long long)gridDim.x * kFftThreads) {
+            const int r = (int)(i / fq.N), c = (int)(i - (long long)r * fq.N);
+            fq.zout[(long long)r * fq.cs + (long long)c * fq.ls] = 0.f;
+        }
+    } else {
+        float *__restrict__ ox = out + (size_t)a0 * R;
+        for (int n = t; n < R; n += kFftThreads) {
+            // n >= H only in the circular form (R = M)
+            const int n0 = n < H ? n : n - H;
+            const float2 u = cmulc(z[fpad(n0 + H)], __ldg(tw + n0));
+            const float2 r = n < H ? cadd(z[fpad(n0)], u) : csub(z[fpad(n0)], u);
+            ox[n] = r.x + dcx;
+            if (two) ox[R + n] = r.y + dcy;
+        }
     }
 }
 
@@ -502,10 +542,28 @@ int launch_filter_fft(const float *in_am, float *out_am, int R, int A, int p, co
     if (p < 2 || p > kFilterFftMaxLog || (circ ? (1 << p) != R : (1 << p) < 2 * R - 1))
         return set_error(RG_EUNSUPPORTED, "filter FFT: bad transform size 2^%d for %d rays", p, R);
     const size_t smem = sizeof(float2) * (((size_t)1 << p) + ((size_t)1 << p) / 16);
-    RG_CK(cudaFuncSetAttribute(k_filter_fft, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    RG_CK(cudaFuncSetAttribute(k_filter_fft<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)smem));
-    RG_CK(launch_pdl(k_filter_fft, (A + 1) / 2, kFftThreads, smem, st, 1, in_am, out_am, R, A, p,
-                     d_tab, g0, circ));
+    RG_CK(launch_pdl(k_filter_fft<false>, (A + 1) / 2, kFftThreads, smem, st, 1, in_am, out_am, R,
+                     A, p, d_tab, g0, circ, FilterQuads{}));
+    RG_CK_LAUNCH("k_filter_fft");
+    return RG_OK;
+}
+
+int launch_filter_fft_quads(const float *in_am, int R, int A, int p, const float2 *d_tab, float g0,
+                            const View *d_views, int pairs, int roff, float4 *quads, float *out,
+                            int N, long long cs, long long ls, cudaStream_t st)
+{
+    if (p < 2 || p > kFilterFftMaxLog || (1 << p) < 2 * R - 1)
+        return set_error(RG_EUNSUPPORTED, "filter FFT: bad transform size 2^%d for %d rays", p, R);
+    if (pairs < 1 || roff < 1 || roff >= A)
+        return set_error(RG_EINVAL, "filter quads: %d view pairs %d rows apart in %d views",
+                         pairs, roff, A);
+    const size_t smem = sizeof(float2) * (((size_t)1 << p) + ((size_t)1 << p) / 16);
+    RG_CK(cudaFuncSetAttribute(k_filter_fft<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)smem));
+    RG_CK(launch_pdl(k_filter_fft<true>, pairs, kFftThreads, smem, st, 1, in_am, nullptr, R, A, p,
+                     d_tab, g0, false, FilterQuads{d_views, roff, quads, out, N, cs, ls}));
     RG_CK_LAUNCH("k_filter_fft");
     return RG_OK;
 }

@@ -70,6 +70,10 @@ constexpr int kStages = 2;                // TMA window buffers (double bufferin
 // subsets of 36 pairs and 64-slice stacks of 180 pairs).
 constexpr int kTmaMinPairs = 256;
 
+// Set by QuadsPrefilled: the backprojection's quads and zeroed output were
+// written by the FBP filter, so the TMA-staged gather skips its prepass.
+thread_local bool t_quads_prefilled = false;
+
 __global__ void k_zero_image(float *__restrict__ out, int N, long long cs, long long ls,
                              long long zo)
 {
@@ -688,7 +692,7 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     int *ec = em ? em->cnt : nullptr;
     const int N = p.g.N, R = p.g.R, half = p.nv / 2, roff = p.g.A / 2;
     const int Rq = quad_entries(MODE, R);
-    {
+    if (!(MODE == 0 && t_quads_prefilled)) {
         dim3 g((Rq + 255) / 256, half, z.n);
         RG_CK(launch_pdl(k_pair_quads<MODE>, g, 256, 0, st, 1, s_am, s_ld, z.in, R, p.d_views,
                          half, roff, quads, zero_out ? out : nullptr, N, cs, ls, z.out));
@@ -740,6 +744,14 @@ bool gather_rot_use_tma(int pairs)
     return pairs >= kTmaMinPairs;
 }
 
+// The TMA-staged form serves (plan, mode, tile height) with quad scratch.
+bool tma_form(const SSPlan &p, int mode, int rows, bool quads)
+{
+    const int t = rows == 16 ? 2 : rows == 8 ? 1 : 0;
+    const int w = mode == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
+    return quads && quad_box(w) <= kQuadBox && p.nv / 2 <= 65535 && gather_rot_use_tma(p.nv / 2);
+}
+
 template <int MODE, int ROWS>
 int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, long long cs,
                     long long ls, int *d_err, cudaStream_t st, const Stack &z, void *quads,
@@ -747,9 +759,11 @@ int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
 {
     const int t = ROWS == 16 ? 2 : ROWS == 8 ? 1 : 0;
     const int w = MODE == 0 ? p.wmax_bp[t] : p.wmax_adj[t];
-    if (quads && quad_box(w) <= kQuadBox && p.nv / 2 <= 65535 && gather_rot_use_tma(p.nv / 2))
+    if (tma_form(p, MODE, ROWS, quads != nullptr))
         return gather_rot_tma<MODE, ROWS>(p, s_am, s_ld, out, cs, ls, d_err, st, z,
                                           (float4 *)quads, w, zero_out, em, edges);
+    if (MODE == 0 && t_quads_prefilled)
+        return set_error(RG_EINVAL, "prefilled quads for a backprojection that stages by loads");
     if (zero_out)
         if (int rc = launch_zero_image(out, p.g.N, cs, ls, st, z)) return rc;
     if (w <= 64)
@@ -766,6 +780,14 @@ int gather_rot_rows(const SSPlan &p, const float *s_am, int s_ld, float *out, lo
 }
 
 }  // namespace
+
+QuadsPrefilled::QuadsPrefilled() { t_quads_prefilled = true; }
+QuadsPrefilled::~QuadsPrefilled() { t_quads_prefilled = false; }
+
+bool gather_quads_form(const SSPlan &p, void *quads)
+{
+    return quads && p.rot_ok && gather_rot_enabled() && tma_form(p, 0, tuned_rows(p, 0), true);
+}
 
 int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_t st,
                       const Stack &z)

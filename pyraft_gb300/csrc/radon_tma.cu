@@ -371,7 +371,8 @@ int st_blocks_build(SSPlan &p, const View *hv)
     p.nblocks = 0;
     p.st_bw = 0;
     const int N = p.g.N, R = p.g.R, nv = p.nv;
-    if (nv < 1) return RG_OK;
+    // the dispatch order packs the ray tile into 16 bits
+    if (nv < 1 || (R + kTmRays - 1) / kTmRays > 65535) return RG_OK;
     for (int bw : {128, 256}) {
         std::vector<StBlock> bl;
         bool fits = true;

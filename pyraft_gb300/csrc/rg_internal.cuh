@@ -360,6 +360,20 @@ int launch_gather_rot(const SSPlan &p, int mode, const float *s_am, int s_ld, fl
 // Whether launch_gather takes the paired path where a plan allows it
 // (RG_GATHER_ROT=0 turns it off).
 bool gather_rot_enabled();
+// Whether a one-slice backprojection (mode 0) with quad scratch runs the
+// TMA-staged paired gather (at the tuned launch shape), whose prepass
+// (quads from the filtered rows, output zeroed) the FBP filter can do in
+// its epilogue (launch_filter_fft_quads).
+bool gather_quads_form(const SSPlan &p, void *quads);
+// While alive, the calling thread's backprojection gathers of that form
+// take the quads and the zeroed output as given and skip their prepass; a
+// backprojection that would stage otherwise fails with RG_EINVAL.
+struct QuadsPrefilled {
+    QuadsPrefilled();
+    ~QuadsPrefilled();
+    QuadsPrefilled(const QuadsPrefilled &) = delete;
+    QuadsPrefilled &operator=(const QuadsPrefilled &) = delete;
+};
 // Zero an N x N strided image (a stack of z.n, z.out apart).
 int launch_zero_image(float *out, int N, long long cs, long long ls, cudaStream_t st,
                       const Stack &z);
@@ -408,6 +422,13 @@ int launch_ramlak_rows(const float *in_am, float *out_am, int R, int A, const fl
 constexpr int kFilterFftMaxLog = 14;
 int launch_filter_fft(const float *in_am, float *out_am, int R, int A, int p, const float2 *d_tab,
                       float g0, bool circ, cudaStream_t st);
+// The same filter (linear form) for the FBP: CTA j filters rows
+// d_views[j].view and d_views[j].view + roff of in_am (j < pairs) and writes
+// the paired backprojection's quads[j][e] (e < R - 1) instead of the rows,
+// and the CTAs zero the N x N output (strides cs, ls).
+int launch_filter_fft_quads(const float *in_am, int R, int A, int p, const float2 *d_tab, float g0,
+                            const View *d_views, int pairs, int roff, float4 *quads, float *out,
+                            int N, long long cs, long long ls, cudaStream_t st);
 
 // bresenham.cu
 struct DDAGeom {

@@ -10,6 +10,10 @@
   update pass) against the FP64 oracle restatement of make_em
   (pyraft/iterative/em.py:109-144): 50 iterations at 512^2 and 5 at
   1024^2 x 720 (the EM bench slice).  Tolerance rel-L2 <= 1e-4.
+- The DDA Radon, its transpose and the normalised DDA backprojection
+  (pyraft's default method) at the benchmarked 2048^2 image and 2048 rays,
+  on 60 views: full-length rays of 2048 to 2900 pixels summed in
+  compensated FP32, against the FP64 oracle.  Tolerance rel-L2 <= 1e-6.
 - The batched uneven OSEM with a 2048^2 x 1800 slice among smaller ones:
   every slice against the one-slice OSEM (rg_em) on the same subsets to
   rel-L2 <= 1e-5 (FP32 atomic ray sums in both), and the smallest slice
@@ -54,7 +58,7 @@ def emission(n, a, seed, ellipses=12):
     return rng.poisson(np.maximum(p, 0) * 50.0 / max(p.mean(), 1e-9)).astype(np.float64)
 
 
-def test_fbp_2048x1800_sampled_rows_vs_oracle(orc):
+def test_fbp_2048x1800_sampled_rows_vs_oracle(orc, monkeypatch):
     N, A, R = 2048, 1800, 2048
     rng = np.random.default_rng(1234)
     desc = rg.random_ellipses(40, rng)
@@ -77,6 +81,15 @@ def test_fbp_2048x1800_sampled_rows_vs_oracle(orc):
     assert L.rg_device_status() == 0
     got = d_img.double().cpu().numpy()
     assert np.isfinite(got).all()
+    # the filter writing the gather's quads (the default) and the filter's
+    # rows plus the gather's prepass (RG_FBP_QUADS=0) agree to FP32 rounding
+    # (the fused filter transforms each view with its partner a quarter turn
+    # on instead of its neighbour)
+    monkeypatch.setenv("RG_FBP_QUADS", "0")
+    d_img.fill_(float("nan"))
+    _native.check(L.rg_fbp(S, I, _native.RG_FILTER_RAMLAK, ws.data_ptr(), wsb, sp))
+    torch.cuda.synchronize()
+    assert rel(d_img.double().cpu().numpy(), got) <= 1e-6
 
     q = orc.ramlak(sino.astype(np.float64), 2.0 / (R - 1))
     row0, step, count = 16, 32, 64
@@ -102,6 +115,27 @@ def test_em_512x720_50_iterations_vs_oracle(orc):
 
 def test_em_1024x720_vs_oracle(orc):
     assert _em_vs_oracle(orc, 1024, 720, 5, 32) <= 1e-4
+
+
+def test_dda_operators_2048_full_length_rays_vs_oracle(orc):
+    """raft/raft_radon_bresenham.cpp:16-105, raft/raft_radon_transpose_
+    bresenham.cpp:17-201 and raft/raft_backprojection_bresenham.cpp:17-251 at
+    a 2048^2 image and 2048 rays over 60 views of [0, pi) (view 0 included,
+    as the oracle restates it)."""
+    N, R, A = 2048, 2048, 60
+    BRES = rg.radon_method.BRESENHAM
+    rng = np.random.default_rng(2048)
+    x = rng.random((N, N))
+    got = np.asarray(rg.radon(rg.image(x), (R, A), BRES))
+    assert rel(got, orc.radon_bresenham(x, R, A)) <= 1e-6
+    y = rng.random((R, A))
+    s = rg.image(y, **SINO_C)
+    got = np.asarray(rg.radon_transpose(s, (N, N), BRES))
+    assert rel(got, orc.radon_transpose_bresenham(y, (N, N))) <= 1e-6
+    got = np.asarray(rg.backprojection(s, (BRES, (N, N), 0)))
+    want = orc.backprojection_bresenham(y, (N, N))
+    assert rel(got, np.where(np.isfinite(want), want, 0.0)) <= 1e-6
+    assert _native.load().rg_device_status() == 0
 
 
 def test_batch_with_a_2048x1800_slice(orc):

@@ -430,6 +430,47 @@ def test_paired_gathers_overwrite_the_output(orc, monkeypatch):
             assert rel(out.cpu().numpy(), ref) <= 1e-5
 
 
+@pytest.mark.parametrize("n,r,a,view_major", [(128, 128, 600, False), (96, 96, 720, True),
+                                              (160, 120, 512, False), (64, 64, 300, False)])
+def test_fbp_filter_writes_the_quads(orc, monkeypatch, n, r, a, view_major):
+    """rg_fbp with the TMA-staged paired backprojection (>= 256 view pairs):
+    the FFT filter writes the gather's quads and zeroes the image in its own
+    epilogue, so the filtered rows are never stored and the gather's prepass
+    does not run.  RG_FBP_QUADS=0 keeps the filter's rows and the prepass.
+    The two agree to FP32 rounding (1e-6: the fused filter transforms each
+    view together with its partner a quarter turn on, not with its
+    neighbour, and a complex transform's rounding mixes its two real rows),
+    into an output full of NaN, from a ray-major and a view-major sinogram,
+    and both match the oracle's Ram-Lak backprojection inside the image's
+    border (1e-5)."""
+    from pyraft_gb300.raftypes import rg_image
+    rng = np.random.default_rng(n + r + a)
+    s = inner_sino(rng, r, a)
+    L = _native.load()
+    st = torch.cuda.current_stream().cuda_stream
+    s_dev = torch.from_numpy(s.astype(np.float32)).cuda()
+    if view_major:
+        s_dev = s_dev.t().contiguous().t()        # columns (views) contiguous
+    S = rg_image(rg.gpu_image(s_dev, *SINO_C))
+    out = {}
+    for fuse in ("1", "0"):
+        monkeypatch.setenv("RG_FBP_QUADS", fuse)
+        img = torch.full((n, n), float("nan"), device="cuda")
+        _native.check(L.rg_fbp(S, rg_image(rg.gpu_image(img)), _native.RG_FILTER_RAMLAK,
+                               None, 0, st))
+        torch.cuda.synchronize()
+        out[fuse] = img.cpu().numpy()
+    assert L.rg_device_status() == 0
+    assert np.isfinite(out["1"]).all()
+    assert rel(out["1"], out["0"]) <= 1e-6
+    # the filtered sinogram's first and last rays are not zero: the image's
+    # border pixels meet them exactly at the detector's validity limit, where
+    # the oracle's FP64 rounding decides, so the border is left out
+    want = orc.backprojection_slantstack(orc.ramlak(s, 2.0 / (r - 1)), n)[1:-1, 1:-1]
+    assert rel(out["1"][1:-1, 1:-1], want) <= 1e-5
+    assert rel(out["0"][1:-1, 1:-1], want) <= 1e-5
+
+
 @pytest.mark.parametrize("n,r,a", [(2, 2, 2), (5, 5, 4), (17, 17, 10), (33, 20, 30), (40, 40, 2)])
 def test_gathers_quarter_turn_small_geometries(orc, monkeypatch, n, r, a):
     """Paired gathers on images much smaller than a tile, and with a single
