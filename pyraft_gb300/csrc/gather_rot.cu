@@ -150,7 +150,7 @@ template <int MODE, int ROWS>
 __device__ __forceinline__ void rot_finish(const float (&accB)[ROWS], const float (&accA)[ROWS],
                                            float *red, int split, int rank, int myrow, int col,
                                            int N, float *__restrict__ out, long long cs,
-                                           long long ls, float scale)
+                                           long long ls, float scale, bool active = true)
 {
     if (split > 1) {
         namespace cg = cooperative_groups;
@@ -180,6 +180,7 @@ __device__ __forceinline__ void rot_finish(const float (&accB)[ROWS], const floa
         cl.sync();    // no CTA leaves while a peer still reads its partials
         return;
     }
+    if (!active) return;   // the other half of a half-tile CTA's rows
 #pragma unroll
     for (int r = 0; r < ROWS; ++r) {
         const int row = myrow + 4 * r;
@@ -531,7 +532,8 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
                                                         const float *__restrict__ em_inv,
                                                         int *em_cnt,
                                                         const float *__restrict__ s_am, int s_ld,
-                                                        int R, long long zs, int edge_rows)
+                                                        int R, long long zs, int edge_rows,
+                                                        int nfull, int nhalf)
 {
     pdl_gate();
     if (MODE == 1 && (int)blockIdx.y >= (int)gridDim.y - edge_rows) {
@@ -539,6 +541,26 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
                        cs, ls, em_x, em_inv, edge_rows);
         return;
     }
+    // Tiles in launch order.  nhalf > 0 (the backprojection of one slice,
+    // no cluster split, no fused update): the first nfull CTAs take whole
+    // tiles, the next 2 nhalf the last nhalf tiles by halves (`part` 0: the
+    // rows of warps 0-3, 1: those of warps 4-7), so that the launch's last
+    // wave spreads evenly over the SMs; the grid's spare CTAs return here.
+    // (The adjoint's launches, split over clusters where the tuner finds it
+    // faster, compile without it.)
+    int tx = blockIdx.x / split, ty = blockIdx.y, part = -1;
+    if (MODE == 0 && nhalf > 0) {
+        int t = blockIdx.y * gridDim.x + blockIdx.x;
+        if (t >= nfull) {
+            const int h = t - nfull;
+            if (h >= 2 * nhalf) return;                 // CTA-uniform, before any barrier
+            t = nfull + (h >> 1);
+            part = h & 1;
+        }
+        tx = t % gridDim.x;
+        ty = t / gridDim.x;
+    }
+    const bool active = MODE != 0 || part < 0 || (int)(threadIdx.x >> 7) == part;
     extern __shared__ __align__(128) float4 qbuf[];   // [kStages][kPairSlots][wb]
     __shared__ __align__(8) unsigned long long full[kStages];
     __shared__ SlotInfo slot[kStages][kPairSlots];
@@ -546,7 +568,7 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
     constexpr int TH = kWarps * ROWS;
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int rank = blockIdx.x % split, tx = blockIdx.x / split, ty = blockIdx.y;
+    const int rank = blockIdx.x % split;
     const int z = blockIdx.z;
     out += (long long)z * zo;
     const int row0 = ty * TH, col0 = tx * kTile;
@@ -615,7 +637,7 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
         // stay inside it), and the call reports the error.
         const bool ok = (expire_first && c == 0) ? false
                                                  : mbar_wait(smem_addr(&full[b]), (c / kStages) & 1);
-        const int nslot = min(kPairSlots, vend - (vbeg + c * kPairSlots));
+        const int nslot = active ? min(kPairSlots, vend - (vbeg + c * kPairSlots)) : 0;
         for (int s = 0; s < nslot; ++s) {
             const SlotInfo si = slot[b][s];
             if (si.nlo == INT_MIN) continue;
@@ -639,7 +661,7 @@ __global__ __launch_bounds__(256) void k_gather_rot_tma(const __grid_constant__ 
         __syncthreads();
     }
     rot_finish<MODE, ROWS>(accB, accA, reinterpret_cast<float *>(qbuf), split, rank, myrow, col,
-                           N, out, cs, ls, scale);
+                           N, out, cs, ls, scale, active);
     if (EMF) rot_em_finish<MODE, ROWS>(row0, col0, N, out, em_x, em_inv, em_cnt, 2 * split);
 }
 
@@ -677,6 +699,28 @@ int gather_rot_w(const SSPlan &p, const float *s_am, int s_ld, float *out, long 
                      scale, out, cs, ls, d_err, z.in, z.out, pb, split, ex, ei, ec, er));
     RG_CK_LAUNCH("k_gather_rot");
     return RG_OK;
+}
+
+// RG_GATHER_HALF_TILES=0 (read per call) launches whole tiles only.
+bool half_tiles_enabled()
+{
+    const char *e = getenv("RG_GATHER_HALF_TILES");
+    return !(e && e[0] == '0' && e[1] == 0);
+}
+
+// SMs of the current device (cached per device).
+int sm_count()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (!cache[dev]) {
+        int n = 0;
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            return 0;
+        cache[dev] = n;
+    }
+    return cache[dev];
 }
 
 // TMA box width for a window bound w: a multiple of 8 entries (128 bytes).
@@ -727,9 +771,25 @@ int gather_rot_tma(const SSPlan &p, const float *s_am, int s_ld, float *out, lon
     const unsigned qb = (unsigned)sizeof(float4);
     const float scale = MODE == 0 ? p.dth : 1.f;
     const int er = edge_rows_for(N, (int)grid.x * split, MODE == 1 && edges);
-    RG_CK(launch_pdl(k, dim3(grid.x * split, grid.y + er, grid.z), 256, smem, st, split,
+    // Uniform tiles leave the last wave uneven: T tiles over S SMs put
+    // floor(T / S) or one more on each SM.  The backprojection of one slice
+    // without a cluster split or fused update runs its last T mod S tiles
+    // as half tiles (two CTAs each), which the SMs that finish first pick
+    // up: 2048^2 x 1800 (2048 tiles, 72 in halves) 1.797 -> 1.748 ms.
+    int nfull = 0, nhalf = 0;
+    dim3 g = grid;
+    if (MODE == 0 && split == 1 && !em && z.n == 1 && half_tiles_enabled()) {
+        const int T = (int)(grid.x * grid.y), S = sm_count();
+        if (S > 0 && T > S && T % S) {
+            nhalf = T % S;
+            nfull = T - nhalf;
+            g.y = (unsigned)((nfull + 2 * nhalf + (int)grid.x - 1) / (int)grid.x);
+        }
+    }
+    RG_CK(launch_pdl(k, dim3(g.x * split, g.y + er, g.z), 256, smem, st, split,
                      tm, (const View *)p.d_views, half, N, scale, out, cs, ls,
-                     d_err, z.out, wb, qb, split, expire, ex, ei, ec, s_am, s_ld, R, z.in, er));
+                     d_err, z.out, wb, qb, split, expire, ex, ei, ec, s_am, s_ld, R, z.in, er,
+                     nfull, nhalf));
     RG_CK_LAUNCH("k_gather_rot_tma");
     return RG_OK;
 }

@@ -471,6 +471,29 @@ def test_fbp_filter_writes_the_quads(orc, monkeypatch, n, r, a, view_major):
     assert rel(out["0"][1:-1, 1:-1], want) <= 1e-5
 
 
+@pytest.mark.parametrize("n,a", [(1000, 600), (777, 520)])
+def test_backprojection_half_tile_tail(orc, monkeypatch, n, a):
+    """The TMA-staged paired backprojection of one slice without a cluster
+    split runs its last (tiles mod SMs) tiles as half tiles, two CTAs each,
+    each summing the rows of four of the tile's eight warps.  Every pixel
+    still gets exactly two partial sums (its tile's and its quarter-turned
+    tile's), so the result must be the same bits as with whole tiles only
+    (RG_GATHER_HALF_TILES=0), and match the oracle.  On 152 SMs: 1000^2 is
+    512 tiles of 32 x 64 pixels, 56 of them in halves; 777^2 is 25 x 13 =
+    325 tiles (partial ones at the right and bottom), 21 in halves."""
+    rng = np.random.default_rng(n + a)
+    s = inner_sino(rng, n, a)
+    monkeypatch.setenv("RG_GATHER_ROWS", "8")
+    monkeypatch.setenv("RG_GATHER_SPLIT", "1")
+    outs = {}
+    for ht in ("1", "0"):
+        monkeypatch.setenv("RG_GATHER_HALF_TILES", ht)
+        outs[ht] = np.asarray(rg.backprojection(sino_img(s), (SLANT, (n, n), 0)))
+    assert _native.load().rg_device_status() == 0
+    assert np.array_equal(outs["1"], outs["0"])
+    assert rel(outs["1"], orc.backprojection_slantstack(s, n)) <= 1e-5
+
+
 @pytest.mark.parametrize("n,r,a", [(2, 2, 2), (5, 5, 4), (17, 17, 10), (33, 20, 30), (40, 40, 2)])
 def test_gathers_quarter_turn_small_geometries(orc, monkeypatch, n, r, a):
     """Paired gathers on images much smaller than a tile, and with a single
