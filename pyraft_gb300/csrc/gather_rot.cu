@@ -38,10 +38,20 @@
 // pair][sample entry], and the gather (k_gather_rot_tma) loads each view
 // pair's window as one TMA box into shared memory, double-buffered on two
 // mbarriers, so the next chunk of 16 pairs streams in while the current one
-// is summed and no thread spends issue slots on staging.  Without that
+// is summed and no thread spends issue slots on staging.  (In the FBP the
+// FFT filter writes the quads and zeroes the output in its epilogue, and
+// the gather runs without its prepass: QuadsPrefilled.)  Without that
 // scratch, below kTmaMinPairs view pairs (where the prepass launch and the
 // pipeline fill cost more) or for windows wider than a TMA box,
 // k_gather_rot stages the quads itself with loads from the sinogram.
+//
+// Tail.  T uniform tiles over S SMs put floor(T / S) or one more tile on
+// each SM, so with whole tiles the SMs that drew fewer idle through the last
+// tile-time.  The TMA backprojection of one slice without a cluster split
+// runs its last T mod S tiles as half tiles, two CTAs each (the rows of
+// warps 0-3, or of warps 4-7, summed; the other warps only stage and wait),
+// which the SMs that finish first pick up.  Every pixel still receives
+// exactly two partial sums, so the bits are those of whole tiles.
 //
 // Precision: both kernels sum straight into FP32 accumulators (in
 // k_gather_rot_tma, per-chunk partial sums would cost 2 ROWS registers: 48

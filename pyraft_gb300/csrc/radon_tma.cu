@@ -25,7 +25,10 @@
 // checked exactly in integer arithmetic.  The kernel re-derives each strip's
 // window start from the same corner positions and checks the width again;
 // a strip that would not fit is skipped with an error flag, never read out
-// of bounds.  Every mbarrier wait is bounded; a CTA whose wait runs out sets
+// of bounds.  The plan also fixes the order in which the (ray tile, view
+// block) CTAs are dispatched, most strips first (st_cta_order), so that the
+// launch's last wave holds its lightest CTAs.  Every mbarrier wait is
+// bounded; a CTA whose wait runs out sets
 // the error flag, waits (bounded) for its own copies and leaves.
 // expire_first (a test switch, 0 in normal use) makes each CTA's first strip
 // wait give up at once, so that tests can see that path run and report.
