@@ -94,7 +94,7 @@ inline bool test_switch(const char *name)
 
 // ----------------------------------------------------------------------------
 // Programmatic dependent launch.  The operators run as chains of short
-// kernels on one stream (an EM/OSEM sub-iteration is five or six).  A kernel
+// kernels on one stream (an EM/OSEM sub-iteration is four or five).  A kernel
 // launched by launch_pdl may be scheduled while the kernel before it on the
 // stream is still finishing its last wave: its CTAs are dispatched and reach
 // pdl_gate(), which first lets the next kernel be scheduled the same way and
