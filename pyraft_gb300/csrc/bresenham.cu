@@ -28,6 +28,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <vector>
 
 #include "rg_internal.cuh"
@@ -264,6 +265,17 @@ __device__ __forceinline__ unsigned long long round53(unsigned long long s)
     return ((s + bias) >> sh) << sh;
 }
 
+// round53 for s < 2^54, where at most one bit is dropped: m = 1 when s has
+// 54 bits, and then s + (bit 1 of s) with bit 0 cleared is the nearest even
+// multiple of 2 (ties to even); below 2^53 s is returned unchanged.  Four
+// 64-bit integer operations in place of round53's bit length and variable
+// shifts.
+__device__ __forceinline__ unsigned long long round53_small(unsigned long long s)
+{
+    const unsigned long long m = s >> 53;
+    return (s + ((s >> 1) & m)) & ~m;
+}
+
 // RN_f32(r) * 2^kq for an integer r < 2^62, built from the integer (r is
 // rounded to 24 bits, to nearest, ties to even) so that no 64-bit
 // conversion runs on the FP64 pipe.  The result is a normal float for the
@@ -347,30 +359,44 @@ __device__ __forceinline__ int dda_walk(DDA &it, int cap, int fp64_walk, Visit &
             else it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
             it.slow_move = 0;
         }
-        while (step < cap && !dda_end(it)) {
-            visit(it.i, it.j, sig(), 0);
-            ++step;
-            if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
-            const unsigned long long prev = w.E;
-            w.E = round53(w.E + w.U);
-            if (w.E <= w.D) {
-                if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32;
-                else it.sigma = it.sigma_tilde;
-                continue;
+        // Every sum the loop rounds (E + U, D - E_prev) is below D + U.  When
+        // that is below 2^54, which holds for all the rays of a view more
+        // than about 18 degrees from its fast axis, at most one bit is
+        // dropped and round53_small does it; the rays of a warp share their
+        // view, so the choice is the same across the warp.
+        auto walk = [&](auto small) {
+            constexpr bool kSmall = decltype(small)::value;
+            auto rnd = [](unsigned long long v) {
+                if constexpr (kSmall) return round53_small(v);
+                else return round53(v);
+            };
+            while (step < cap && !dda_end(it)) {
+                visit(it.i, it.j, sig(), 0);
+                ++step;
+                if (it.fast_is_i) it.i += it.Delta_fast; else it.j += it.Delta_fast;
+                const unsigned long long prev = w.E;
+                w.E = rnd(w.E + w.U);
+                if (w.E <= w.D) {
+                    if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32;
+                    else it.sigma = it.sigma_tilde;
+                    continue;
+                }
+                w.E -= w.D;                          // fl(eps - d), exact
+                const unsigned long long diff = rnd(w.D - prev);
+                if constexpr (FORM == kDdaSigma32)
+                    it.sigma32 = f32_scaled(diff, w.kq) * it.sigma_per_eps32;
+                else
+                    it.sigma = __dmul_rn(__ll2double_rn((long long)diff), sp_q);
+                if (step >= cap || dda_end(it)) break;
+                visit(it.i, it.j, sig(), 1);
+                ++step;
+                if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
+                if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32 - it.sigma32;
+                else it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
             }
-            w.E -= w.D;                          // fl(eps - d), exact
-            const unsigned long long diff = round53(w.D - prev);
-            if constexpr (FORM == kDdaSigma32)
-                it.sigma32 = f32_scaled(diff, w.kq) * it.sigma_per_eps32;
-            else
-                it.sigma = __dmul_rn(__ll2double_rn((long long)diff), sp_q);
-            if (step >= cap || dda_end(it)) break;
-            visit(it.i, it.j, sig(), 1);
-            ++step;
-            if (it.fast_is_i) it.j += it.Delta_slow; else it.i += it.Delta_slow;
-            if constexpr (FORM == kDdaSigma32) it.sigma32 = it.sigma_tilde32 - it.sigma32;
-            else it.sigma = __dsub_rn(it.sigma_tilde, it.sigma);
-        }
+        };
+        if (w.D + w.U < (1ull << 54)) walk(std::true_type{});
+        else walk(std::false_type{});
     } else {
         for (; step < cap && !dda_end(it); ++step) {
             visit(it.i, it.j, sig(), it.slow_move);

@@ -187,3 +187,54 @@ def test_branch_free_rounding_equals_round53():
         half = (1 << sh) >> 1
         bias = half - 1 + ((s >> sh) & 1) if half else 0
         assert ((s + bias) >> sh) << sh == round53(s) if s else s == 0
+
+
+def round53_small(s):
+    """bresenham.cu round53_small: round53 for s < 2^54 (at most one bit
+    dropped): m = 1 when s has 54 bits."""
+    m = s >> 53
+    return (s + ((s >> 1) & m)) & ~m
+
+
+def test_one_bit_rounding_equals_round53():
+    rng = np.random.default_rng(13)
+    vals = [0, 1, 2, (1 << 53) - 2, (1 << 53) - 1, 1 << 53, (1 << 53) + 1, (1 << 53) + 2,
+            (1 << 53) + 3, (1 << 54) - 3, (1 << 54) - 2, (1 << 54) - 1]
+    vals += [int(rng.integers(0, 1 << 54)) for _ in range(100000)]
+    vals += [(1 << 53) + int(rng.integers(0, 1 << 20)) for _ in range(20000)]
+    for s in vals:
+        assert round53_small(s) == round53(s), s
+
+
+def test_one_bit_walk_equals_fp64_walk():
+    """The rays whose D + U < 2^54 (views more than about 18 degrees from the
+    fast axis) take the one-bit rounding in the kernels: that walk, with the
+    sigma split's rounding too, against IEEE FP64 step by step."""
+    taken = 0
+    rng = np.random.default_rng(17)
+    for n in (255, 1024, 2048):
+        dx = 2.0 / (n - 1)
+        for theta in np.concatenate([np.linspace(0.0, np.pi / 4, 90)[1:], rng.random(40) * np.pi / 4]):
+            u = abs(dx * math.tan(theta))
+            for eps0 in (0.0, u / 3.0, dx * rng.random(), 0.5 * dx):
+                eps1 = first_add(u, dx, eps0)
+                if not int_path_ok(u, dx, eps1):
+                    continue
+                q = min(math.ulp(u), math.ulp(dx))
+                U, D, E = int(u / q), int(dx / q), int(eps1 / q)
+                if D + U >= 1 << 54:
+                    continue
+                want = fp64_steps(u, dx, eps1, 2 * n)
+                got = []
+                for _ in range(2 * n):
+                    prev = E
+                    E = round53_small(E + U)
+                    slow = E > D
+                    diff = None
+                    if slow:
+                        E = E - D
+                        diff = round53_small(D - prev) * q
+                    got.append((E * q, slow, diff))
+                assert got == want, (n, theta, eps0)
+                taken += 1
+    assert taken > 300
