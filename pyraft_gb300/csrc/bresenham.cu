@@ -253,16 +253,19 @@ struct DDAInt {
     int kq;        // q = 2^kq
 };
 
-// s (< 2^63) rounded to 53 significant bits, to nearest, ties to even:
-// adding half - 1 plus the kept part's lowest bit, then truncating, rounds
-// to nearest with ties to even.  No branch: sh is 0 below 2^53.
+// s rounded to 53 significant bits, to nearest, ties to even: the bits of
+// s above bit 52 (m = s >> 53; at most 8 of them in the walk, whose sums
+// stay below 2^61) say how many low bits go (sh = their count); adding
+// half - 1 plus the kept part's lowest bit and clearing the dropped bits
+// rounds to nearest with ties to even.  No branch, and besides the add's
+// carry only the low word changes: sh is 0 below 2^53.
 __device__ __forceinline__ unsigned long long round53(unsigned long long s)
 {
-    const int n = 64 - __clzll((long long)s);   // bit length (0 for s == 0)
-    const int sh = max(n - 53, 0);
-    const unsigned long long half = (1ull << sh) >> 1;
-    const unsigned long long bias = half ? half - 1 + ((s >> sh) & 1ull) : 0ull;
-    return ((s + bias) >> sh) << sh;
+    const unsigned m = (unsigned)(s >> 53);
+    const int sh = 32 - __clz((int)m);                  // 0 .. 11
+    const unsigned low = (1u << sh) - 1u;               // the dropped bits
+    const unsigned bias = (low >> 1) + ((((unsigned)s >> sh) & 1u) & (m != 0u ? 1u : 0u));
+    return (s + bias) & ~(unsigned long long)low;
 }
 
 // round53 for s < 2^54, where at most one bit is dropped: m = 1 when s has

@@ -238,3 +238,23 @@ def test_one_bit_walk_equals_fp64_walk():
                 assert got == want, (n, theta, eps0)
                 taken += 1
     assert taken > 300
+
+
+def round53_top(s):
+    """bresenham.cu round53 as the kernels compute it: the shift from the
+    bits above bit 52, the dropped bits cleared with a mask."""
+    m = s >> 53
+    sh = m.bit_length()
+    low = (1 << sh) - 1
+    bias = (low >> 1) + (((s >> sh) & 1) if m else 0)
+    return (s + bias) & ~low
+
+
+def test_mask_rounding_equals_round53():
+    rng = np.random.default_rng(19)
+    vals = [0, 1, (1 << 53) - 1, 1 << 53, (1 << 53) + 1, (1 << 54) + 2, (1 << 54) + 6,
+            (1 << 61) - 1, (1 << 61) - 256, (1 << 61) - 255, (1 << 62) + 12345, (1 << 63) - 1]
+    vals += [int(rng.integers(0, 1 << 62)) for _ in range(50000)]
+    vals += [int(rng.integers(1 << 53, 1 << 61)) for _ in range(50000)]
+    for s in vals:
+        assert round53_top(s) == round53(s), s
